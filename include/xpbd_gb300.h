@@ -1,0 +1,205 @@
+/*
+ * xpbd_gb300.h -- C ABI of the GB300-native RDC-XPBD substep (libxpbd_gb300.so).
+ *
+ * The reference (RaymondMcGuire/rdc-xpbd-taichi) exposes this path as the
+ * Python class XPBDNeoHookeanSolver (xpbd_gpu/neohookean_solver.py:16-587)
+ * over Taichi kernels; it has no FFI of its own.  Each entry point below
+ * replaces one method of that class (cited beside it), so a Python host
+ * binds them with ctypes and keeps the class interface.
+ *
+ * Conventions
+ *  - Every function returns an int status (XPBD_OK == 0).
+ *  - Device buffers are allocated by the caller (e.g. torch CUDA tensors) and
+ *    passed as raw pointers; the library never frees them.  The library owns
+ *    only a small per-solver block of device state (SDF table, FP64 Chebyshev
+ *    state, per-iteration history), released by xpbd_destroy.
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default
+ *    stream.  All work is stream-ordered; no entry point synchronises unless
+ *    it says so.
+ *  - A handle is not thread-safe; separate handles are independent.
+ *  - Vertex arrays are float4 per vertex: (x, y, z, w).  In x, p0 and p1 the w
+ *    lane carries inv_m; in dx it carries the constraint count.
+ */
+#ifndef XPBD_GB300_H
+#define XPBD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XPBD_ABI_VERSION 1
+
+enum xpbd_status {
+  XPBD_OK = 0,
+  XPBD_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, bad enum */
+  XPBD_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+  XPBD_ERR_NONFINITE = 3,        /* the residual reduction saw NaN/Inf */
+  XPBD_ERR_NO_SDF = 4,           /* xpbd_base.py:66-67 raises ValueError */
+  XPBD_ERR_BAD_MESH = 5,         /* index out of range / empty mesh */
+  XPBD_ERR_HISTORY_FULL = 6      /* more iterations than the history holds */
+};
+
+/* sdf.py:60-124 */
+enum xpbd_sdf_kind { XPBD_SDF_PLANE = 0, XPBD_SDF_SPHERE = 1, XPBD_SDF_CUBE = 2 };
+
+/* Scatter variants of the Jacobi accumulation. */
+enum xpbd_scatter { XPBD_SCATTER_ATOMIC = 0, XPBD_SCATTER_GATHER = 1 };
+
+/* One SDF obstacle (sdf.py:7-124).  48 bytes. */
+typedef struct xpbd_sdf {
+  int32_t kind;  /* xpbd_sdf_kind */
+  int32_t fixed; /* SdfModel.fixed (sdf.py:10-11) */
+  float a[3];    /* plane: point; sphere, cube: center */
+  float b[3];    /* plane: unit normal; sphere: (radius, 0, 0); cube: half size */
+  float vel[3];  /* SdfModel.vel (sdf.py:9); zero in the reference */
+  float pad;
+} xpbd_sdf;
+
+/* Solver constants (neohookean_solver.py:18-77, xpbd_base.py:26-39). */
+typedef struct xpbd_params {
+  float lame_mu;                /* calc_second_lame (neohookean_solver.py:11-12) */
+  float lame_lambda;            /* calc_first_lame (neohookean_solver.py:7-8) */
+  float gravity[3];             /* xpbd_base.py:33-34 */
+  float damping;                /* xpbd_base.py:35 */
+  float hydrostatic_relaxation; /* split mode only (neohookean_solver.py:243) */
+  float deviatoric_relaxation;  /* split mode only (neohookean_solver.py:183) */
+  float cheb_gamma;             /* neohookean_solver.py:135 */
+  int32_t cheb_enable;
+  int32_t cheb_warmup;
+  int32_t block_mode;           /* 1: block 2x2 solve, 0: split hydro + dev */
+  int32_t constraints_iter;     /* Jacobi iterations per substep */
+  int32_t monitor;              /* record mean |det F - 1|, |tr F^T F - 3| */
+  int32_t precise_hydro;        /* 1: cancellation-free det F - 1, tr F^T F - 3 */
+  int32_t scatter;              /* xpbd_scatter */
+  int32_t use_graph;            /* 1: xpbd_solve replays a cached CUDA graph */
+  double rho_min, rho_max, rho_beta; /* neohookean_solver.py:66-68 */
+} xpbd_params;
+
+/* Caller-owned device buffers of one body (already in solver vertex/tet order). */
+typedef struct xpbd_body {
+  int32_t n_verts;
+  int32_t n_tets;
+  float* x;              /* [V][4] positions, w = inv_m */
+  float* v;              /* [V][4] velocities */
+  float* p0;             /* [V][4] predicted positions (ping), w = inv_m */
+  float* p1;             /* [V][4] predicted positions (pong), w = inv_m */
+  float* dx;             /* [V][4] Jacobi accumulator; must be zero at create */
+  const int32_t* tets;   /* [T][4] vertex ids */
+  const float* dm_a;     /* [T][4] inv_Dm[0][0..2], inv_Dm[1][0] */
+  const float* dm_b;     /* [T][4] inv_Dm[1][1..2], inv_Dm[2][0..1] */
+  const float* dm_c;     /* [T][2] inv_Dm[2][2], V0 */
+  float* lam;            /* [T][2] lambda_D, lambda_H */
+  /* deterministic gather variant (XPBD_SCATTER_GATHER); may be NULL otherwise */
+  const int32_t* v2t_offsets; /* [V+1] CSR row offsets */
+  const int32_t* v2t_slots;   /* [4T] tet*4+corner, ascending per vertex */
+  float* corner_dx;           /* [4T][4] per-corner contributions */
+  /* solver vertex i is the caller's vertex vert_perm[i]; NULL = identity */
+  const int32_t* vert_perm;   /* [V] */
+} xpbd_body;
+
+/* Vertex fields addressable by xpbd_import_vec3 / xpbd_export_vec3. */
+enum xpbd_field { XPBD_FIELD_X = 0, XPBD_FIELD_V = 1, XPBD_FIELD_PRED_X = 2 };
+
+int xpbd_abi_version(void);
+const char* xpbd_status_string(int status);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* xpbd_last_error(void);
+
+/* Number of CUDA-visible devices (0 when none); never fails. */
+int xpbd_device_count(void);
+
+/* Constructor (neohookean_solver.py:18-77 after the mesh is on the device).
+ * Copies the SDF list (xpbd_base.py:60-70) and allocates the solver state.
+ * `max_records` = iterations the per-frame history can hold. */
+int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf* sdfs,
+                int32_t n_sdf, int32_t max_records, void** out_handle);
+int xpbd_destroy(void* handle);
+
+/* Replace the SDF table contents (same count as at create); synchronises
+ * `stream` first so that no queued kernel sees a partial table. */
+int xpbd_set_sdfs(void* handle, const xpbd_sdf* sdfs, int32_t n_sdf, void* stream);
+
+/* Replace constants (e.g. after the host changed damping); resets cached graphs. */
+int xpbd_set_params(void* handle, const xpbd_params* params);
+
+/* apply_external_forces (xpbd_base.py:139-146): p = x + (v += g dt) dt. */
+int xpbd_apply_external_forces(void* handle, float dt, void* stream);
+
+/* solve_sdf_collision (xpbd_base.py:162-178) on the predicted positions. */
+int xpbd_solve_sdf_collision(void* handle, float dt, void* stream);
+
+/* solve_step (neohookean_solver.py:453-560): lambda reset, SDF projection,
+ * constraints_iter Jacobi iterations with residual-driven Chebyshev.
+ * Per-iteration records go to history rows [record_base, record_base+iters). */
+int xpbd_solve_step(void* handle, float dt, int32_t record_base, void* stream);
+
+/* advance (xpbd_base.py:148-160). */
+int xpbd_advance(void* handle, float dt, float damping, void* stream);
+
+/* One substep = apply_external_forces + solve_step + advance, with predict and
+ * SDF projection fused into one vertex pass (neohookean_solver.py:577-579). */
+int xpbd_substep(void* handle, float dt, int32_t record_base, void* stream);
+
+/* solve (neohookean_solver.py:562-587): one frame, chunked by dt in float64,
+ * replayed from a cached CUDA graph. */
+int xpbd_solve(void* handle, double frame_dt, double dt, int32_t substeps, void* stream);
+
+/* Copy history rows [0, n) as {r_hat, omega, hydro_error, dev_error} doubles
+ * to host memory; synchronises `stream`. */
+int xpbd_read_history(void* handle, double* host_out, int32_t n, void* stream);
+
+/* Spectral-radius estimate rho_hat (neohookean_solver.py:65, persists across
+ * substeps); get synchronises `stream`. */
+int xpbd_get_rho_hat(void* handle, double* out, void* stream);
+int xpbd_set_rho_hat(void* handle, double value, void* stream);
+
+/* Device-to-device transfer of a vertex field in the caller's vertex order
+ * ([V][3] floats), permuting through vert_perm: the Taichi field accessors
+ * mesh.verts.<f>.from_numpy / .to_numpy (xpbd_base.py:54, renderer.py:49).
+ * Importing XPBD_FIELD_X keeps inv_m in the w lane. */
+int xpbd_import_vec3(void* handle, int32_t field, const float* src, void* stream);
+int xpbd_export_vec3(void* handle, int32_t field, float* dst, void* stream);
+
+/* Kernel classes for xpbd_read_profile. */
+enum xpbd_kernel_class {
+  XPBD_K_BEGIN = 0,    /* predict + SDF (V) */
+  XPBD_K_PROJECT = 1,  /* Neo-Hookean projection + Jacobi scatter (T) */
+  XPBD_K_GATHER = 2,   /* deterministic vertex gather (V) */
+  XPBD_K_RESIDUAL = 3, /* residual / monitoring sweep + FP64 scalars (T) */
+  XPBD_K_UPDATE = 4,   /* post_solve + Chebyshev mix (V) */
+  XPBD_K_END = 5,      /* advance (V) */
+  XPBD_K_COUNT = 6
+};
+
+/* Profiling: with `enable`, every kernel launch is bracketed by CUDA events
+ * on its stream and xpbd_solve launches directly instead of replaying its
+ * graph.  (The reference's counterpart is the host perf_counter brackets of
+ * solve_step, neohookean_solver.py:454-560.) */
+int xpbd_set_profiling(void* handle, int32_t enable);
+
+/* Accumulated device milliseconds and launch counts per kernel class
+ * (arrays of n <= XPBD_K_COUNT); synchronises `stream`; `reset` clears. */
+int xpbd_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, int32_t reset, void* stream);
+
+/* Sticky device error flags (XPBD_OK or XPBD_ERR_NONFINITE); synchronises. */
+int xpbd_check_status(void* handle, void* stream);
+
+/* Host mesh preprocessing (replaces the patcher's reorder, xpbd_base.py:42).
+ * Permutations perm[new] = old: tets in Morton (Z-order) order of their
+ * centroids; vertices in order of first use by the sorted tets (unused
+ * vertices last, in Morton order).  Either output may be NULL. */
+int xpbd_morton_order(const double* pts, int32_t n_verts, const int32_t* tets, int32_t n_tets,
+                      int32_t* vert_perm, int32_t* tet_perm);
+
+/* Vertex -> (tet*4+corner) CSR for the gather variant, slots ascending. */
+int xpbd_build_vertex_csr(const int32_t* tets, int32_t n_tets, int32_t n_verts,
+                          int32_t* offsets /* [V+1] */, int32_t* slots /* [4T] */);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XPBD_GB300_H */

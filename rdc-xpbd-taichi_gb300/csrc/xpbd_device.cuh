@@ -1,0 +1,185 @@
+// Device-side math of the RDC-XPBD substep: tet kinematics, the Neo-Hookean
+// constraint pair, the 2x2 pivoted LU and the SDF obstacles.  FP32 throughout
+// (the reference's arithmetic type); callers reduce in FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/xpbd_gb300.h"
+
+namespace xpbd {
+
+// xpbd_gpu/constants.py:3
+constexpr float kEps = 1e-12f;
+
+struct Tet {
+  float4 p[4];    // gathered predicted positions, w = inv_m
+  float dm[9];    // inv_Dm row-major
+  float V0;
+};
+
+// F = Ds * inv_Dm with Ds = [p1-p0, p2-p0, p3-p0] as columns
+// (neohookean_solver.py:371-373).  F[r*3+c].
+__device__ __forceinline__ void deformation_gradient(const Tet& t, float F[9]) {
+  const float e[3][3] = {
+      {t.p[1].x - t.p[0].x, t.p[2].x - t.p[0].x, t.p[3].x - t.p[0].x},
+      {t.p[1].y - t.p[0].y, t.p[2].y - t.p[0].y, t.p[3].y - t.p[0].y},
+      {t.p[1].z - t.p[0].z, t.p[2].z - t.p[0].z, t.p[3].z - t.p[0].z}};
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      F[r * 3 + c] = e[r][0] * t.dm[0 * 3 + c] + e[r][1] * t.dm[1 * 3 + c] + e[r][2] * t.dm[2 * 3 + c];
+}
+
+// C_D = tr(F^T F) - 3 and C_H = det F - 1 (neohookean_solver.py:376-380).
+// kPrecise evaluates both through G = F - I:
+//   tr(F^T F) - 3 = 2 tr G + |G|^2,
+//   det(I + G) - 1 = tr G + (sum of principal 2x2 minors of G) + det G,
+// which avoids the cancellation against 3 and 1 when F is near a rotation-free
+// isochoric state (nu -> 0.5).
+template <bool kPrecise>
+__device__ __forceinline__ void invariants(const float F[9], float& C_D, float& C_H) {
+  if (kPrecise) {
+    const float g00 = F[0] - 1.f, g11 = F[4] - 1.f, g22 = F[8] - 1.f;
+    const float g01 = F[1], g02 = F[2], g10 = F[3], g12 = F[5], g20 = F[6], g21 = F[7];
+    const float tr = g00 + g11 + g22;
+    const float gg = g00 * g00 + g01 * g01 + g02 * g02 + g10 * g10 + g11 * g11 + g12 * g12 +
+                     g20 * g20 + g21 * g21 + g22 * g22;
+    C_D = 2.f * tr + gg;
+    const float m2 = (g00 * g11 - g01 * g10) + (g00 * g22 - g02 * g20) + (g11 * g22 - g12 * g21);
+    const float detG = g00 * (g11 * g22 - g21 * g12) - g10 * (g01 * g22 - g21 * g02) +
+                       g20 * (g01 * g12 - g11 * g02);
+    C_H = tr + (m2 + detG);
+  } else {
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) s += F[i] * F[i];
+    C_D = s - 3.f;
+    // cofactor expansion along the first column
+    const float det = F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
+                      F[6] * (F[1] * F[5] - F[4] * F[2]);
+    C_H = det - 1.f;
+  }
+}
+
+// Corner gradients g_{c+1}[r] = sum_k gradF[r][k] * inv_Dm[c][k]
+// (grad123 = gradF * inv_Dm^T, neohookean_solver.py:382-404); g0 = -(g1+g2+g3).
+__device__ __forceinline__ void corner_gradients(const float gF[9], const float dm[9], float3 g[4]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    g[c + 1].x = gF[0] * dm[c * 3 + 0] + gF[1] * dm[c * 3 + 1] + gF[2] * dm[c * 3 + 2];
+    g[c + 1].y = gF[3] * dm[c * 3 + 0] + gF[4] * dm[c * 3 + 1] + gF[5] * dm[c * 3 + 2];
+    g[c + 1].z = gF[6] * dm[c * 3 + 0] + gF[7] * dm[c * 3 + 1] + gF[8] * dm[c * 3 + 2];
+  }
+  g[0].x = -(g[1].x + g[2].x + g[3].x);
+  g[0].y = -(g[1].y + g[2].y + g[3].y);
+  g[0].z = -(g[1].z + g[2].z + g[3].z);
+}
+
+// dC_H/dF = [F1 x F2, F2 x F0, F0 x F1] as columns (neohookean_solver.py:391-398).
+__device__ __forceinline__ void cofactor(const float F[9], float H[9]) {
+  // column j of F: (F[j], F[3+j], F[6+j])
+  const float3 c0 = make_float3(F[0], F[3], F[6]);
+  const float3 c1 = make_float3(F[1], F[4], F[7]);
+  const float3 c2 = make_float3(F[2], F[5], F[8]);
+  const float3 x0 = make_float3(c1.y * c2.z - c1.z * c2.y, c1.z * c2.x - c1.x * c2.z, c1.x * c2.y - c1.y * c2.x);
+  const float3 x1 = make_float3(c2.y * c0.z - c2.z * c0.y, c2.z * c0.x - c2.x * c0.z, c2.x * c0.y - c2.y * c0.x);
+  const float3 x2 = make_float3(c0.y * c1.z - c0.z * c1.y, c0.z * c1.x - c0.x * c1.z, c0.x * c1.y - c0.y * c1.x);
+  H[0] = x0.x; H[1] = x1.x; H[2] = x2.x;
+  H[3] = x0.y; H[4] = x1.y; H[5] = x2.y;
+  H[6] = x0.z; H[7] = x1.z; H[8] = x2.z;
+}
+
+__device__ __forceinline__ float dot3(const float3 a, const float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// solve2x2_pivot_lu (neohookean_solver.py:331-356); returns ok.
+__device__ __forceinline__ bool solve2x2_pivot_lu(float A00, float A01, float A10, float A11, float b0, float b1,
+                                                  float& x0, float& x1) {
+  if (fabsf(A00) < fabsf(A10)) {
+    float t = A00; A00 = A10; A10 = t;
+    t = A01; A01 = A11; A11 = t;
+    t = b0; b0 = b1; b1 = t;
+  }
+  x0 = 0.f;
+  x1 = 0.f;
+  if (fabsf(A00) < kEps) return false;
+  const float m = A10 / A00;
+  const float A11_ = A11 - m * A01;
+  const float b1_ = b1 - m * b0;
+  if (fabsf(A11_) < kEps) return false;
+  x1 = b1_ / A11_;
+  x0 = (b0 - A01 * x1) / A00;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// SDFs (sdf.py)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float sdf_dist(const xpbd_sdf& s, const float3 p) {
+  if (s.kind == XPBD_SDF_PLANE) {  // sdf.py:68-70
+    return (p.x - s.a[0]) * s.b[0] + (p.y - s.a[1]) * s.b[1] + (p.z - s.a[2]) * s.b[2];
+  }
+  if (s.kind == XPBD_SDF_SPHERE) {  // sdf.py:86-88
+    const float dx = p.x - s.a[0], dy = p.y - s.a[1], dz = p.z - s.a[2];
+    return sqrtf(dx * dx + dy * dy + dz * dz) - s.b[0];
+  }
+  // XPBD_SDF_CUBE, sdf.py:107-110
+  const float dx = fabsf(p.x - s.a[0]) - s.b[0];
+  const float dy = fabsf(p.y - s.a[1]) - s.b[1];
+  const float dz = fabsf(p.z - s.a[2]) - s.b[2];
+  const float mx = fmaxf(dx, 0.f), my = fmaxf(dy, 0.f), mz = fmaxf(dz, 0.f);
+  return sqrtf(mx * mx + my * my + mz * mz) + fminf(fmaxf(dx, fmaxf(dy, dz)), 0.f);
+}
+
+__device__ __forceinline__ float3 sdf_normal(const xpbd_sdf& s, const float3 p) {
+  if (s.kind == XPBD_SDF_PLANE) return make_float3(s.b[0], s.b[1], s.b[2]);  // sdf.py:72-74
+  const float dx = p.x - s.a[0], dy = p.y - s.a[1], dz = p.z - s.a[2];
+  if (s.kind == XPBD_SDF_SPHERE) {  // sdf.py:90-92: v * 1 / (|v| + eps)
+    const float inv = 1.f / (sqrtf(dx * dx + dy * dy + dz * dz) + kEps);
+    return make_float3(dx * inv, dy * inv, dz * inv);
+  }
+  // sdf.py:112-124: sign of the dominant axis of (p - c)
+  const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+  int axis = 0;
+  float amax = ax;
+  if (ay > ax) { axis = 1; amax = ay; }
+  if (az > amax) axis = 2;
+  float3 n = make_float3(0.f, 0.f, 0.f);
+  if (axis == 0) n.x = dx > 0.f ? 1.f : -1.f;
+  else if (axis == 1) n.y = dy > 0.f ? 1.f : -1.f;
+  else n.z = dz > 0.f ? 1.f : -1.f;
+  return n;
+}
+
+// _solve_sdf_collision_one + SdfModel.check (xpbd_base.py:162-174, sdf.py:14-27)
+// for one live vertex; SDFs are applied sequentially in list order.
+__device__ __forceinline__ void sdf_project_all(const xpbd_sdf* __restrict__ sdfs, int n_sdf, float3& p,
+                                                const float3 vel) {
+  for (int s = 0; s < n_sdf; ++s) {
+    const xpbd_sdf sd = sdfs[s];
+    const float phi = sdf_dist(sd, p);
+    if (phi < 0.f) {
+      const float3 n = sdf_normal(sd, p);
+      const float dotnv = n.x * (sd.vel[0] - vel.x) + n.y * (sd.vel[1] - vel.y) + n.z * (sd.vel[2] - vel.z);
+      if (dotnv > 0.f || sd.fixed) {
+        const float pen = -sdf_dist(sd, p);
+        if (pen > 0.f) {
+          p.x += n.x * pen;
+          p.y += n.y * pen;
+          p.z += n.z * pen;
+        }
+      }
+    }
+  }
+}
+
+// Vector reduction into global memory: red.global.add.v4.f32 (sm_90+).
+__device__ __forceinline__ void red_add_v4(float4* addr, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
+               : "memory");
+}
+
+}  // namespace xpbd

@@ -1,0 +1,124 @@
+// Host mesh preprocessing for the GB300 solver.
+//
+// The reference obtains its mesh from meshtaichi_patcher (xpbd_base.py:42),
+// whose patch partition + reorder serves Taichi's mesh_local staging.  Here the
+// mesh is reordered along a Z-order (Morton) curve so that the tet sweep's
+// vertex gathers and the Jacobi scatter hit nearby cache lines, and a
+// vertex -> (tet, corner) CSR is built for the deterministic gather variant.
+#include <algorithm>
+#include <cstdint>
+#include <numeric>
+#include <vector>
+
+#include "../../include/xpbd_gb300.h"
+
+namespace {
+
+// Spread the low 21 bits of v so that bit i lands at bit 3i.
+inline uint64_t spread3(uint64_t v) {
+  v &= 0x1fffffull;
+  v = (v | (v << 32)) & 0x1f00000000ffffull;
+  v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+  v = (v | (v << 8)) & 0x100f00f00f00f00full;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
+
+struct Box {
+  double lo[3], scale[3];
+};
+
+inline uint64_t morton(const Box& b, double x, double y, double z) {
+  const double q[3] = {(x - b.lo[0]) * b.scale[0], (y - b.lo[1]) * b.scale[1], (z - b.lo[2]) * b.scale[2]};
+  uint64_t c[3];
+  for (int k = 0; k < 3; ++k) {
+    double v = q[k];
+    if (!(v > 0.0)) v = 0.0;
+    if (v > 2097151.0) v = 2097151.0;
+    c[k] = (uint64_t)v;
+  }
+  return spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
+}
+
+void order_by(const std::vector<uint64_t>& code, int32_t* perm) {
+  const size_t n = code.size();
+  std::vector<int32_t> idx(n);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return code[a] < code[b]; });
+  std::copy(idx.begin(), idx.end(), perm);
+}
+
+}  // namespace
+
+extern "C" {
+
+int xpbd_morton_order(const double* pts, int32_t n_verts, const int32_t* tets, int32_t n_tets, int32_t* vert_perm,
+                      int32_t* tet_perm) {
+  if (!pts || n_verts <= 0 || n_tets < 0 || (n_tets > 0 && !tets)) return XPBD_ERR_INVALID_ARGUMENT;
+  for (int64_t k = 0; k < 4ll * n_tets; ++k)
+    if (tets[k] < 0 || tets[k] >= n_verts) return XPBD_ERR_BAD_MESH;
+  Box b;
+  for (int k = 0; k < 3; ++k) {
+    double lo = pts[k], hi = pts[k];
+    for (int32_t i = 1; i < n_verts; ++i) {
+      lo = std::min(lo, pts[3 * i + k]);
+      hi = std::max(hi, pts[3 * i + k]);
+    }
+    b.lo[k] = lo;
+    b.scale[k] = hi > lo ? 2097151.0 / (hi - lo) : 0.0;
+  }
+  if (tet_perm && n_tets > 0) {
+    std::vector<uint64_t> code(n_tets);
+    for (int32_t t = 0; t < n_tets; ++t) {
+      double c[3] = {0.0, 0.0, 0.0};
+      for (int q = 0; q < 4; ++q) {
+        const int32_t v = tets[4 * t + q];
+        if (v < 0 || v >= n_verts) return XPBD_ERR_BAD_MESH;
+        for (int k = 0; k < 3; ++k) c[k] += 0.25 * pts[3 * v + k];
+      }
+      code[t] = morton(b, c[0], c[1], c[2]);
+    }
+    order_by(code, tet_perm);
+  }
+  if (vert_perm) {
+    // Vertices are numbered in order of first use by the Morton-sorted tets,
+    // so the corners of consecutive tets are close in memory; vertices no tet
+    // uses follow in Morton order of their positions.
+    std::vector<uint64_t> code(n_verts);
+    for (int32_t i = 0; i < n_verts; ++i) code[i] = morton(b, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+    std::vector<int32_t> by_code(n_verts);
+    order_by(code, by_code.data());
+    std::vector<char> seen(n_verts, 0);
+    int32_t k = 0;
+    if (tet_perm) {
+      for (int32_t t = 0; t < n_tets; ++t)
+        for (int q = 0; q < 4; ++q) {
+          const int32_t v = tets[4 * tet_perm[t] + q];
+          if (!seen[v]) {
+            seen[v] = 1;
+            vert_perm[k++] = v;
+          }
+        }
+    }
+    for (int32_t i = 0; i < n_verts; ++i)
+      if (!seen[by_code[i]]) vert_perm[k++] = by_code[i];
+  }
+  return XPBD_OK;
+}
+
+int xpbd_build_vertex_csr(const int32_t* tets, int32_t n_tets, int32_t n_verts, int32_t* offsets, int32_t* slots) {
+  if (!tets || !offsets || !slots || n_tets < 0 || n_verts <= 0) return XPBD_ERR_INVALID_ARGUMENT;
+  std::fill(offsets, offsets + n_verts + 1, 0);
+  for (int64_t k = 0; k < 4ll * n_tets; ++k) {
+    const int32_t v = tets[k];
+    if (v < 0 || v >= n_verts) return XPBD_ERR_BAD_MESH;
+    offsets[v + 1]++;
+  }
+  for (int32_t v = 0; v < n_verts; ++v) offsets[v + 1] += offsets[v];
+  std::vector<int32_t> fill(offsets, offsets + n_verts);
+  for (int64_t k = 0; k < 4ll * n_tets; ++k) slots[fill[tets[k]]++] = (int32_t)k;
+  return XPBD_OK;
+}
+
+}  // extern "C"

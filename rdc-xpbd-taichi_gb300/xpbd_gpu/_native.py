@@ -1,0 +1,187 @@
+"""Build and load ``libxpbd_gb300.so`` (hand-written sm_103a CUDA + C ABI).
+
+The library is compiled in-tree with nvcc (``build()``) and bound with
+ctypes.  The structures below mirror ``include/xpbd_gb300.h`` field for
+field.  There is no CPU fallback: ``load()`` raises if the library is missing
+and the solver classes raise if no CUDA device is visible.
+"""
+import ctypes
+import os
+import subprocess
+import threading
+from concurrent.futures import ThreadPoolExecutor
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+SRC_DIR = os.path.join(os.path.dirname(PKG_DIR), "csrc")
+REPO_DIR = os.path.dirname(os.path.dirname(PKG_DIR))
+INCLUDE_DIR = os.path.join(REPO_DIR, "include")
+LIB_NAME = "libxpbd_gb300.so"
+LIB_PATH = os.path.join(PKG_DIR, LIB_NAME)
+BUILD_DIR = os.path.join(os.path.dirname(PKG_DIR), "_build")
+
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
+SOURCES = ["xpbd_solver.cu", "xpbd_mesh.cpp"]
+
+XPBD_OK = 0
+STATUS_NAMES = {
+    0: "XPBD_OK", 1: "XPBD_ERR_INVALID_ARGUMENT", 2: "XPBD_ERR_CUDA",
+    3: "XPBD_ERR_NONFINITE", 4: "XPBD_ERR_NO_SDF", 5: "XPBD_ERR_BAD_MESH",
+    6: "XPBD_ERR_HISTORY_FULL",
+}
+SDF_PLANE, SDF_SPHERE, SDF_CUBE = 0, 1, 2
+SCATTER_ATOMIC, SCATTER_GATHER = 0, 1
+FIELD_X, FIELD_V, FIELD_PRED_X = 0, 1, 2
+KERNEL_CLASSES = ("begin", "project", "gather", "residual", "update", "end")
+
+
+class XpbdSdf(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("fixed", ctypes.c_int32),
+                ("a", ctypes.c_float * 3), ("b", ctypes.c_float * 3),
+                ("vel", ctypes.c_float * 3), ("pad", ctypes.c_float)]
+
+
+class XpbdParams(ctypes.Structure):
+    _fields_ = [("lame_mu", ctypes.c_float), ("lame_lambda", ctypes.c_float),
+                ("gravity", ctypes.c_float * 3), ("damping", ctypes.c_float),
+                ("hydrostatic_relaxation", ctypes.c_float),
+                ("deviatoric_relaxation", ctypes.c_float),
+                ("cheb_gamma", ctypes.c_float),
+                ("cheb_enable", ctypes.c_int32), ("cheb_warmup", ctypes.c_int32),
+                ("block_mode", ctypes.c_int32), ("constraints_iter", ctypes.c_int32),
+                ("monitor", ctypes.c_int32), ("precise_hydro", ctypes.c_int32),
+                ("scatter", ctypes.c_int32), ("use_graph", ctypes.c_int32),
+                ("rho_min", ctypes.c_double), ("rho_max", ctypes.c_double),
+                ("rho_beta", ctypes.c_double)]
+
+
+_P = ctypes.c_void_p
+
+
+class XpbdBody(ctypes.Structure):
+    _fields_ = [("n_verts", ctypes.c_int32), ("n_tets", ctypes.c_int32),
+                ("x", _P), ("v", _P), ("p0", _P), ("p1", _P), ("dx", _P),
+                ("tets", _P), ("dm_a", _P), ("dm_b", _P), ("dm_c", _P), ("lam", _P),
+                ("v2t_offsets", _P), ("v2t_slots", _P), ("corner_dx", _P),
+                ("vert_perm", _P)]
+
+
+# name -> (restype, argtypes); every symbol declared in include/xpbd_gb300.h
+_SIGNATURES = {
+    "xpbd_abi_version": (ctypes.c_int, []),
+    "xpbd_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "xpbd_last_error": (ctypes.c_char_p, []),
+    "xpbd_device_count": (ctypes.c_int, []),
+    "xpbd_create": (ctypes.c_int, [ctypes.POINTER(XpbdParams), ctypes.POINTER(XpbdBody),
+                                   ctypes.POINTER(XpbdSdf), ctypes.c_int32, ctypes.c_int32,
+                                   ctypes.POINTER(ctypes.c_void_p)]),
+    "xpbd_destroy": (ctypes.c_int, [_P]),
+    "xpbd_set_params": (ctypes.c_int, [_P, ctypes.POINTER(XpbdParams)]),
+    "xpbd_set_sdfs": (ctypes.c_int, [_P, ctypes.POINTER(XpbdSdf), ctypes.c_int32, _P]),
+    "xpbd_apply_external_forces": (ctypes.c_int, [_P, ctypes.c_float, _P]),
+    "xpbd_solve_sdf_collision": (ctypes.c_int, [_P, ctypes.c_float, _P]),
+    "xpbd_solve_step": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int32, _P]),
+    "xpbd_advance": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, _P]),
+    "xpbd_substep": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int32, _P]),
+    "xpbd_solve": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_int32, _P]),
+    "xpbd_read_history": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, _P]),
+    "xpbd_get_rho_hat": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _P]),
+    "xpbd_set_rho_hat": (ctypes.c_int, [_P, ctypes.c_double, _P]),
+    "xpbd_import_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
+    "xpbd_export_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
+    "xpbd_check_status": (ctypes.c_int, [_P, _P]),
+    "xpbd_set_profiling": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "xpbd_read_profile": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
+                                         ctypes.c_int32, ctypes.c_int32, _P]),
+    "xpbd_morton_order": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int32, _P, _P]),
+    "xpbd_build_vertex_csr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def _nvcc():
+    cand = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    return cand if os.path.exists(cand) else "nvcc"
+
+
+def _stale():
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    deps = [os.path.join(SRC_DIR, f) for f in os.listdir(SRC_DIR)]
+    deps.append(os.path.join(INCLUDE_DIR, "xpbd_gb300.h"))
+    return any(os.path.getmtime(p) > t for p in deps)
+
+
+def build(force=False, verbose=False):
+    """Compile the CUDA/C++ sources for sm_103a into ``libxpbd_gb300.so``.
+
+    Translation units compile in parallel; the link is a shared library with
+    the CUDA runtime linked statically.  Returns the library path.
+    """
+    if not force and not _stale():
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    nvcc = _nvcc()
+    objs = []
+
+    def compile_one(src):
+        obj = os.path.join(BUILD_DIR, src + ".o")
+        cmd = [nvcc] + ARCH_FLAGS + NVCC_FLAGS + ["-I", INCLUDE_DIR, "-c",
+                                                  os.path.join(SRC_DIR, src), "-o", obj]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))
+        if verbose and r.stderr:
+            print(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    tmp = LIB_PATH + ".tmp"
+    cmd = [nvcc] + ARCH_FLAGS + ["-shared", "-o", tmp] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def load():
+    """Load the library (building it first if it is missing or stale)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if _stale():
+            build()
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        if lib.xpbd_abi_version() != 1:
+            raise RuntimeError("libxpbd_gb300.so ABI mismatch")
+        _lib = lib
+        return lib
+
+
+class XpbdError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%d): %s" % (STATUS_NAMES.get(status, "?"), status, msg))
+        self.status = status
+
+
+def check(status):
+    """Raise for a non-zero status with the library's last error message."""
+    if status == XPBD_OK:
+        return
+    lib = load()
+    msg = lib.xpbd_last_error().decode() or lib.xpbd_status_string(status).decode()
+    if status == 4:  # XPBD_ERR_NO_SDF mirrors xpbd_base.py:66-67
+        raise ValueError(msg)
+    raise XpbdError(status, msg)

@@ -1,0 +1,274 @@
+"""XPBDNeoHookeanSolver: residual-driven Chebyshev Jacobi block Neo-Hookean XPBD.
+
+Drop-in for the reference class (``xpbd_gpu/neohookean_solver.py:16-587``):
+same constructor arguments, ``solve()`` / ``solve_step(dt)``, monitoring
+attributes (``convergence_history``, ``convergence_callback``,
+``monitor_convergence``, ``current_frame``/``current_substep``), timing
+attributes (``solve_compute_time_total/calls/iterations``) and the
+Chebyshev state (``rho_hat`` persists across substeps and frames).
+
+Every substep runs on the GPU as hand-written sm_103a kernels
+(``libxpbd_gb300.so``, ``include/xpbd_gb300.h``).  The residual r_hat, the
+spectral-radius estimate rho_hat and the omega recurrence are evaluated on
+the device in FP64, so a frame needs no host round trip; ``solve()`` replays
+one cached CUDA graph per frame.  With ``monitor_convergence`` the frame is
+driven substep by substep so that ``convergence_callback`` fires after each
+substep, as in the reference (:574-583).
+
+Extensions (keyword-only): ``total_mass`` / ``density`` (the reference fixes
+1 kg, xpbd_base.py:36), ``gravity``, ``scatter`` ('atomic' = vector
+red.global.add, 'gather' = deterministic vertex->tet CSR), ``precise_hydro``
+(cancellation-free det F - 1; default on for poisson_ratio >= 0.49),
+``use_graph`` and ``reorder`` (Morton order on the device).
+"""
+import numpy as np
+
+from xpbd_gpu import _native
+from xpbd_gpu.xpbd_base import XPBDSolverBase, _torch, calc_tet_volume  # noqa: F401
+
+
+def calc_first_lame(E, nu):
+    """neohookean_solver.py:7-8."""
+    return 2.0 * nu / (1.0 - 2.0 * nu) * calc_second_lame(E, nu)
+
+
+def calc_second_lame(E, nu):
+    """neohookean_solver.py:11-12."""
+    return E / (2.0 * (1.0 + nu))
+
+
+def frame_chunks(frame_dt, dt):
+    """dt0 of each chunk of one frame, in float64 (neohookean_solver.py:563-568)."""
+    out = []
+    left = frame_dt
+    while left > 0.0:
+        d = min(dt, left)
+        left -= d
+        out.append(d)
+    return out
+
+
+class XPBDNeoHookeanSolver(XPBDSolverBase):
+
+    def __init__(self, rest_pose, sdf, young_modulus=200000.0, poisson_ratio=0.495, scale=1.0,
+                 offset=(0.0, 0.0, 0.0), frame_dt=1e-2, dt=1e-2, substeps_num=20, constraints_iter=5,
+                 reorder_all=False, block_size=256, hydrostatic_relaxation=1.2, deviatoric_relaxation=1.2,
+                 cheb_enable=True, cheb_warmup=5, cheb_gamma=0.6666, block_neohookean_enable=False,
+                 monitor_convergence=False, *, total_mass=1.0, density=None, gravity=(0.0, -9.8, 0.0),
+                 scatter="atomic", precise_hydro=None, use_graph=True, reorder=True):
+        self.constraints_iter = constraints_iter
+        self.hydrostatic_relaxation = hydrostatic_relaxation
+        self.deviatoric_relaxation = deviatoric_relaxation
+        self.young_modulus = young_modulus
+        self.poisson_ratio = poisson_ratio
+        self.lame1 = calc_first_lame(young_modulus, poisson_ratio)
+        self.lame2 = calc_second_lame(young_modulus, poisson_ratio)
+        self.cheb_enable = cheb_enable
+        self.cheb_gamma = cheb_gamma
+        self.cheb_warmup = cheb_warmup
+        self.block_neohookean_enable = block_neohookean_enable
+        self.monitor_convergence = monitor_convergence
+        self.convergence_history = []
+        self.current_substep_convergence = []
+        self.current_frame = 0
+        self.current_substep = 0
+        self.convergence_callback = None
+        self.rho_min = 0.00001  # :66-68
+        self.rho_max = 0.99999
+        self.rho_beta = 0.2
+        self.prev_r_hat = None
+        self._timing_events = []
+        self._time_done = 0.0
+        self.solve_compute_calls = 0
+        self.solve_compute_iterations = 0
+        if scatter not in ("atomic", "gather"):
+            raise ValueError("scatter must be 'atomic' or 'gather'")
+        self.scatter = scatter
+        self.precise_hydro = (poisson_ratio >= 0.49) if precise_hydro is None else bool(precise_hydro)
+        self.use_graph = bool(use_graph)
+        self.block_size = block_size
+        super().__init__(rest_pose, sdf, scale, offset, frame_dt, dt, substeps_num, reorder_all, block_size,
+                         total_mass=total_mass, density=density, gravity=gravity, reorder=reorder)
+
+    # -- construction (neohookean_solver.py:79-95) ------------------------------
+    def initialize_specific(self, scale, offset):
+        x, V0, inv_Dm = self.initialize(scale, offset)
+        m, inv_m = self.compute_lumped_mass(x, V0)
+        self._upload(x, V0, inv_Dm, m, inv_m)
+        if self.scatter == "gather":
+            self._ensure_gather_buffers()
+        self._build_mesh_view()
+        self._max_records = max(1, self._records_per_frame())
+        prm = self._params()
+        self._prm_bytes = bytes(prm)
+        h = _native.ctypes.c_void_p()
+        table = self._sdf_table()
+        body = self._body()
+        _native.check(self._lib.xpbd_create(prm, body, table, len(self.sdfs), self._max_records,
+                                            _native.ctypes.byref(h)))
+        self._handle = h.value
+
+    def _records_per_frame(self):
+        return len(frame_chunks(self.frame_dt, self.dt)) * self.substeps_num * self.constraints_iter
+
+    def _params(self):
+        p = _native.XpbdParams()
+        p.lame_mu = self.lame2
+        p.lame_lambda = self.lame1
+        p.gravity[:] = [float(g) for g in np.asarray(self.gravity, dtype=np.float64).reshape(3)]
+        p.damping = self.damping
+        p.hydrostatic_relaxation = self.hydrostatic_relaxation
+        p.deviatoric_relaxation = self.deviatoric_relaxation
+        p.cheb_gamma = self.cheb_gamma
+        p.cheb_enable = 1 if self.cheb_enable else 0
+        p.cheb_warmup = int(self.cheb_warmup)
+        p.block_mode = 1 if self.block_neohookean_enable else 0
+        p.constraints_iter = int(self.constraints_iter)
+        p.monitor = 1 if self.monitor_convergence else 0
+        p.precise_hydro = 1 if self.precise_hydro else 0
+        p.scatter = _native.SCATTER_GATHER if self.scatter == "gather" else _native.SCATTER_ATOMIC
+        p.use_graph = 1 if self.use_graph else 0
+        p.rho_min, p.rho_max, p.rho_beta = self.rho_min, self.rho_max, self.rho_beta
+        return p
+
+    def _sync(self):
+        super()._sync()
+        if self.scatter == "gather" and self._corner is None:
+            raise RuntimeError("scatter='gather' needs the CSR buffers built at construction")
+        prm = self._params()
+        b = bytes(prm)
+        if b != self._prm_bytes:
+            _native.check(self._lib.xpbd_set_params(self._handle, prm))
+            self._prm_bytes = b
+
+    # -- Chebyshev state ---------------------------------------------------------
+    @property
+    def rho_hat(self):
+        out = _native.ctypes.c_double()
+        _native.check(self._lib.xpbd_get_rho_hat(self._handle, _native.ctypes.byref(out), self._stream()))
+        return out.value
+
+    @rho_hat.setter
+    def rho_hat(self, value):
+        if getattr(self, "_handle", None) is None:
+            return  # set by the reference's constructor order; device starts at 0.999
+        _native.check(self._lib.xpbd_set_rho_hat(self._handle, float(value), self._stream()))
+
+    # -- timing attributes (neohookean_solver.py:71-73, :558-560) --------------
+    @property
+    def solve_compute_time_total(self):
+        if self._timing_events:
+            for a, b in self._timing_events:
+                b.synchronize()
+                self._time_done += a.elapsed_time(b) * 1e-3
+            self._timing_events = []
+        return self._time_done
+
+    def _events(self):
+        torch = _torch()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        return a, b
+
+    # -- history ------------------------------------------------------------------
+    def read_history(self, n=None):
+        """(n, 4) float64 rows {r_hat, omega, hydro_error, dev_error} of the last
+        frame (or of the last solve_step), in iteration order."""
+        n = self._max_records if n is None else int(n)
+        out = np.zeros((n, 4), dtype=np.float64)
+        if n:
+            _native.check(self._lib.xpbd_read_history(
+                self._handle, out.ctypes.data_as(_native.ctypes.POINTER(_native.ctypes.c_double)), n,
+                self._stream()))
+        return out
+
+    def set_profiling(self, enable):
+        """Bracket every kernel launch with CUDA events (frames then launch
+        directly instead of replaying the graph)."""
+        _native.check(self._lib.xpbd_set_profiling(self._handle, 1 if enable else 0))
+
+    def read_profile(self, reset=False):
+        """{kernel class: {'ms': total device ms, 'launches': n}} since the last reset."""
+        n = len(_native.KERNEL_CLASSES)
+        ms = (_native.ctypes.c_double * n)()
+        cnt = (_native.ctypes.c_int64 * n)()
+        _native.check(self._lib.xpbd_read_profile(self._handle, ms, cnt, n, 1 if reset else 0, self._stream()))
+        return {k: {"ms": ms[i], "launches": int(cnt[i])} for i, k in enumerate(_native.KERNEL_CLASSES)}
+
+    def check_status(self):
+        """Raise if a residual reduction produced NaN/Inf (sticky device flag)."""
+        _native.check(self._lib.xpbd_check_status(self._handle, self._stream()))
+
+    def _records_to_history(self, rows):
+        K = self.constraints_iter
+        for it in range(K):
+            rec = dict(frame=self.current_frame, substep=self.current_substep, iter=it,
+                       iter_compute_time_sec=0.0, hydro_error=float(rows[it, 2]),
+                       dev_error=float(rows[it, 3]))
+            self.convergence_history.append(rec)
+            self.current_substep_convergence.append(rec)
+
+    # -- stepping -------------------------------------------------------------------
+    def solve_step(self, dt):
+        """neohookean_solver.py:453-560 (predicted positions must be set, e.g. by
+        apply_external_forces)."""
+        self._sync()
+        a, b = self._events()
+        a.record()
+        _native.check(self._lib.xpbd_solve_step(self._handle, float(dt), 0, self._stream()))
+        b.record()
+        self._timing_events.append((a, b))
+        self.solve_compute_calls += 1
+        self.solve_compute_iterations += self.constraints_iter
+        if self.monitor_convergence:
+            rows = self.read_history(self.constraints_iter)
+            t_it = a.elapsed_time(b) * 1e-3 / max(1, self.constraints_iter)
+            start = len(self.convergence_history)
+            self._records_to_history(rows)
+            for r in self.convergence_history[start:]:
+                r["iter_compute_time_sec"] = t_it
+        if self.cheb_enable and self.constraints_iter > 0:
+            self.prev_r_hat = float(self.read_history(self.constraints_iter)[-1, 0])
+
+    def solve(self):
+        """neohookean_solver.py:562-587: one frame."""
+        self._sync()
+        stream = self._stream()
+        self.current_substep = 0
+        if not self.monitor_convergence:
+            a, b = self._events()
+            a.record()
+            _native.check(self._lib.xpbd_solve(self._handle, float(self.frame_dt), float(self.dt),
+                                               int(self.substeps_num), stream))
+            b.record()
+            self._timing_events.append((a, b))
+            chunks = frame_chunks(self.frame_dt, self.dt)
+            self.solve_compute_calls += len(chunks) * self.substeps_num
+            self.solve_compute_iterations += len(chunks) * self.substeps_num * self.constraints_iter
+            self.time += sum(chunks)
+            if chunks:
+                self.current_substep = self.substeps_num - 1
+            self.current_frame += 1
+            return
+        for dt0 in frame_chunks(self.frame_dt, self.dt):
+            sub_dt = dt0 / self.substeps_num
+            for substep in range(self.substeps_num):
+                self.current_substep = substep
+                self.current_substep_convergence = []
+                a, b = self._events()
+                a.record()
+                _native.check(self._lib.xpbd_substep(self._handle, float(sub_dt), 0, stream))
+                b.record()
+                self._timing_events.append((a, b))
+                self.solve_compute_calls += 1
+                self.solve_compute_iterations += self.constraints_iter
+                rows = self.read_history(self.constraints_iter)
+                t_it = a.elapsed_time(b) * 1e-3 / max(1, self.constraints_iter)
+                self._records_to_history(rows)
+                for r in self.current_substep_convergence:
+                    r["iter_compute_time_sec"] = t_it
+                if self.convergence_callback:
+                    self.convergence_callback(self.current_frame, self.current_substep,
+                                              self.current_substep_convergence)
+            self.time += dt0
+        self.current_frame += 1

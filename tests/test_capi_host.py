@@ -1,0 +1,112 @@
+"""C ABI checks that need no GPU: the library loads, exports every function
+declared in include/xpbd_gb300.h, and the host-only entry points and error
+paths behave."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from xpbd_gpu import _native
+from xpbd_gpu.mesh import kuhn_grid
+
+HEADER = os.path.join(ROOT, "include", "xpbd_gb300.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(xpbd_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_bound_functions():
+    assert set(declared_functions()) == set(_native._SIGNATURES)
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    for name in declared_functions():
+        assert hasattr(native_lib, name), name
+    assert native_lib.xpbd_abi_version() == 1
+
+
+def test_status_strings(native_lib):
+    assert native_lib.xpbd_status_string(0) == b"ok"
+    assert b"SDF" in native_lib.xpbd_status_string(4)
+
+
+def test_create_without_sdf_is_value_error(native_lib):
+    prm = _native.XpbdParams()
+    prm.lame_mu = prm.lame_lambda = 1.0
+    body = _native.XpbdBody()
+    h = ctypes.c_void_p()
+    st = native_lib.xpbd_create(prm, body, None, 0, 1, ctypes.byref(h))
+    assert st == 4
+    with pytest.raises(ValueError):
+        _native.check(st)
+
+
+def test_create_rejects_bad_arguments(native_lib):
+    prm = _native.XpbdParams()
+    prm.lame_mu = prm.lame_lambda = 1.0
+    prm.scatter = 7
+    body = _native.XpbdBody()
+    sdf = (_native.XpbdSdf * 1)()
+    h = ctypes.c_void_p()
+    assert native_lib.xpbd_create(prm, body, sdf, 1, 1, ctypes.byref(h)) == 1
+    prm.scatter = 0
+    assert native_lib.xpbd_create(prm, body, sdf, 1, 1, ctypes.byref(h)) == 5  # empty mesh
+    assert native_lib.xpbd_create(None, body, sdf, 1, 1, ctypes.byref(h)) == 1
+    assert native_lib.xpbd_destroy(None) == 0
+    assert native_lib.xpbd_substep(None, ctypes.c_float(0.01), 0, None) == 1
+
+
+def test_morton_order_is_a_permutation_with_locality(native_lib):
+    m = kuhn_grid(8, 8, 8, 0.1, jitter=0.1, seed=0)
+    V, T = m.n_verts, m.n_tets
+    vp = np.empty(V, dtype=np.int32)
+    tp = np.empty(T, dtype=np.int32)
+    pts = np.ascontiguousarray(m.points)
+    tt = np.ascontiguousarray(m.tets, dtype=np.int32)
+    assert native_lib.xpbd_morton_order(pts.ctypes.data, V, tt.ctypes.data, T, vp.ctypes.data, tp.ctypes.data) == 0
+    assert sorted(vp.tolist()) == list(range(V))
+    assert sorted(tp.tolist()) == list(range(T))
+    # consecutive tets are spatially compact: windows of 64 tets span a smaller box
+    cen = m.points[m.tets].mean(1)
+
+    def window_extent(order):
+        c = cen[order][: (T // 64) * 64].reshape(-1, 64, 3)
+        return np.linalg.norm(c.max(1) - c.min(1), axis=1).mean()
+
+    assert window_extent(tp) < 0.75 * window_extent(np.arange(T))
+    # vertices are numbered by first use: the first tet's corners come first
+    assert set(vp[:4].tolist()) == set(m.tets[tp[0]].tolist())
+
+
+def test_morton_rejects_bad_index(native_lib):
+    pts = np.zeros((4, 3))
+    tt = np.array([[0, 1, 2, 9]], dtype=np.int32)
+    vp = np.empty(4, dtype=np.int32)
+    tp = np.empty(1, dtype=np.int32)
+    assert native_lib.xpbd_morton_order(pts.ctypes.data, 4, tt.ctypes.data, 1, vp.ctypes.data, tp.ctypes.data) == 5
+
+
+def test_vertex_csr(native_lib):
+    m = kuhn_grid(3, 2, 2, 1.0)
+    V, T = m.n_verts, m.n_tets
+    off = np.empty(V + 1, dtype=np.int32)
+    slots = np.empty(4 * T, dtype=np.int32)
+    tt = np.ascontiguousarray(m.tets, dtype=np.int32)
+    assert native_lib.xpbd_build_vertex_csr(tt.ctypes.data, T, V, off.ctypes.data, slots.ctypes.data) == 0
+    assert off[0] == 0 and off[-1] == 4 * T
+    flat = m.tets.reshape(-1)
+    for v in range(V):
+        s = slots[off[v]:off[v + 1]]
+        assert np.all(np.diff(s) > 0)
+        assert np.all(flat[s] == v)
+        assert len(s) == (flat == v).sum()
+
+
+def test_device_count_without_gpu_is_zero_or_more(native_lib):
+    assert native_lib.xpbd_device_count() >= 0

@@ -1,0 +1,103 @@
+"""GPU checks of the reference-facing interface (xpbd_gpu package)."""
+import numpy as np
+import pytest
+
+import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+
+def _solver(**over):
+    from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
+    d = gc.load("kuhn2_block_cheb")
+    kw = gc.solver_kwargs(d)
+    kw.update(over)
+    return d, XPBDNeoHookeanSolver(rest_pose=(d["points"], d["tets"]), sdf=gc.product_sdfs(d), **kw)
+
+
+def test_fields_and_indices_match_reference_setup():
+    d, s = _solver()
+    np.testing.assert_array_equal(s.indices.to_numpy(), d["indices"])
+    assert s.indices.shape[0] == 12 * len(d["tets"])
+    np.testing.assert_allclose(s.mesh.cells.V0.to_numpy(), d["V0"], rtol=1e-6)
+    np.testing.assert_allclose(s.mesh.cells.inv_Dm.to_numpy(), d["inv_Dm"], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(s.mesh.verts.m.to_numpy(), d["mass"], rtol=1e-6)
+    np.testing.assert_allclose(s.mesh.verts.inv_m.to_numpy(), d["inv_m"], rtol=1e-6)
+    assert len(s.mesh.verts) == len(d["points"]) and len(s.mesh.cells) == len(d["tets"])
+    assert s.mesh.verts.x.to_numpy().dtype == np.float32
+
+
+def test_from_numpy_roundtrip_in_caller_order():
+    _, s = _solver()
+    rng = np.random.default_rng(0)
+    a = rng.normal(size=(s.n_verts, 3)).astype(np.float32)
+    s.mesh.verts.v.from_numpy(a)
+    np.testing.assert_array_equal(s.mesh.verts.v.to_numpy(), a)
+    x = s.mesh.verts.x.to_numpy()
+    s.mesh.verts.x.from_numpy(x + 1.0)
+    np.testing.assert_array_equal(s.mesh.verts.x.to_numpy(), x + 1.0)
+    # inv_m survives a position import
+    np.testing.assert_array_equal(s.mesh.verts.inv_m.to_numpy() == 0, s._host_inv_m == 0)
+
+
+def test_no_sdf_raises_value_error():
+    from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
+    d = gc.load("kuhn2_block_cheb")
+    with pytest.raises(ValueError, match="SDF"):
+        XPBDNeoHookeanSolver(rest_pose=(d["points"], d["tets"]), sdf=[])
+    with pytest.raises(ValueError):
+        XPBDNeoHookeanSolver(rest_pose=(d["points"], d["tets"]), sdf=None)
+
+
+def test_rho_hat_persists_across_frames_and_is_settable():
+    _, s = _solver(monitor_convergence=False)
+    assert abs(s.rho_hat - 0.999) < 1e-15
+    s.solve()
+    r1 = s.rho_hat
+    assert r1 != 0.999
+    s.rho_hat = 0.5
+    assert s.rho_hat == 0.5
+
+
+def test_sdf_parameter_change_reaches_device():
+    """Moving the plane up pushes the body up at the next substep."""
+    from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
+    from xpbd_gpu.sdf import PlaneSdf
+    from xpbd_gpu.mesh import kuhn_grid
+    m = kuhn_grid(2, 2, 2, 0.1, origin=(0, 0.05, 0))
+    plane = PlaneSdf(point=[0, 0, 0], dir=[0, 1, 0], fixed=False)
+    s = XPBDNeoHookeanSolver(m, plane, frame_dt=1 / 60, dt=1 / 60, substeps_num=1, constraints_iter=2,
+                             block_neohookean_enable=True)
+    plane.point[None] = [0.0, 0.5, 0.0]
+    s.solve()
+    assert s.mesh.verts.x.to_numpy()[:, 1].min() >= 0.49
+
+
+def test_nonfinite_residual_sets_status():
+    from xpbd_gpu._native import XpbdError
+    _, s = _solver(monitor_convergence=False)
+    x = s.mesh.verts.x.to_numpy()
+    x[0, 0] = np.nan
+    s.mesh.verts.x.from_numpy(x)
+    s.solve()
+    with pytest.raises(XpbdError):
+        s.check_status()
+
+
+def test_usd_export_accessors():
+    """What usd_export.py:58-92 reads from the solver and the SDFs."""
+    from xpbd_gpu.sdf import CubeSdf, PlaneSdf, SphereSdf
+    d, s = _solver()
+    verts = s.mesh.verts.x
+    assert verts.to_numpy().shape == (len(d["points"]), 3)
+    face = s.indices
+    assert face.shape[0] // 3 * [3] == [3] * (face.shape[0] // 3)
+    for sdf in s.sdfs:
+        if isinstance(sdf, SphereSdf):
+            assert sdf.center[None].to_numpy().shape == (3,)
+            float(sdf.radius[None])
+        elif isinstance(sdf, CubeSdf):
+            assert (sdf.half_size[None].to_numpy() * 2.0).astype(np.float32).shape == (3,)
+        elif isinstance(sdf, PlaneSdf):
+            assert sdf.point[None].to_numpy().shape == (3,)
+            np.testing.assert_allclose(np.linalg.norm(sdf.dir[None].to_numpy()), 1.0, rtol=1e-6)
