@@ -318,6 +318,19 @@ def run_gb300(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args):
+    """Frames with direct launches and no timing, for an external profiler."""
+    import torch
+    from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
+    mesh, specs, kw, desc = workload(args.workload)
+    solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, use_graph=False, **kw)
+    for _ in range(args.profile_frames):
+        solver.solve()
+    torch.cuda.synchronize()
+    solver.check_status()
+    print("profile mode: %d frame(s) of %s" % (args.profile_frames, desc))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -331,8 +344,12 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=3)
     ap.add_argument("--ref-iters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
+    ap.add_argument("--profile-frames", type=int, default=1)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.mode == "profile":
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)
