@@ -206,7 +206,8 @@ def run_gb300(args):
     from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver, frame_chunks
 
     mesh, specs, kw, desc = workload(args.workload)
-    solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, **kw)
+    solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
+                                  patch_pipeline=args.patch_pipeline, **kw)
     frame_units = tet_iterations_per_frame(mesh, kw)
     n_chunks = len(frame_chunks(kw["frame_dt"], kw["dt"]))
     per_iter = 3 + (1 if args.scatter == "gather" else 0)
@@ -295,7 +296,8 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc, "step": "one frame (%d tet-iterations)" % frame_units,
-                   "scatter": args.scatter, "l2": "flushed between steps (%d MiB write)" % (L2_FLUSH_BYTES >> 20),
+                   "scatter": args.scatter, "sweep_order": args.sweep_order,
+                   "patch_pipeline": args.patch_pipeline, "l2": "flushed between steps (%d MiB write)" % (L2_FLUSH_BYTES >> 20),
                    "parallelism": "replicas" if world > 1 else "single GPU", "graph": "one CUDA graph per frame"},
         "frames_per_s": 1e3 / ms_per_step * world,
         "gpu_launches": launches_per_frame * args.steps,
@@ -323,7 +325,8 @@ def run_profile(args):
     import torch
     from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
     mesh, specs, kw, desc = workload(args.workload)
-    solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, use_graph=False, **kw)
+    solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
+                                  patch_pipeline=args.patch_pipeline, use_graph=False, **kw)
     for _ in range(args.profile_frames):
         solver.solve()
     torch.cuda.synchronize()
@@ -338,7 +341,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
-    ap.add_argument("--scatter", default="atomic", choices=["atomic", "gather"])
+    ap.add_argument("--scatter", default="patch", choices=["atomic", "gather", "patch"])
+    ap.add_argument("--sweep-order", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--patch-pipeline", type=int, default=0, choices=[0, 1])
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-iters", type=int, default=3)

@@ -38,14 +38,21 @@ enum xpbd_status {
   XPBD_ERR_NONFINITE = 3,        /* the residual reduction saw NaN/Inf */
   XPBD_ERR_NO_SDF = 4,           /* xpbd_base.py:66-67 raises ValueError */
   XPBD_ERR_BAD_MESH = 5,         /* index out of range / empty mesh */
-  XPBD_ERR_HISTORY_FULL = 6      /* more iterations than the history holds */
+  XPBD_ERR_HISTORY_FULL = 6,     /* more iterations than the history holds */
+  XPBD_ERR_TIMEOUT = 7           /* a bounded device-side wait gave up */
 };
 
 /* sdf.py:60-124 */
 enum xpbd_sdf_kind { XPBD_SDF_PLANE = 0, XPBD_SDF_SPHERE = 1, XPBD_SDF_CUBE = 2 };
 
 /* Scatter variants of the Jacobi accumulation. */
-enum xpbd_scatter { XPBD_SCATTER_ATOMIC = 0, XPBD_SCATTER_GATHER = 1 };
+/* Scatter variants of the Jacobi accumulation.
+ *  ATOMIC: one thread per tet, four red.global.add.v4.f32 per tet.
+ *  GATHER: per-corner contributions, then a deterministic vertex->tet CSR sum.
+ *  PATCH:  one CTA per patch of P Morton-consecutive tets; the patch's vertex
+ *          neighbourhood is staged in shared memory, contributions accumulate
+ *          there and one red.global.add.v4.f32 per patch vertex is issued. */
+enum xpbd_scatter { XPBD_SCATTER_ATOMIC = 0, XPBD_SCATTER_GATHER = 1, XPBD_SCATTER_PATCH = 2 };
 
 /* One SDF obstacle (sdf.py:7-124).  48 bytes. */
 typedef struct xpbd_sdf {
@@ -74,6 +81,11 @@ typedef struct xpbd_params {
   int32_t precise_hydro;        /* 1: cancellation-free det F - 1, tr F^T F - 3 */
   int32_t scatter;              /* xpbd_scatter */
   int32_t use_graph;            /* 1: xpbd_solve replays a cached CUDA graph */
+  int32_t sweep_order;          /* PATCH only: 1 = residual visits patches last-to-first */
+  int32_t patch_pipeline;       /* PATCH only: 0 = one CTA per patch, 1 = persistent CTAs
+                                   streaming tet records with cp.async.bulk */
+  int32_t patch_reduce;         /* PATCH, pipeline 0: 1 = reduce per patch vertex in shared
+                                   memory before the global reduction */
   double rho_min, rho_max, rho_beta; /* neohookean_solver.py:66-68 */
 } xpbd_params;
 
@@ -89,7 +101,8 @@ typedef struct xpbd_body {
   const int32_t* tets;   /* [T][4] vertex ids */
   const float* dm_a;     /* [T][4] inv_Dm[0][0..2], inv_Dm[1][0] */
   const float* dm_b;     /* [T][4] inv_Dm[1][1..2], inv_Dm[2][0..1] */
-  const float* dm_c;     /* [T][2] inv_Dm[2][2], V0 */
+  const float* dm_c;     /* [T] inv_Dm[2][2] */
+  const float* v0;       /* [T] rest volume V0 */
   float* lam;            /* [T][2] lambda_D, lambda_H */
   /* deterministic gather variant (XPBD_SCATTER_GATHER); may be NULL otherwise */
   const int32_t* v2t_offsets; /* [V+1] CSR row offsets */
@@ -97,6 +110,22 @@ typedef struct xpbd_body {
   float* corner_dx;           /* [4T][4] per-corner contributions */
   /* solver vertex i is the caller's vertex vert_perm[i]; NULL = identity */
   const int32_t* vert_perm;   /* [V] */
+  /* tile variant (XPBD_SCATTER_PATCH); may be NULL / 0 otherwise.  With it,
+   * dm_a, dm_b, dm_c, lam and tet_lid hold n_patches * patch_tets entries
+   * (zero padded past n_tets) so that every patch is copied whole.  Patch p is
+   * tets [p*patch_tets, min((p+1)*patch_tets, T)); its vertices are
+   * patch_verts[patch_voff[p] .. patch_voff[p+1]) (at most 256), and byte q of
+   * tet_lid[t] is the patch-local index of corner q. */
+  int32_t n_patches;
+  int32_t patch_tets;         /* 64, 128 or 256 */
+  const uint32_t* tet_lid;    /* [T] */
+  const int32_t* patch_voff;  /* [n_patches+1] */
+  const int32_t* patch_verts; /* [patch_voff[n_patches]] */
+  /* patch-local vertex -> corner lists (xpbd_build_patch_csr): the corners of
+   * patch vertex k are slots[p*4P + pv_start[k] .. next start) with slot =
+   * 4 * (tet - p*P) + corner, ascending. */
+  const uint16_t* pv_start;   /* [patch_voff[n_patches]] */
+  const uint16_t* pv_slots;   /* [4 * n_patches * patch_tets] */
 } xpbd_body;
 
 /* Vertex fields addressable by xpbd_import_vec3 / xpbd_export_vec3. */
@@ -184,7 +213,8 @@ int xpbd_set_profiling(void* handle, int32_t enable);
  * (arrays of n <= XPBD_K_COUNT); synchronises `stream`; `reset` clears. */
 int xpbd_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, int32_t reset, void* stream);
 
-/* Sticky device error flags (XPBD_OK or XPBD_ERR_NONFINITE); synchronises. */
+/* Sticky device error flags (XPBD_OK, XPBD_ERR_NONFINITE or XPBD_ERR_TIMEOUT);
+ * synchronises. */
 int xpbd_check_status(void* handle, void* stream);
 
 /* Host mesh preprocessing (replaces the patcher's reorder, xpbd_base.py:42).
@@ -193,6 +223,19 @@ int xpbd_check_status(void* handle, void* stream);
  * vertices last, in Morton order).  Either output may be NULL. */
 int xpbd_morton_order(const double* pts, int32_t n_verts, const int32_t* tets, int32_t n_tets,
                       int32_t* vert_perm, int32_t* tet_perm);
+
+/* Patches of `patch_tets` consecutive tets for the tile variant: fills
+ * patch_voff [ceil(T/P)+1], patch_verts (capacity 4T; ids ascending per
+ * patch) and tet_lid, and returns the largest patch vertex count in
+ * *max_patch_verts (the layout is usable only if it is <= 256). */
+int xpbd_build_patches(const int32_t* tets, int32_t n_tets, int32_t n_verts, int32_t patch_tets,
+                       int32_t* patch_voff, int32_t* patch_verts, uint32_t* tet_lid, int32_t* max_patch_verts);
+
+/* Patch-local vertex -> corner lists for the tile variant, from the layout of
+ * xpbd_build_patches: pv_start [patch_voff[n_patches]], pv_slots
+ * [4 * ceil(T/P) * P] (unused tail entries are 0xffff). */
+int xpbd_build_patch_csr(const int32_t* patch_voff, const uint32_t* tet_lid, int32_t n_tets, int32_t patch_tets,
+                         uint16_t* pv_start, uint16_t* pv_slots);
 
 /* Vertex -> (tet*4+corner) CSR for the gather variant, slots ascending. */
 int xpbd_build_vertex_csr(const int32_t* tets, int32_t n_tets, int32_t n_verts,

@@ -107,6 +107,76 @@ int xpbd_morton_order(const double* pts, int32_t n_verts, const int32_t* tets, i
   return XPBD_OK;
 }
 
+int xpbd_build_patches(const int32_t* tets, int32_t n_tets, int32_t n_verts, int32_t patch_tets,
+                       int32_t* patch_voff, int32_t* patch_verts, uint32_t* tet_lid, int32_t* max_patch_verts) {
+  if (!tets || n_tets <= 0 || n_verts <= 0 || patch_tets <= 0 || !patch_voff || !patch_verts || !tet_lid ||
+      !max_patch_verts)
+    return XPBD_ERR_INVALID_ARGUMENT;
+  const int32_t np = (n_tets + patch_tets - 1) / patch_tets;
+  std::vector<int32_t> uniq;
+  uniq.reserve(4 * patch_tets);
+  int32_t total = 0, mx = 0;
+  patch_voff[0] = 0;
+  for (int32_t p = 0; p < np; ++p) {
+    const int32_t t0 = p * patch_tets;
+    const int32_t t1 = std::min(n_tets, t0 + patch_tets);
+    uniq.clear();
+    for (int64_t k = 4ll * t0; k < 4ll * t1; ++k) {
+      const int32_t v = tets[k];
+      if (v < 0 || v >= n_verts) return XPBD_ERR_BAD_MESH;
+      uniq.push_back(v);
+    }
+    std::sort(uniq.begin(), uniq.end());
+    uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+    const int32_t nv = (int32_t)uniq.size();
+    mx = std::max(mx, nv);
+    std::copy(uniq.begin(), uniq.end(), patch_verts + total);
+    for (int32_t t = t0; t < t1; ++t) {
+      uint32_t packed = 0;
+      for (int q = 0; q < 4; ++q) {
+        const int32_t loc = (int32_t)(std::lower_bound(uniq.begin(), uniq.end(), tets[4 * t + q]) - uniq.begin());
+        packed |= (uint32_t)(loc & 0xff) << (8 * q);
+      }
+      tet_lid[t] = packed;
+    }
+    total += nv;
+    patch_voff[p + 1] = total;
+  }
+  *max_patch_verts = mx;
+  return XPBD_OK;
+}
+
+int xpbd_build_patch_csr(const int32_t* patch_voff, const uint32_t* tet_lid, int32_t n_tets, int32_t patch_tets,
+                         uint16_t* pv_start, uint16_t* pv_slots) {
+  if (!patch_voff || !tet_lid || !pv_start || !pv_slots || n_tets <= 0 || patch_tets <= 0 || patch_tets > 256)
+    return XPBD_ERR_INVALID_ARGUMENT;
+  const int32_t np = (n_tets + patch_tets - 1) / patch_tets;
+  std::fill(pv_slots, pv_slots + (size_t)4 * np * patch_tets, (uint16_t)0xffff);
+  std::vector<int32_t> cnt, fill;
+  for (int32_t p = 0; p < np; ++p) {
+    const int32_t vb = patch_voff[p], nv = patch_voff[p + 1] - vb;
+    if (nv < 0 || nv > 256) return XPBD_ERR_BAD_MESH;
+    const int32_t t0 = p * patch_tets, t1 = std::min(n_tets, t0 + patch_tets);
+    cnt.assign(nv + 1, 0);
+    for (int32_t t = t0; t < t1; ++t)
+      for (int q = 0; q < 4; ++q) {
+        const int32_t l = (tet_lid[t] >> (8 * q)) & 0xff;
+        if (l >= nv) return XPBD_ERR_BAD_MESH;
+        cnt[l + 1]++;
+      }
+    for (int32_t k = 0; k < nv; ++k) cnt[k + 1] += cnt[k];
+    fill.assign(cnt.begin(), cnt.end() - 1);
+    for (int32_t k = 0; k < nv; ++k) pv_start[vb + k] = (uint16_t)cnt[k];
+    uint16_t* slots = pv_slots + (size_t)4 * p * patch_tets;
+    for (int32_t t = t0; t < t1; ++t)
+      for (int q = 0; q < 4; ++q) {
+        const int32_t l = (tet_lid[t] >> (8 * q)) & 0xff;
+        slots[fill[l]++] = (uint16_t)(4 * (t - t0) + q);
+      }
+  }
+  return XPBD_OK;
+}
+
 int xpbd_build_vertex_csr(const int32_t* tets, int32_t n_tets, int32_t n_verts, int32_t* offsets, int32_t* slots) {
   if (!tets || !offsets || !slots || n_tets < 0 || n_verts <= 0) return XPBD_ERR_INVALID_ARGUMENT;
   std::fill(offsets, offsets + n_verts + 1, 0);

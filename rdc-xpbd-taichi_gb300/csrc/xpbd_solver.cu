@@ -40,6 +40,7 @@ struct DevState {
   double omega;         // omega of the latest iteration of this substep
   int nonfinite;        // sticky: a residual sum was NaN/Inf
   int bad_mesh;         // set by the index validation kernel
+  int timeout;          // sticky: a bounded mbarrier wait gave up
 };
 
 struct Dev {
@@ -51,12 +52,20 @@ struct Dev {
   const int4* tets;
   const float4* dm_a;
   const float4* dm_b;
-  const float2* dm_c;
+  const float* dm_c;
+  const float* v0;
   float2* lam;
   const int* v2t_off;
   const int* v2t_slot;
   float4* corner;
   const int* perm;  // solver vertex i <- caller vertex perm[i] (nullptr = identity)
+  // tile variant: patch p = tets [p*P, (p+1)*P), vertices verts[voff[p]..voff[p+1])
+  int n_patches, P, n_pverts;
+  const uint32_t* lid;
+  const int* voff;
+  const int* pverts;
+  const uint16_t* pv_start;
+  const uint16_t* pv_slots;
   const xpbd_sdf* sdfs;
   int n_sdf;
   DevState* st;
@@ -170,11 +179,10 @@ __device__ __forceinline__ void load_tet(const Dev& d, int t, int4& id, Tet& tt)
   id = __ldg(d.tets + t);
   const float4 a = __ldg(d.dm_a + t);
   const float4 b = __ldg(d.dm_b + t);
-  const float2 c = __ldg(d.dm_c + t);
   tt.dm[0] = a.x; tt.dm[1] = a.y; tt.dm[2] = a.z;
   tt.dm[3] = a.w; tt.dm[4] = b.x; tt.dm[5] = b.y;
-  tt.dm[6] = b.z; tt.dm[7] = b.w; tt.dm[8] = c.x;
-  tt.V0 = c.y;
+  tt.dm[6] = b.z; tt.dm[7] = b.w; tt.dm[8] = __ldg(d.dm_c + t);
+  tt.V0 = __ldg(d.v0 + t);
 }
 
 template <bool kGather>
@@ -190,23 +198,16 @@ __device__ __forceinline__ void emit(const Dev& d, int t, int corner, int vid, f
 // split pair solve_hydrostatic + solve_deviatoric (:196-254, :144-194), both
 // reading the same predicted positions.  kFirst: lambda == 0 (the reset at
 // :458-459), so lambda is not read.
-template <bool kBlockMode, bool kFirst, bool kPrecise, bool kGather>
-__global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float dt, float mu, float la, float relax_h,
-                                                   float relax_d) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= d.T) return;
-  int4 id;
-  Tet tt;
-  load_tet(d, t, id, tt);
-  const float4* P = d.p[cur];
-  tt.p[0] = ldg4(P + id.x);
-  tt.p[1] = ldg4(P + id.y);
-  tt.p[2] = ldg4(P + id.z);
-  tt.p[3] = ldg4(P + id.w);
-  float2 L = kFirst ? make_float2(0.f, 0.f) : d.lam[t];
+// One tet of solve_neohookean_block (neohookean_solver.py:358-451) when
+// kBlockMode, else of the split pair solve_hydrostatic + solve_deviatoric
+// (:196-254, :144-194), both reading the same predicted positions.  Updates L
+// = (lambda_D, lambda_H) and returns the four corner displacements and the
+// constraint count added to each corner.
+// aD, aH: the time-scaled compliances alpha / dt^2 of the tet (:413-416).
+template <bool kBlockMode, bool kPrecise>
+__device__ __forceinline__ void project_tet(const Tet& tt, float aD, float aH, float relax_h, float relax_d, float2& L,
+                                            float3 dp[4], float& cnt) {
   const float w[4] = {tt.p[0].w, tt.p[1].w, tt.p[2].w, tt.p[3].w};
-  const int vid[4] = {id.x, id.y, id.z, id.w};
-
   float F[9];
   deformation_gradient(tt, F);
   float C_D, C_H;
@@ -221,10 +222,6 @@ __global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float dt, fl
   float3 gH[4];
   corner_gradients(H, tt.dm, gH);
 
-  const float alpha_D = 1.f / (mu * tt.V0);
-  const float alpha_H = 1.f / (la * tt.V0);
-  const float dt2 = dt * dt;
-
   if (kBlockMode) {
     float A11 = w[0] * dot3(gD[0], gD[0]) + w[1] * dot3(gD[1], gD[1]) + w[2] * dot3(gD[2], gD[2]) +
                 w[3] * dot3(gD[3], gD[3]);
@@ -232,8 +229,6 @@ __global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float dt, fl
                 w[3] * dot3(gH[3], gH[3]);
     const float A12 = w[0] * dot3(gD[0], gH[0]) + w[1] * dot3(gD[1], gH[1]) + w[2] * dot3(gD[2], gH[2]) +
                       w[3] * dot3(gD[3], gH[3]);
-    const float aD = alpha_D / dt2;
-    const float aH = alpha_H / dt2;
     A11 += aD;
     A22 += aH;
     const float b1 = -(C_D + aD * L.x);
@@ -244,13 +239,13 @@ __global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float dt, fl
       dD = fabsf(A11) > kEps ? b1 / A11 : 0.f;
       dH = fabsf(A22) > kEps ? b2 / A22 : 0.f;
     }
-    d.lam[t] = make_float2(L.x + dD, L.y + dH);
+    L.x += dD;
+    L.y += dH;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float3 dp = make_float3(w[c] * (gD[c].x * dD + gH[c].x * dH), w[c] * (gD[c].y * dD + gH[c].y * dH),
-                                    w[c] * (gD[c].z * dD + gH[c].z * dH));
-      emit<kGather>(d, t, c, vid[c], dp, 1.f);
-    }
+    for (int c = 0; c < 4; ++c)
+      dp[c] = make_float3(w[c] * (gD[c].x * dD + gH[c].x * dH), w[c] * (gD[c].y * dD + gH[c].y * dH),
+                          w[c] * (gD[c].z * dD + gH[c].z * dH));
+    cnt = 1.f;  // :448-451 count every corner
   } else {
     // hydrostatic then deviatoric, each gated by w_sum > EPS (:237, :177)
     float wsH = w[0] * dot3(gH[0], gH[0]);
@@ -263,25 +258,207 @@ __global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float dt, fl
     wsD += w[3] * dot3(gD[3], gD[3]);
     float dlH = 0.f, dlD = 0.f, cH = 0.f, cD = 0.f;
     if (wsH > kEps) {
-      const float at = alpha_H / dt2;
+      const float at = aH;
       dlH = -(C_H + at * L.y) / (wsH + at);
       dlH *= relax_h;
       cH = 1.f;
     }
     if (wsD > kEps) {
-      const float at = alpha_D / dt2;
+      const float at = aD;
       dlD = -(C_D + at * L.x) / (wsD + at);
       dlD *= relax_d;
       cD = 1.f;
     }
-    d.lam[t] = make_float2(L.x + dlD, L.y + dlH);
+    L.x += dlD;
+    L.y += dlH;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
       const float sH = dlH * w[c], sD = dlD * w[c];
-      const float3 dp = make_float3(sH * gH[c].x + sD * gD[c].x, sH * gH[c].y + sD * gD[c].y,
-                                    sH * gH[c].z + sD * gD[c].z);
-      emit<kGather>(d, t, c, vid[c], dp, cH + cD);
+      dp[c] = make_float3(sH * gH[c].x + sD * gD[c].x, sH * gH[c].y + sD * gD[c].y, sH * gH[c].z + sD * gD[c].z);
     }
+    cnt = cH + cD;
+  }
+}
+
+// One thread per tet; scatter by vector atomics or into the per-corner buffer.
+// kFirst: lambda == 0 (the reset at neohookean_solver.py:458-459), not read.
+// cD, cH = 1 / (mu dt^2), 1 / (lambda dt^2): aD = alpha_D / dt^2 = cD / V0.
+template <bool kBlockMode, bool kFirst, bool kPrecise, bool kGather>
+__global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float cD, float cH, float relax_h, float relax_d) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.T) return;
+  int4 id;
+  Tet tt;
+  load_tet(d, t, id, tt);
+  const float4* P = d.p[cur];
+  tt.p[0] = ldg4(P + id.x);
+  tt.p[1] = ldg4(P + id.y);
+  tt.p[2] = ldg4(P + id.z);
+  tt.p[3] = ldg4(P + id.w);
+  float2 L = kFirst ? make_float2(0.f, 0.f) : d.lam[t];
+  const int vid[4] = {id.x, id.y, id.z, id.w};
+  float3 dp[4];
+  float cnt;
+  const float inv_v0 = 1.f / tt.V0;
+  project_tet<kBlockMode, kPrecise>(tt, cD * inv_v0, cH * inv_v0, relax_h, relax_d, L, dp, cnt);
+  d.lam[t] = L;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) emit<kGather>(d, t, c, vid[c], dp[c], cnt);
+}
+
+__device__ __forceinline__ float det9(const float m[9]) {
+  return m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) + m[6] * (m[1] * m[5] - m[4] * m[2]);
+}
+
+// ---------------------------------------------------------------------------
+// Tile variant.  Patch p = kP Morton-consecutive tets (arrays padded to a
+// multiple of the patch size) whose <= 256 vertices are listed in
+// pverts[voff[p] .. voff[p+1]).  Persistent CTAs walk the patches; one thread
+// streams the next patch's tet records (48 bytes per tet: 4 u8 local corner
+// ids, inv_Dm, lambda) into shared memory with cp.async.bulk while the CTA
+// works on the current patch, whose vertex neighbourhood is staged in shared
+// memory once and shared by all its tets.  V0 = 1 / (6 det inv_Dm).
+// ---------------------------------------------------------------------------
+
+struct __align__(16) PatchStage {
+  float4 dma[256];
+  float4 dmb[256];
+  float2 lam[256];
+  uint32_t lid[256];
+  float dmc[256];
+};
+
+constexpr int kMaxPolls = 1 << 20;
+
+// Issue the bulk copies of patch p's tet records into `st` (one thread);
+// completion is tracked by the transaction count of `bar`.
+template <bool kLam>
+__device__ __forceinline__ void issue_records(const Dev& d, PatchStage& st, unsigned long long* barp, int p, int kP) {
+  const size_t t0 = (size_t)p * kP;
+  const uint32_t bytes = kP * (16u + 16u + 4u + 4u + (kLam ? 8u : 0u));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(barp);
+  mbar_expect_tx(bar, bytes);
+  bulk_g2s(st.dma, d.dm_a + t0, kP * 16u, bar);
+  bulk_g2s(st.dmb, d.dm_b + t0, kP * 16u, bar);
+  bulk_g2s(st.lid, d.lid + t0, kP * 4u, bar);
+  bulk_g2s(st.dmc, d.dm_c + t0, kP * 4u, bar);
+  if (kLam) bulk_g2s(st.lam, d.lam + t0, kP * 8u, bar);
+}
+
+__device__ __forceinline__ void stage_tet(const PatchStage& st, int i, Tet& tt, uint32_t& lid) {
+  const float4 A = st.dma[i], B = st.dmb[i];
+  tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+  tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+  tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = st.dmc[i];
+  lid = st.lid[i];
+}
+
+
+// Shared memory of the pipelined tile kernels: two stages, each with the tet
+// records of one patch (bulk copy), the positions (and for the residual the
+// Jacobi accumulators) of its vertices (cp.async gathers) and their ids.
+template <bool kDx>
+struct __align__(16) TileSmem {
+  PatchStage st[2];
+  float4 sp[2][256];
+  float4 sdx[2][kDx ? 256 : 1];
+  int sg[2][256];
+  unsigned long long bar[2];
+};
+
+// Gather the vertex tile of one patch into stage s (thread j < nv takes vertex j).
+template <bool kDx>
+__device__ __forceinline__ void gather_tile(const Dev& d, TileSmem<kDx>& sm, int s, const float4* P, int g) {
+  const int j = threadIdx.x;
+  sm.sg[s][j] = g;
+  cp_async16(&sm.sp[s][j], P + g);
+  if (kDx) cp_async16(&sm.sdx[s][j], d.dx + g);
+}
+
+// Patch ids of the CTA's walk; `reverse` visits them last-to-first.
+__device__ __forceinline__ int walk_patch(int q, int n, bool reverse) { return reverse ? n - 1 - q : q; }
+
+// Pipelined tile projection (256 tets per patch, one vertex per thread).
+// Iteration k computes patch q_k while the records and vertex tile of
+// q_{k+1} are in flight and the vertex list of q_{k+2} is being read.
+template <bool kBlockMode, bool kFirst, bool kPrecise>
+__global__ void __launch_bounds__(256) k_project_tile(Dev d, int cur, float cD, float cH, float relax_h,
+                                                     float relax_d) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TileSmem<false>& sm = *reinterpret_cast<TileSmem<false>*>(smem_raw);
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(reinterpret_cast<uint64_t*>(&sm.bar[0]), 1);
+    mbar_init(reinterpret_cast<uint64_t*>(&sm.bar[1]), 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  const int n = d.n_patches, G = gridDim.x, tid = threadIdx.x;
+  const float4* P = d.p[cur];
+  int q = blockIdx.x;
+  if (q >= n) return;
+  // prologue: records + tile of q, vertex id of q + G
+  if (tid == 0) issue_records<!kFirst>(d, sm.st[0], &sm.bar[0], q, 256);
+  {
+    const int vb = __ldg(d.voff + q), nv = __ldg(d.voff + q + 1) - vb;
+    if (tid < nv) gather_tile<false>(d, sm, 0, P, __ldg(d.pverts + vb + tid));
+  }
+  cp_async_commit();
+  int gn = -1;
+  if (q + G < n) {
+    const int vb = __ldg(d.voff + q + G), nv = __ldg(d.voff + q + G + 1) - vb;
+    if (tid < nv) gn = __ldg(d.pverts + vb + tid);
+  }
+  int k = 0;
+  bool issued_next = false;
+  for (; q < n; q += G, ++k) {
+    const int s = k & 1;
+    const int qn = q + G;
+    issued_next = qn < n;
+    if (issued_next) {
+      if (tid == 0) {
+        fence_proxy_async();
+        issue_records<!kFirst>(d, sm.st[s ^ 1], &sm.bar[s ^ 1], qn, 256);
+      }
+      if (gn >= 0) gather_tile<false>(d, sm, s ^ 1, P, gn);
+    }
+    cp_async_commit();
+    gn = -1;
+    if (qn + G < n) {
+      const int vb = __ldg(d.voff + qn + G), nv = __ldg(d.voff + qn + G + 1) - vb;
+      if (tid < nv) gn = __ldg(d.pverts + vb + tid);
+    }
+    cp_async_wait<1>();
+    if (tid == 0 && !mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[s]), (k >> 1) & 1, kMaxPolls)) {
+      abort_flag = 1;
+      d.st->timeout = 1;
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    const int t = q * 256 + tid;
+    if (t < d.T) {
+      Tet tt;
+      uint32_t lid;
+      stage_tet(sm.st[s], tid, tt, lid);
+      const int l[4] = {(int)(lid & 0xffu), (int)((lid >> 8) & 0xffu), (int)((lid >> 16) & 0xffu), (int)(lid >> 24)};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) tt.p[c] = sm.sp[s][l[c]];
+      float2 L = kFirst ? make_float2(0.f, 0.f) : sm.st[s].lam[tid];
+      const float six_det = 6.f * det9(tt.dm);  // 1 / V0
+      float3 dp[4];
+      float cnt;
+      project_tet<kBlockMode, kPrecise>(tt, six_det * cD, six_det * cH, relax_h, relax_d, L, dp, cnt);
+      d.lam[t] = L;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) red_add_v4(d.dx + sm.sg[s][l[c]], dp[c].x, dp[c].y, dp[c].z, cnt);
+    }
+    __syncthreads();  // stage s is refilled two iterations later
+  }
+  cp_async_wait<0>();
+  if (abort_flag && tid == 0) {
+    mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[k & 1]), (k >> 1) & 1, kMaxPolls);
+    if (issued_next) mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[(k & 1) ^ 1]), ((k + 1) >> 1) & 1, kMaxPolls);
   }
 }
 
@@ -303,53 +480,21 @@ __device__ __forceinline__ float3 post_position(const float4 p, const float4 D) 
 
 struct SweepArgs {
   int cur;
-  float dt, mu, la;
+  float cD, cH;  // 1 / (mu dt^2), 1 / (lambda dt^2)
   int it, warmup, rec;
+  int reverse;  // tile residual: visit patches last-to-first
   double rho_min, rho_max, rho_beta;
 };
 
-// compute_xpbd_residual (neohookean_solver.py:298-329) and the monitoring
-// errors (:256-296) at the post-Jacobi positions p[cur] + dx/count, i.e.
-// before the Chebyshev mix (:490-494).  Per-thread FP32 partials over a
-// grid-stride range, FP64 warp/block/grid reduction.  The last block to
-// finish applies the rho_hat / omega recurrence (:495-504, :537-546) in FP64
-// and writes history row `rec` = {r_hat, omega, hydro, dev}.
-template <bool kRes, bool kMon, bool kPrecise>
-__global__ void __launch_bounds__(kBlock) k_residual(Dev d, SweepArgs a) {
-  float sr = 0.f, sh = 0.f, sd = 0.f;
-  const float4* P = d.p[a.cur];
-  const float dt2 = a.dt * a.dt;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < d.T; t += gridDim.x * blockDim.x) {
-    int4 id;
-    Tet tt;
-    load_tet(d, t, id, tt);
-    const int vid[4] = {id.x, id.y, id.z, id.w};
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const float3 q = post_position(ldg4(P + vid[c]), ldg4(d.dx + vid[c]));
-      tt.p[c] = make_float4(q.x, q.y, q.z, 0.f);
-    }
-    float F[9];
-    deformation_gradient(tt, F);
-    float C_D, C_H;
-    invariants<kPrecise>(F, C_D, C_H);
-    if (kRes) {
-      const float2 L = d.lam[t];
-      const float aD = (1.f / (a.mu * tt.V0)) / dt2;
-      const float aH = (1.f / (a.la * tt.V0)) / dt2;
-      const float rD = C_D + aD * L.x;
-      const float rH = C_H + aH * L.y;
-      sr += sqrtf(rD * rD + rH * rH);
-    }
-    if (kMon) {
-      sh += fabsf(C_H);
-      sd += fabsf(C_D);
-    }
-  }
-  __shared__ double red[3][kBlock / 32];
+// Block + grid FP64 reduction of the per-thread partial sums; the last block to
+// finish applies the rho_hat / omega recurrence (neohookean_solver.py:495-504,
+// :537-546) and writes history row `rec` = {r_hat, omega, hydro, dev}.
+template <bool kRes, bool kMon>
+__device__ __forceinline__ void finish_residual(const Dev& d, const SweepArgs& a, float sr, float sh, float sd) {
+  __shared__ double red[3][32];
   __shared__ bool last;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double r0 = warp_sum((double)sr), r1 = warp_sum((double)sh), r2 = warp_sum((double)sd);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const double r0 = warp_sum((double)sr), r1 = warp_sum((double)sh), r2 = warp_sum((double)sd);
   if (lane == 0) {
     red[0][warp] = r0;
     red[1][warp] = r1;
@@ -358,7 +503,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(Dev d, SweepArgs a) {
   __syncthreads();
   if (threadIdx.x == 0) {
     double b0 = 0.0, b1 = 0.0, b2 = 0.0;
-    for (int k = 0; k < kBlock / 32; ++k) {
+    for (int k = 0; k < nw; ++k) {
       b0 += red[0][k];
       b1 += red[1][k];
       b2 += red[2][k];
@@ -409,6 +554,269 @@ __global__ void __launch_bounds__(kBlock) k_residual(Dev d, SweepArgs a) {
   }
 }
 
+template <bool kRes, bool kMon, bool kPrecise>
+__device__ __forceinline__ void residual_terms(const Tet& tt, float2 L, float aD, float aH, float& sr, float& sh,
+                                               float& sd) {
+  float F[9];
+  deformation_gradient(tt, F);
+  float C_D, C_H;
+  invariants<kPrecise>(F, C_D, C_H);
+  if (kRes) {
+    const float rD = C_D + aD * L.x;
+    const float rH = C_H + aH * L.y;
+    sr += sqrtf(rD * rD + rH * rH);
+  }
+  if (kMon) {
+    sh += fabsf(C_H);
+    sd += fabsf(C_D);
+  }
+}
+
+// compute_xpbd_residual (neohookean_solver.py:298-329) and the monitoring
+// errors (:256-296) at the post-Jacobi positions p[cur] + dx/count, i.e.
+// before the Chebyshev mix (:490-494).  Grid-stride over tets with per-thread
+// FP32 partials, then finish_residual.
+template <bool kRes, bool kMon, bool kPrecise>
+__global__ void __launch_bounds__(kBlock) k_residual(Dev d, SweepArgs a) {
+  float sr = 0.f, sh = 0.f, sd = 0.f;
+  const float4* P = d.p[a.cur];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < d.T; t += gridDim.x * blockDim.x) {
+    int4 id;
+    Tet tt;
+    load_tet(d, t, id, tt);
+    const int vid[4] = {id.x, id.y, id.z, id.w};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float3 q = post_position(ldg4(P + vid[c]), ldg4(d.dx + vid[c]));
+      tt.p[c] = make_float4(q.x, q.y, q.z, 0.f);
+    }
+    const float2 L = kRes ? d.lam[t] : make_float2(0.f, 0.f);
+    const float inv_v0 = 1.f / tt.V0;
+    residual_terms<kRes, kMon, kPrecise>(tt, L, a.cD * inv_v0, a.cH * inv_v0, sr, sh, sd);
+  }
+  finish_residual<kRes, kMon>(d, a, sr, sh, sd);
+}
+
+// Pipelined tile residual: the same walk as k_project_tile (optionally
+// last-to-first, so that the records the projection touched last are still
+// in L2); the tile carries positions and Jacobi accumulators, converted to
+// post-Jacobi positions in shared memory before the tets use them.
+template <bool kRes, bool kMon, bool kPrecise>
+__global__ void __launch_bounds__(256) k_residual_tile(Dev d, SweepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TileSmem<true>& sm = *reinterpret_cast<TileSmem<true>*>(smem_raw);
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(reinterpret_cast<uint64_t*>(&sm.bar[0]), 1);
+    mbar_init(reinterpret_cast<uint64_t*>(&sm.bar[1]), 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  float sr = 0.f, sh = 0.f, sd = 0.f;
+  const int n = d.n_patches, G = gridDim.x, tid = threadIdx.x;
+  const bool rev = a.reverse != 0;
+  const float4* P = d.p[a.cur];
+  int q = blockIdx.x;
+  int k = 0;
+  bool issued_next = false;
+  if (q < n) {
+    const int p0 = walk_patch(q, n, rev);
+    if (tid == 0) issue_records<kRes>(d, sm.st[0], &sm.bar[0], p0, 256);
+    const int vb = __ldg(d.voff + p0), nv = __ldg(d.voff + p0 + 1) - vb;
+    if (tid < nv) gather_tile<true>(d, sm, 0, P, __ldg(d.pverts + vb + tid));
+  }
+  cp_async_commit();
+  int gn = -1;
+  if (q + G < n) {
+    const int p1 = walk_patch(q + G, n, rev);
+    const int vb = __ldg(d.voff + p1), nv = __ldg(d.voff + p1 + 1) - vb;
+    if (tid < nv) gn = __ldg(d.pverts + vb + tid);
+  }
+  for (; q < n; q += G, ++k) {
+    const int s = k & 1;
+    const int p = walk_patch(q, n, rev);
+    const int qn = q + G;
+    issued_next = qn < n;
+    if (issued_next) {
+      if (tid == 0) {
+        fence_proxy_async();
+        issue_records<kRes>(d, sm.st[s ^ 1], &sm.bar[s ^ 1], walk_patch(qn, n, rev), 256);
+      }
+      if (gn >= 0) gather_tile<true>(d, sm, s ^ 1, P, gn);
+    }
+    cp_async_commit();
+    gn = -1;
+    if (qn + G < n) {
+      const int p2 = walk_patch(qn + G, n, rev);
+      const int vb = __ldg(d.voff + p2), nv = __ldg(d.voff + p2 + 1) - vb;
+      if (tid < nv) gn = __ldg(d.pverts + vb + tid);
+    }
+    cp_async_wait<1>();
+    if (tid == 0 && !mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[s]), (k >> 1) & 1, kMaxPolls)) {
+      abort_flag = 1;
+      d.st->timeout = 1;
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    {
+      const int nv = __ldg(d.voff + p + 1) - __ldg(d.voff + p);
+      if (tid < nv) {
+        const float3 x = post_position(sm.sp[s][tid], sm.sdx[s][tid]);
+        sm.sp[s][tid] = make_float4(x.x, x.y, x.z, 0.f);
+      }
+    }
+    __syncthreads();
+    const int t = p * 256 + tid;
+    if (t < d.T) {
+      Tet tt;
+      uint32_t lid;
+      stage_tet(sm.st[s], tid, tt, lid);
+      tt.p[0] = sm.sp[s][lid & 0xffu];
+      tt.p[1] = sm.sp[s][(lid >> 8) & 0xffu];
+      tt.p[2] = sm.sp[s][(lid >> 16) & 0xffu];
+      tt.p[3] = sm.sp[s][lid >> 24];
+      const float six_det = 6.f * det9(tt.dm);
+      const float2 L = kRes ? sm.st[s].lam[tid] : make_float2(0.f, 0.f);
+      residual_terms<kRes, kMon, kPrecise>(tt, L, six_det * a.cD, six_det * a.cH, sr, sh, sd);
+    }
+    __syncthreads();
+  }
+  cp_async_wait<0>();
+  if (abort_flag && tid == 0) {
+    mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[k & 1]), (k >> 1) & 1, kMaxPolls);
+    if (issued_next) mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[(k & 1) ^ 1]), ((k + 1) >> 1) & 1, kMaxPolls);
+  }
+  // every CTA joins the reduction so the ticket count stays whole; the sticky
+  // timeout flag marks the sweep invalid for the host
+  finish_residual<kRes, kMon>(d, a, sr, sh, sd);
+}
+
+// Tile variant, one CTA per patch: the tet records are loaded straight into
+// registers and the vertex neighbourhood into shared memory; many resident
+// CTAs per SM overlap each other's load and compute phases.  The corner
+// contributions are reduced per patch vertex in shared memory, in the fixed
+// order of the patch's vertex -> corner lists, so that one
+// red.global.add.v4 per patch vertex (instead of one per tet corner) reaches
+// the L2.
+// kReduce: reduce per patch vertex before the global reduction (else one
+// red.global.add.v4 per tet corner).
+template <bool kBlockMode, bool kFirst, bool kPrecise, int kP, bool kReduce>
+__global__ void __launch_bounds__(kP) k_project_patch1(Dev d, int cur, float cD, float cH, float relax_h,
+                                                      float relax_d) {
+  __shared__ float4 sp[256];
+  __shared__ int sg[256];
+  __shared__ float4 sdp[kReduce ? 4 * kP : 1];
+  __shared__ __align__(16) uint16_t sslot[kReduce ? 4 * kP : 8];
+  __shared__ uint16_t sstart[kReduce ? 257 : 1];
+  const int p = blockIdx.x;
+  const int vb = __ldg(d.voff + p);
+  const int nv = __ldg(d.voff + p + 1) - vb;
+  const int t0 = p * kP;
+  const int nt = d.T - t0 < kP ? d.T - t0 : kP;
+  const int t = t0 + threadIdx.x;
+  const bool has = threadIdx.x < nt;
+  Tet tt;
+  uint32_t lid = 0;
+  float2 L = make_float2(0.f, 0.f);
+  if (has) {
+    const float4 A = __ldg(d.dm_a + t), B = __ldg(d.dm_b + t);
+    tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+    tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+    tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
+    lid = __ldg(d.lid + t);
+    if (!kFirst) L = d.lam[t];
+  }
+  // the patch's vertex -> corner lists: 4 kP u16 slots (16-byte chunks) + starts
+  if (kReduce) {
+    const uint4* src = reinterpret_cast<const uint4*>(d.pv_slots + (size_t)4 * kP * p);
+    uint4* dst = reinterpret_cast<uint4*>(sslot);
+    for (int k = threadIdx.x; k < kP / 2; k += kP) dst[k] = __ldg(src + k);
+    if (threadIdx.x == 0) sstart[nv] = (uint16_t)(4 * nt);
+  }
+  const float4* P = d.p[cur];
+  for (int j = threadIdx.x; j < nv; j += kP) {
+    const int g = __ldg(d.pverts + vb + j);
+    sg[j] = g;
+    if (kReduce) sstart[j] = __ldg(d.pv_start + vb + j);
+    sp[j] = ldg4(P + g);
+  }
+  __syncthreads();
+  if (has) {
+    const int l[4] = {(int)(lid & 0xffu), (int)((lid >> 8) & 0xffu), (int)((lid >> 16) & 0xffu), (int)(lid >> 24)};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tt.p[c] = sp[l[c]];
+    const float six_det = 6.f * det9(tt.dm);
+    float3 dp[4];
+    float cnt;
+    project_tet<kBlockMode, kPrecise>(tt, six_det * cD, six_det * cH, relax_h, relax_d, L, dp, cnt);
+    d.lam[t] = L;
+    if (kReduce) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) sdp[4 * threadIdx.x + c] = make_float4(dp[c].x, dp[c].y, dp[c].z, cnt);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) red_add_v4(d.dx + sg[l[c]], dp[c].x, dp[c].y, dp[c].z, cnt);
+    }
+  }
+  if (!kReduce) return;
+  __syncthreads();
+  for (int j = threadIdx.x; j < nv; j += kP) {
+    const int s0 = sstart[j], s1 = sstart[j + 1];
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = s0; k < s1; ++k) {
+      const float4 c = sdp[sslot[k]];
+      acc.x += c.x;
+      acc.y += c.y;
+      acc.z += c.z;
+      acc.w += c.w;
+    }
+    red_add_v4(d.dx + sg[j], acc.x, acc.y, acc.z, acc.w);
+  }
+}
+
+template <bool kRes, bool kMon, bool kPrecise, int kP>
+__global__ void __launch_bounds__(kP) k_residual_patch1(Dev d, SweepArgs a) {
+  __shared__ float4 sp[256];
+  float sr = 0.f, sh = 0.f, sd = 0.f;
+  const float4* P = d.p[a.cur];
+  const int n = d.n_patches;
+  for (int q = blockIdx.x; q < n; q += gridDim.x) {
+    const int p = a.reverse ? n - 1 - q : q;
+    const int vb = __ldg(d.voff + p);
+    const int nv = __ldg(d.voff + p + 1) - vb;
+    const int t = p * kP + threadIdx.x;
+    const bool has = t < d.T;
+    Tet tt;
+    uint32_t lid = 0;
+    float2 L = make_float2(0.f, 0.f);
+    if (has) {
+      const float4 A = __ldg(d.dm_a + t), B = __ldg(d.dm_b + t);
+      tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+      tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+      tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
+      lid = __ldg(d.lid + t);
+      if (kRes) L = d.lam[t];
+    }
+    __syncthreads();  // the previous patch's readers are done with sp
+    for (int j = threadIdx.x; j < nv; j += kP) {
+      const int g = __ldg(d.pverts + vb + j);
+      const float3 x = post_position(ldg4(P + g), ldg4(d.dx + g));
+      sp[j] = make_float4(x.x, x.y, x.z, 0.f);
+    }
+    __syncthreads();
+    if (has) {
+      tt.p[0] = sp[lid & 0xffu];
+      tt.p[1] = sp[(lid >> 8) & 0xffu];
+      tt.p[2] = sp[(lid >> 16) & 0xffu];
+      tt.p[3] = sp[lid >> 24];
+      const float six_det = 6.f * det9(tt.dm);
+      residual_terms<kRes, kMon, kPrecise>(tt, L, six_det * a.cD, six_det * a.cH, sr, sh, sd);
+    }
+  }
+  finish_residual<kRes, kMon>(d, a, sr, sh, sd);
+}
+
 // Field transfer in caller vertex order (mesh.verts.<f>.from_numpy / to_numpy).
 __global__ void __launch_bounds__(kBlock) k_import(Dev d, float4* f, const float* __restrict__ src) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -443,6 +851,37 @@ __global__ void k_validate(Dev d) {
   if (d.v2t_off != nullptr && t <= d.V) {
     const int o = d.v2t_off[t];
     if (o < 0 || o > 4 * d.T) d.st->bad_mesh = 1;
+  }
+  if (d.lid != nullptr && t < d.T) {
+    const int p = t / d.P;
+    const int nv = d.voff[p + 1] - d.voff[p];
+    const uint32_t l = d.lid[t];
+    if ((int)(l & 0xffu) >= nv || (int)((l >> 8) & 0xffu) >= nv || (int)((l >> 16) & 0xffu) >= nv ||
+        (int)(l >> 24) >= nv)
+      d.st->bad_mesh = 1;
+  }
+  if (d.voff != nullptr && t < d.n_patches) {
+    const int a = d.voff[t], b = d.voff[t + 1];
+    if (a < 0 || b < a || b > d.n_pverts || b - a > 256) d.st->bad_mesh = 1;
+    if (t == 0 && a != 0) d.st->bad_mesh = 1;
+    if (t == d.n_patches - 1 && b != d.n_pverts) d.st->bad_mesh = 1;
+    if (!d.st->bad_mesh) {
+      // local vertex -> corner lists: starts nondecreasing in [0, 4 nt], slots < 4 nt
+      const int nt = d.T - t * d.P < d.P ? d.T - t * d.P : d.P;
+      int prev = 0;
+      for (int k = a; k < b; ++k) {
+        const int st = d.pv_start[k];
+        if (st < prev || st > 4 * nt) d.st->bad_mesh = 1;
+        prev = st;
+      }
+      const uint16_t* sl = d.pv_slots + (size_t)4 * d.P * t;
+      for (int k = 0; k < 4 * nt; ++k)
+        if (sl[k] >= 4 * nt) d.st->bad_mesh = 1;
+    }
+  }
+  if (d.pverts != nullptr) {
+    for (int k = t; k < d.n_pverts; k += gridDim.x * blockDim.x)
+      if ((unsigned)d.pverts[k] >= (unsigned)d.V) d.st->bad_mesh = 1;
   }
   if (d.perm != nullptr && t < d.V) {
     if ((unsigned)d.perm[t] >= (unsigned)d.V) d.st->bad_mesh = 1;
@@ -494,6 +933,10 @@ struct Solver {
   Dev d{};
   int device = 0;
   int sm_count = 0;
+  int res_grid = 0;        // grid of the grid-stride residual kernels
+  int patch_grid = 0;      // grid of the persistent tile kernels
+  int patch1_grid = 0;     // grid of the one-CTA-per-patch residual
+  int tile_res_grid = 0;   // grid of the pipelined tile residual
   int max_records = 0;
   int cur = 0;  // buffer holding the current predicted positions
   cudaStream_t cap = nullptr;
@@ -540,7 +983,7 @@ inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 int check_params(const xpbd_params* p) {
   if (!p) return fail(XPBD_ERR_INVALID_ARGUMENT, "params is NULL");
   if (p->constraints_iter < 0) return fail(XPBD_ERR_INVALID_ARGUMENT, "constraints_iter < 0");
-  if (p->scatter != XPBD_SCATTER_ATOMIC && p->scatter != XPBD_SCATTER_GATHER)
+  if (p->scatter != XPBD_SCATTER_ATOMIC && p->scatter != XPBD_SCATTER_GATHER && p->scatter != XPBD_SCATTER_PATCH)
     return fail(XPBD_ERR_INVALID_ARGUMENT, "unknown scatter variant");
   if (!(p->lame_mu != 0.f) || !(p->lame_lambda != 0.f))
     return fail(XPBD_ERR_INVALID_ARGUMENT, "Lame parameters must be non-zero");
@@ -560,31 +1003,98 @@ int launch_begin(Solver* s, bool predict, bool sdf, float dt, cudaStream_t st) {
 }
 
 template <bool kBlockMode, bool kFirst, bool kPrecise>
-void launch_project_t(Solver* s, float dt, cudaStream_t st) {
+void launch_project_t(Solver* s, float cD, float cH, cudaStream_t st) {
   const int g = blocks_for(s->d.T);
   const xpbd_params& p = s->prm;
   if (p.scatter == XPBD_SCATTER_GATHER)
-    k_project<kBlockMode, kFirst, kPrecise, true><<<g, kBlock, 0, st>>>(
-        s->d, s->cur, dt, p.lame_mu, p.lame_lambda, p.hydrostatic_relaxation, p.deviatoric_relaxation);
+    k_project<kBlockMode, kFirst, kPrecise, true><<<g, kBlock, 0, st>>>(s->d, s->cur, cD, cH, p.hydrostatic_relaxation,
+                                                                        p.deviatoric_relaxation);
   else
-    k_project<kBlockMode, kFirst, kPrecise, false><<<g, kBlock, 0, st>>>(
-        s->d, s->cur, dt, p.lame_mu, p.lame_lambda, p.hydrostatic_relaxation, p.deviatoric_relaxation);
+    k_project<kBlockMode, kFirst, kPrecise, false><<<g, kBlock, 0, st>>>(s->d, s->cur, cD, cH, p.hydrostatic_relaxation,
+                                                                         p.deviatoric_relaxation);
+}
+
+template <bool kBlockMode, bool kFirst, bool kPrecise, int kP>
+void launch_project_patch_p(Solver* s, float cD, float cH, cudaStream_t st) {
+  const xpbd_params& p = s->prm;
+  if (p.patch_pipeline == 1 && kP == 256) {
+    const int g = s->d.n_patches < s->patch_grid ? s->d.n_patches : s->patch_grid;
+    k_project_tile<kBlockMode, kFirst, kPrecise><<<g, 256, sizeof(TileSmem<false>), st>>>(
+        s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
+  } else {
+    if (p.patch_reduce)
+      k_project_patch1<kBlockMode, kFirst, kPrecise, kP, true><<<s->d.n_patches, kP, 0, st>>>(
+          s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
+    else
+      k_project_patch1<kBlockMode, kFirst, kPrecise, kP, false><<<s->d.n_patches, kP, 0, st>>>(
+          s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
+  }
+}
+
+template <bool kBlockMode, bool kFirst, bool kPrecise>
+void launch_project_patch_t(Solver* s, float cD, float cH, cudaStream_t st) {
+  switch (s->d.P) {
+    case 256: launch_project_patch_p<kBlockMode, kFirst, kPrecise, 256>(s, cD, cH, st); break;
+    case 128: launch_project_patch_p<kBlockMode, kFirst, kPrecise, 128>(s, cD, cH, st); break;
+    default: launch_project_patch_p<kBlockMode, kFirst, kPrecise, 64>(s, cD, cH, st); break;
+  }
+}
+
+// 1 / (mu dt^2) and 1 / (lambda dt^2), rounded once from double
+inline void compliance_factors(const xpbd_params& p, float dt, float& cD, float& cH) {
+  const double dt2 = (double)dt * (double)dt;
+  cD = (float)(1.0 / ((double)p.lame_mu * dt2));
+  cH = (float)(1.0 / ((double)p.lame_lambda * dt2));
+}
+
+template <bool kBlockMode, bool kFirst, bool kPrecise>
+void launch_project_any(Solver* s, float cD, float cH, cudaStream_t st) {
+  if (s->prm.scatter == XPBD_SCATTER_PATCH) launch_project_patch_t<kBlockMode, kFirst, kPrecise>(s, cD, cH, st);
+  else launch_project_t<kBlockMode, kFirst, kPrecise>(s, cD, cH, st);
 }
 
 void launch_project(Solver* s, bool first, float dt, cudaStream_t st) {
   Prof prof(s, XPBD_K_PROJECT, st);
   const bool blk = s->prm.block_mode != 0, pr = s->prm.precise_hydro != 0;
+  float cD, cH;
+  compliance_factors(s->prm, dt, cD, cH);
   if (blk) {
-    if (first) pr ? launch_project_t<true, true, true>(s, dt, st) : launch_project_t<true, true, false>(s, dt, st);
-    else pr ? launch_project_t<true, false, true>(s, dt, st) : launch_project_t<true, false, false>(s, dt, st);
+    if (first) pr ? launch_project_any<true, true, true>(s, cD, cH, st) : launch_project_any<true, true, false>(s, cD, cH, st);
+    else pr ? launch_project_any<true, false, true>(s, cD, cH, st) : launch_project_any<true, false, false>(s, cD, cH, st);
   } else {
-    if (first) pr ? launch_project_t<false, true, true>(s, dt, st) : launch_project_t<false, true, false>(s, dt, st);
-    else pr ? launch_project_t<false, false, true>(s, dt, st) : launch_project_t<false, false, false>(s, dt, st);
+    if (first) pr ? launch_project_any<false, true, true>(s, cD, cH, st) : launch_project_any<false, true, false>(s, cD, cH, st);
+    else pr ? launch_project_any<false, false, true>(s, cD, cH, st) : launch_project_any<false, false, false>(s, cD, cH, st);
+  }
+}
+
+template <bool kRes, bool kMon, bool kPrecise, int kP>
+void launch_residual_patch_p(Solver* s, const SweepArgs& a, cudaStream_t st) {
+  const int n = s->d.n_patches;
+  if (s->prm.patch_pipeline == 1 && kP == 256) {
+    const int g = n < s->tile_res_grid ? n : s->tile_res_grid;
+    k_residual_tile<kRes, kMon, kPrecise><<<g, 256, sizeof(TileSmem<true>), st>>>(s->d, a);
+  } else {
+    const int g = n < s->patch1_grid ? n : s->patch1_grid;
+    k_residual_patch1<kRes, kMon, kPrecise, kP><<<g, kP, 0, st>>>(s->d, a);
+  }
+}
+
+template <bool kRes, bool kMon, bool kPrecise>
+void launch_residual_patch_t(Solver* s, const SweepArgs& a, cudaStream_t st) {
+  switch (s->d.P) {
+    case 256: launch_residual_patch_p<kRes, kMon, kPrecise, 256>(s, a, st); break;
+    case 128: launch_residual_patch_p<kRes, kMon, kPrecise, 128>(s, a, st); break;
+    default: launch_residual_patch_p<kRes, kMon, kPrecise, 64>(s, a, st); break;
   }
 }
 
 template <bool kRes, bool kMon>
 void launch_residual_t(Solver* s, const SweepArgs& a, int grid, cudaStream_t st) {
+  if (s->prm.scatter == XPBD_SCATTER_PATCH) {
+    if (s->prm.precise_hydro) launch_residual_patch_t<kRes, kMon, true>(s, a, st);
+    else launch_residual_patch_t<kRes, kMon, false>(s, a, st);
+    return;
+  }
   if (s->prm.precise_hydro) k_residual<kRes, kMon, true><<<grid, kBlock, 0, st>>>(s->d, a);
   else k_residual<kRes, kMon, false><<<grid, kBlock, 0, st>>>(s->d, a);
 }
@@ -601,18 +1111,16 @@ void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
   if (cheb || mon) {
     SweepArgs a;
     a.cur = s->cur;
-    a.dt = dt;
-    a.mu = p.lame_mu;
-    a.la = p.lame_lambda;
+    compliance_factors(p, dt, a.cD, a.cH);
     a.it = it;
     a.warmup = p.cheb_warmup;
     a.rec = rec;
+    a.reverse = p.sweep_order == 1 ? 1 : 0;
     a.rho_min = p.rho_min;
     a.rho_max = p.rho_max;
     a.rho_beta = p.rho_beta;
     int grid = blocks_for(s->d.T);
-    const int cap = s->sm_count * 4;
-    if (grid > cap) grid = cap;
+    if (grid > s->res_grid) grid = s->res_grid;
     if (grid < 1) grid = 1;
     Prof prof(s, XPBD_K_RESIDUAL, st);
     if (cheb && mon) launch_residual_t<true, true>(s, a, grid, st);
@@ -699,6 +1207,7 @@ const char* xpbd_status_string(int status) {
     case XPBD_ERR_NO_SDF: return "At least one SDF object must be provided.";
     case XPBD_ERR_BAD_MESH: return "bad mesh";
     case XPBD_ERR_HISTORY_FULL: return "history full";
+    case XPBD_ERR_TIMEOUT: return "device wait timed out";
     default: return "unknown status";
   }
 }
@@ -728,11 +1237,19 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
   if (body->n_verts <= 0 || body->n_tets <= 0) return fail(XPBD_ERR_BAD_MESH, "empty mesh");
   if ((long long)body->n_tets * 4 >= (1ll << 31)) return fail(XPBD_ERR_BAD_MESH, "too many tets");
   if (!body->x || !body->v || !body->p0 || !body->p1 || !body->dx || !body->tets || !body->dm_a || !body->dm_b ||
-      !body->dm_c || !body->lam)
+      !body->dm_c || !body->v0 || !body->lam)
     return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL body buffer");
   if (params->scatter == XPBD_SCATTER_GATHER && (!body->v2t_offsets || !body->v2t_slots || !body->corner_dx))
     return fail(XPBD_ERR_INVALID_ARGUMENT, "gather variant needs v2t_offsets, v2t_slots and corner_dx");
   if (max_records < 0) return fail(XPBD_ERR_INVALID_ARGUMENT, "max_records < 0");
+  const bool has_patch = body->tet_lid && body->patch_voff && body->patch_verts && body->pv_start && body->pv_slots;
+  if (params->scatter == XPBD_SCATTER_PATCH && !has_patch)
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "patch variant needs tet_lid, patch_voff, patch_verts, pv_start, pv_slots");
+  if (has_patch) {
+    const int P = body->patch_tets;
+    if (P != 64 && P != 128 && P != 256) return fail(XPBD_ERR_INVALID_ARGUMENT, "patch_tets must be 64, 128 or 256");
+    if (body->n_patches != (body->n_tets + P - 1) / P) return fail(XPBD_ERR_BAD_MESH, "n_patches != ceil(T / P)");
+  }
 
   Solver* s = new (std::nothrow) Solver();
   if (!s) return fail(XPBD_ERR_INVALID_ARGUMENT, "out of host memory");
@@ -750,12 +1267,22 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
   d.tets = reinterpret_cast<const int4*>(body->tets);
   d.dm_a = reinterpret_cast<const float4*>(body->dm_a);
   d.dm_b = reinterpret_cast<const float4*>(body->dm_b);
-  d.dm_c = reinterpret_cast<const float2*>(body->dm_c);
+  d.dm_c = body->dm_c;
+  d.v0 = body->v0;
   d.lam = reinterpret_cast<float2*>(body->lam);
   d.v2t_off = body->v2t_offsets;
   d.v2t_slot = body->v2t_slots;
   d.corner = reinterpret_cast<float4*>(body->corner_dx);
   d.perm = body->vert_perm;
+  if (has_patch) {
+    d.n_patches = body->n_patches;
+    d.P = body->patch_tets;
+    d.lid = body->tet_lid;
+    d.voff = body->patch_voff;
+    d.pverts = body->patch_verts;
+    d.pv_start = body->pv_start;
+    d.pv_slots = body->pv_slots;
+  }
   d.n_sdf = n_sdf;
   s->max_records = max_records;
 
@@ -776,6 +1303,35 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
   if (e == cudaSuccess) e = cudaMalloc(&d.hist, sizeof(double) * 4 * (size_t)(max_records > 0 ? max_records : 1));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cleanup(fail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
+  if (has_patch) {
+    e = cudaMemcpy(&d.n_pverts, d.voff + d.n_patches, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cleanup(fail(XPBD_ERR_CUDA, std::string("patch offsets: ") + cudaGetErrorString(e)));
+  }
+  {
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_residual<true, false, false>, kBlock, 0) != cudaSuccess ||
+        bps < 1)
+      bps = 2;
+    s->res_grid = s->sm_count * bps;
+    bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_project_tile<true, false, true>, 256,
+                                                      sizeof(TileSmem<false>)) != cudaSuccess ||
+        bps < 1)
+      bps = 2;
+    s->patch_grid = s->sm_count * bps;
+    bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_residual_tile<true, false, true>, 256,
+                                                      sizeof(TileSmem<true>)) != cudaSuccess ||
+        bps < 1)
+      bps = 2;
+    s->tile_res_grid = s->sm_count * bps;
+    bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_residual_patch1<true, false, true, 256>, 256, 0) !=
+            cudaSuccess ||
+        bps < 1)
+      bps = 2;
+    s->patch1_grid = s->sm_count * bps;
+  }
   DevState h{};
   h.rho_hat = 0.999;  // neohookean_solver.py:65
   h.omega = 1.0;
@@ -783,7 +1339,8 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
   if (e == cudaSuccess) e = cudaMemset(d.hist, 0, sizeof(double) * 4 * (size_t)(max_records > 0 ? max_records : 1));
   if (e != cudaSuccess) return cleanup(fail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
   // validate the mesh indices once, before any kernel gathers through them
-  const int nval = (d.T > d.V + 1 ? d.T : d.V + 1);
+  int nval = (d.T > d.V + 1 ? d.T : d.V + 1);
+  if (d.n_patches + 1 > nval) nval = d.n_patches + 1;
   k_validate<<<blocks_for(nval), kBlock>>>(d);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -819,6 +1376,8 @@ int xpbd_set_params(void* handle, const xpbd_params* params) {
   if (r != XPBD_OK) return r;
   if (params->scatter == XPBD_SCATTER_GATHER && (!s->d.v2t_off || !s->d.v2t_slot || !s->d.corner))
     return fail(XPBD_ERR_INVALID_ARGUMENT, "gather variant needs CSR buffers given at create");
+  if (params->scatter == XPBD_SCATTER_PATCH && !s->d.lid)
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "patch variant needs the patch layout given at create");
   if (std::memcmp(&s->prm, params, sizeof(xpbd_params)) != 0) drop_graph(s);
   s->prm = *params;
   return XPBD_OK;
@@ -1013,7 +1572,10 @@ int xpbd_check_status(void* handle, void* stream) {
   if (!s) return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle");
   int flag = 0;
   XPBD_CUDA(cudaMemcpyAsync(&flag, &s->d.st->nonfinite, sizeof(int), cudaMemcpyDeviceToHost, S(stream)));
+  int tmo = 0;
+  XPBD_CUDA(cudaMemcpyAsync(&tmo, &s->d.st->timeout, sizeof(int), cudaMemcpyDeviceToHost, S(stream)));
   XPBD_CUDA(cudaStreamSynchronize(S(stream)));
+  if (tmo) return fail(XPBD_ERR_TIMEOUT, "a bounded mbarrier wait timed out; results are invalid");
   return flag ? fail(XPBD_ERR_NONFINITE, "non-finite residual") : XPBD_OK;
 }
 

@@ -27,10 +27,11 @@ XPBD_OK = 0
 STATUS_NAMES = {
     0: "XPBD_OK", 1: "XPBD_ERR_INVALID_ARGUMENT", 2: "XPBD_ERR_CUDA",
     3: "XPBD_ERR_NONFINITE", 4: "XPBD_ERR_NO_SDF", 5: "XPBD_ERR_BAD_MESH",
-    6: "XPBD_ERR_HISTORY_FULL",
+    6: "XPBD_ERR_HISTORY_FULL", 7: "XPBD_ERR_TIMEOUT",
 }
 SDF_PLANE, SDF_SPHERE, SDF_CUBE = 0, 1, 2
-SCATTER_ATOMIC, SCATTER_GATHER = 0, 1
+SCATTER_ATOMIC, SCATTER_GATHER, SCATTER_PATCH = 0, 1, 2
+SCATTERS = {"atomic": SCATTER_ATOMIC, "gather": SCATTER_GATHER, "patch": SCATTER_PATCH}
 FIELD_X, FIELD_V, FIELD_PRED_X = 0, 1, 2
 KERNEL_CLASSES = ("begin", "project", "gather", "residual", "update", "end")
 
@@ -51,6 +52,8 @@ class XpbdParams(ctypes.Structure):
                 ("block_mode", ctypes.c_int32), ("constraints_iter", ctypes.c_int32),
                 ("monitor", ctypes.c_int32), ("precise_hydro", ctypes.c_int32),
                 ("scatter", ctypes.c_int32), ("use_graph", ctypes.c_int32),
+                ("sweep_order", ctypes.c_int32), ("patch_pipeline", ctypes.c_int32),
+                ("patch_reduce", ctypes.c_int32),
                 ("rho_min", ctypes.c_double), ("rho_max", ctypes.c_double),
                 ("rho_beta", ctypes.c_double)]
 
@@ -61,9 +64,12 @@ _P = ctypes.c_void_p
 class XpbdBody(ctypes.Structure):
     _fields_ = [("n_verts", ctypes.c_int32), ("n_tets", ctypes.c_int32),
                 ("x", _P), ("v", _P), ("p0", _P), ("p1", _P), ("dx", _P),
-                ("tets", _P), ("dm_a", _P), ("dm_b", _P), ("dm_c", _P), ("lam", _P),
+                ("tets", _P), ("dm_a", _P), ("dm_b", _P), ("dm_c", _P), ("v0", _P), ("lam", _P),
                 ("v2t_offsets", _P), ("v2t_slots", _P), ("corner_dx", _P),
-                ("vert_perm", _P)]
+                ("vert_perm", _P),
+                ("n_patches", ctypes.c_int32), ("patch_tets", ctypes.c_int32),
+                ("tet_lid", _P), ("patch_voff", _P), ("patch_verts", _P),
+                ("pv_start", _P), ("pv_slots", _P)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/xpbd_gb300.h
@@ -95,6 +101,9 @@ _SIGNATURES = {
                                          ctypes.c_int32, ctypes.c_int32, _P]),
     "xpbd_morton_order": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int32, _P, _P]),
     "xpbd_build_vertex_csr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
+    "xpbd_build_patch_csr": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
+    "xpbd_build_patches": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P,
+                                          ctypes.POINTER(ctypes.c_int32)]),
 }
 
 _lock = threading.Lock()

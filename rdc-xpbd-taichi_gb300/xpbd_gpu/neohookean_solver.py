@@ -55,7 +55,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
                  reorder_all=False, block_size=256, hydrostatic_relaxation=1.2, deviatoric_relaxation=1.2,
                  cheb_enable=True, cheb_warmup=5, cheb_gamma=0.6666, block_neohookean_enable=False,
                  monitor_convergence=False, *, total_mass=1.0, density=None, gravity=(0.0, -9.8, 0.0),
-                 scatter="atomic", precise_hydro=None, use_graph=True, reorder=True):
+                 scatter="patch", precise_hydro=None, use_graph=True, reorder=True, sweep_order=1,
+                 patch_pipeline=0, patch_reduce=0):
         self.constraints_iter = constraints_iter
         self.hydrostatic_relaxation = hydrostatic_relaxation
         self.deviatoric_relaxation = deviatoric_relaxation
@@ -81,9 +82,12 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         self._time_done = 0.0
         self.solve_compute_calls = 0
         self.solve_compute_iterations = 0
-        if scatter not in ("atomic", "gather"):
-            raise ValueError("scatter must be 'atomic' or 'gather'")
+        if scatter not in _native.SCATTERS:
+            raise ValueError("scatter must be one of %s" % sorted(_native.SCATTERS))
         self.scatter = scatter
+        self.sweep_order = int(sweep_order)
+        self.patch_pipeline = int(patch_pipeline)
+        self.patch_reduce = int(patch_reduce)
         self.precise_hydro = (poisson_ratio >= 0.49) if precise_hydro is None else bool(precise_hydro)
         self.use_graph = bool(use_graph)
         self.block_size = block_size
@@ -97,6 +101,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         self._upload(x, V0, inv_Dm, m, inv_m)
         if self.scatter == "gather":
             self._ensure_gather_buffers()
+        if self.scatter == "patch" and not self._ensure_patch_buffers():
+            raise ValueError("mesh has patches with more than 256 vertices even at 64 tets per patch")
         self._build_mesh_view()
         self._max_records = max(1, self._records_per_frame())
         prm = self._params()
@@ -126,8 +132,11 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         p.constraints_iter = int(self.constraints_iter)
         p.monitor = 1 if self.monitor_convergence else 0
         p.precise_hydro = 1 if self.precise_hydro else 0
-        p.scatter = _native.SCATTER_GATHER if self.scatter == "gather" else _native.SCATTER_ATOMIC
+        p.scatter = _native.SCATTERS[self.scatter]
         p.use_graph = 1 if self.use_graph else 0
+        p.sweep_order = self.sweep_order
+        p.patch_pipeline = self.patch_pipeline
+        p.patch_reduce = self.patch_reduce
         p.rho_min, p.rho_max, p.rho_beta = self.rho_min, self.rho_max, self.rho_beta
         return p
 
@@ -135,6 +144,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         super()._sync()
         if self.scatter == "gather" and self._corner is None:
             raise RuntimeError("scatter='gather' needs the CSR buffers built at construction")
+        if self.scatter == "patch" and self._tet_lid is None:
+            raise RuntimeError("scatter='patch' needs the patch layout built at construction")
         prm = self._params()
         b = bytes(prm)
         if b != self._prm_bytes:

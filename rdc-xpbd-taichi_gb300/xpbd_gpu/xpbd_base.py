@@ -8,8 +8,9 @@ arguments, ``mesh.verts.{x,pred_x,v,m,inv_m}``, ``indices``, ``sdfs``/``sdf``,
 Layout on the device (torch CUDA tensors, handed to ``libxpbd_gb300.so`` as
 raw pointers): per vertex float4 ``x``, ``v``, two predicted-position buffers
 ``p0``/``p1`` and the Jacobi accumulator ``dx``; per tet ``int4`` corner ids,
-``inv_Dm`` + ``V0`` as float4/float4/float2 and ``(lambda_D, lambda_H)`` as
-float2.  Vertices and tets are stored in Morton order; the field accessors
+``inv_Dm`` as float4/float4/float, ``V0`` and ``(lambda_D, lambda_H)`` as
+float2 (tet records padded to a multiple of 256 tets), plus, for the tile
+variant, 4 u8 patch-local corner ids per tet and the patch vertex lists.  Vertices and tets are stored in Morton order; the field accessors
 return and accept arrays in the caller's (file) order.
 """
 import os
@@ -261,10 +262,15 @@ class XPBDSolverBase:
         x4 = np.zeros((V, 4), dtype=np.float32)
         x4[:, :3] = x[vperm]
         x4[:, 3] = inv_m[vperm]
-        D = inv_Dm[tperm].reshape(T, 9).astype(np.float32)
+        # tet records are padded to a multiple of the largest patch (256 tets)
+        # so that every patch's slice can be bulk-copied whole
+        Tp = -(-T // 256) * 256
+        D = np.zeros((Tp, 9), dtype=np.float32)
+        D[:T] = inv_Dm[tperm].reshape(T, 9)
         dm_a = np.ascontiguousarray(D[:, 0:4])
         dm_b = np.ascontiguousarray(D[:, 4:8])
-        dm_c = np.stack([D[:, 8], V0[tperm].astype(np.float32)], axis=1)
+        dm_c = np.ascontiguousarray(D[:, 8])
+        v0 = V0[tperm].astype(np.float32)
 
         def dt_(a, dtype=torch.float32):
             return torch.from_numpy(np.ascontiguousarray(a)).to(device=dev, dtype=dtype)
@@ -275,10 +281,13 @@ class XPBDSolverBase:
         self._dx4 = torch.zeros((V, 4), dtype=torch.float32, device=dev)
         self._tets = dt_(tets_new, torch.int32)
         self._dm_a, self._dm_b, self._dm_c = dt_(dm_a), dt_(dm_b), dt_(dm_c)
-        self._lam = torch.zeros((T, 2), dtype=torch.float32, device=dev)
+        self._v0 = dt_(v0)
+        self._lam = torch.zeros((Tp, 2), dtype=torch.float32, device=dev)
         self._perm = dt_(vperm, torch.int32)
         self._stage = torch.empty((V, 3), dtype=torch.float32, device=dev)
         self._v2t_off = self._v2t_slots = self._corner = None
+        self._tet_lid = self._patch_voff = self._patch_verts = None
+        self._patch_tets = 0
         self._host_m = m
         self._host_inv_m = inv_m.copy()
 
@@ -295,6 +304,38 @@ class XPBDSolverBase:
         self._v2t_slots = torch.from_numpy(slots).to(self._device)
         self._corner = torch.zeros((4 * T, 4), dtype=torch.float32, device=self._device)
 
+    def _ensure_patch_buffers(self):
+        """Patches of P Morton-consecutive tets with <= 256 vertices each
+        (P = 256, else 128, else 64); returns False if no P fits."""
+        if self._tet_lid is not None:
+            return True
+        torch = _torch()
+        V, T = self.n_verts, self.n_tets
+        tt = np.ascontiguousarray(self._tets_solver)
+        for P in (256, 128, 64):
+            npat = (T + P - 1) // P
+            voff = np.empty(npat + 1, dtype=np.int32)
+            pverts = np.empty(4 * T, dtype=np.int32)
+            lid = np.zeros(-(-T // 256) * 256, dtype=np.uint32)
+            mx = _native.ctypes.c_int32()
+            _native.check(self._lib.xpbd_build_patches(tt.ctypes.data, T, V, P, voff.ctypes.data, pverts.ctypes.data,
+                                                       lid.ctypes.data, _native.ctypes.byref(mx)))
+            if mx.value <= 256:
+                self._patch_tets = P
+                self._n_patches = npat
+                self._tet_lid = torch.from_numpy(lid.view(np.int32)).to(self._device)
+                self._patch_voff = torch.from_numpy(voff).to(self._device)
+                self._patch_verts = torch.from_numpy(pverts[:voff[-1]].copy()).to(self._device)
+                self.patch_max_verts = mx.value
+                pv_start = np.empty(int(voff[-1]), dtype=np.uint16)
+                pv_slots = np.empty(4 * npat * P, dtype=np.uint16)
+                _native.check(self._lib.xpbd_build_patch_csr(voff.ctypes.data, lid.ctypes.data, T, P,
+                                                             pv_start.ctypes.data, pv_slots.ctypes.data))
+                self._pv_start = torch.from_numpy(pv_start.view(np.int16)).to(self._device)
+                self._pv_slots = torch.from_numpy(pv_slots.view(np.int16)).to(self._device)
+                return True
+        return False
+
     def _body(self):
         b = _native.XpbdBody()
         b.n_verts, b.n_tets = self.n_verts, self.n_tets
@@ -303,7 +344,15 @@ class XPBDSolverBase:
         b.dx = self._dx4.data_ptr()
         b.tets = self._tets.data_ptr()
         b.dm_a, b.dm_b, b.dm_c = self._dm_a.data_ptr(), self._dm_b.data_ptr(), self._dm_c.data_ptr()
+        b.v0 = self._v0.data_ptr()
         b.lam = self._lam.data_ptr()
+        if self._tet_lid is not None:
+            b.n_patches, b.patch_tets = self._n_patches, self._patch_tets
+            b.tet_lid = self._tet_lid.data_ptr()
+            b.patch_voff = self._patch_voff.data_ptr()
+            b.patch_verts = self._patch_verts.data_ptr()
+            b.pv_start = self._pv_start.data_ptr()
+            b.pv_slots = self._pv_slots.data_ptr()
         if self._corner is not None:
             b.v2t_offsets = self._v2t_off.data_ptr()
             b.v2t_slots = self._v2t_slots.data_ptr()
@@ -326,10 +375,10 @@ class XPBDSolverBase:
             m=VertexScalarField(self, "m"),
             inv_m=VertexScalarField(self, "inv_m")))
         cells = ElementSet(self.n_tets, dict(
-            V0=CellField(self, lambda: self._cell_array(self._dm_c[:, 1])),
+            V0=CellField(self, lambda: self._cell_array(self._v0)),
             inv_Dm=CellField(self, self._inv_dm_array),
-            lambda_D=CellField(self, lambda: self._cell_array(self._lam[:, 0])),
-            lambda_H=CellField(self, lambda: self._cell_array(self._lam[:, 1]))))
+            lambda_D=CellField(self, lambda: self._cell_array(self._lam[:self.n_tets, 0])),
+            lambda_H=CellField(self, lambda: self._cell_array(self._lam[:self.n_tets, 1]))))
         self.mesh = DeviceMesh(self._rest.points, verts, cells)
 
     # -- device access helpers -------------------------------------------------
@@ -343,8 +392,9 @@ class XPBDSolverBase:
         return out
 
     def _inv_dm_array(self):
-        D = np.concatenate([self._dm_a.cpu().numpy(), self._dm_b.cpu().numpy(),
-                            self._dm_c[:, :1].cpu().numpy()], axis=1).reshape(-1, 3, 3)
+        T = self.n_tets
+        D = np.concatenate([self._dm_a[:T].cpu().numpy(), self._dm_b[:T].cpu().numpy(),
+                            self._dm_c[:T].cpu().numpy()[:, None]], axis=1).reshape(-1, 3, 3)
         out = np.empty_like(D)
         out[self._tperm] = D
         return out

@@ -110,3 +110,40 @@ def test_vertex_csr(native_lib):
 
 def test_device_count_without_gpu_is_zero_or_more(native_lib):
     assert native_lib.xpbd_device_count() >= 0
+
+
+def test_build_patches_layout(native_lib):
+    m = kuhn_grid(6, 5, 4, 1.0, jitter=0.1, seed=1)
+    V, T = m.n_verts, m.n_tets
+    tt = np.ascontiguousarray(m.tets, dtype=np.int32)
+    for P in (256, 128, 64):
+        npat = (T + P - 1) // P
+        voff = np.empty(npat + 1, dtype=np.int32)
+        pv = np.empty(4 * T, dtype=np.int32)
+        lid = np.empty(T, dtype=np.uint32)
+        mx = ctypes.c_int32()
+        assert native_lib.xpbd_build_patches(tt.ctypes.data, T, V, P, voff.ctypes.data, pv.ctypes.data,
+                                             lid.ctypes.data, ctypes.byref(mx)) == 0
+        assert voff[0] == 0 and np.all(np.diff(voff) > 0) and mx.value == np.diff(voff).max() <= 256
+        for p in range(npat):
+            verts = pv[voff[p]:voff[p + 1]]
+            assert np.all(np.diff(verts) > 0)
+            for t in range(p * P, min(T, (p + 1) * P)):
+                loc = [(int(lid[t]) >> (8 * q)) & 0xFF for q in range(4)]
+                assert list(verts[loc]) == list(m.tets[t])
+        start = np.empty(voff[-1], dtype=np.uint16)
+        slots = np.empty(4 * npat * P, dtype=np.uint16)
+        assert native_lib.xpbd_build_patch_csr(voff.ctypes.data, lid.ctypes.data, T, P, start.ctypes.data,
+                                               slots.ctypes.data) == 0
+        for p in range(npat):
+            nv = voff[p + 1] - voff[p]
+            ntet = min(T, (p + 1) * P) - p * P
+            blk = slots[4 * P * p: 4 * P * (p + 1)]
+            st = list(start[voff[p]:voff[p + 1]]) + [4 * ntet]
+            assert np.all(blk[4 * ntet:] == 0xFFFF)
+            for k in range(nv):
+                seg = blk[st[k]:st[k + 1]]
+                assert np.all(np.diff(seg.astype(int)) > 0)
+                for sl in seg:
+                    t, q = p * P + int(sl) // 4, int(sl) % 4
+                    assert (int(lid[t]) >> (8 * q)) & 0xFF == k

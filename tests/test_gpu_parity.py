@@ -29,10 +29,15 @@ def make_solver(d, **over):
 
 
 @pytest.mark.parametrize("name", gc.golden_names())
-@pytest.mark.parametrize("scatter", ["atomic", "gather"])
+@pytest.mark.parametrize("scatter", ["atomic", "gather", "patch", "patch-tma", "patch-reduce"])
 def test_frames_match_reference(name, scatter):
     d = gc.load(name)
-    s = make_solver(d, scatter=scatter, monitor_convergence=False)
+    if scatter == "patch-tma":
+        s = make_solver(d, scatter="patch", patch_pipeline=1, monitor_convergence=False)
+    elif scatter == "patch-reduce":
+        s = make_solver(d, scatter="patch", patch_reduce=1, monitor_convergence=False)
+    else:
+        s = make_solver(d, scatter=scatter, monitor_convergence=False)
     diag = gc.bbox_diag(d["x_init"])
     np.testing.assert_allclose(s.mesh.verts.x.to_numpy(), d["x_init"], rtol=0, atol=1e-6 * diag)
     np.testing.assert_array_equal(s.mesh.verts.inv_m.to_numpy() == 0, d["inv_m"] == 0)
@@ -54,9 +59,10 @@ def test_frames_match_reference(name, scatter):
 
 
 @pytest.mark.parametrize("name", ["kuhn2_block_cheb", "kuhn2_split_nocheb", "kuhn3_block_cheb_nu049"])
-def test_monitoring_records_match_reference(name):
+@pytest.mark.parametrize("scatter", ["atomic", "patch"])
+def test_monitoring_records_match_reference(name, scatter):
     d = gc.load(name)
-    s = make_solver(d, monitor_convergence=True)
+    s = make_solver(d, monitor_convergence=True, scatter=scatter)
     seen = []
     s.convergence_callback = lambda frame, substep, recs: seen.append((frame, substep, len(recs)))
     for _ in range(int(d["frames"])):
@@ -113,7 +119,8 @@ def test_granular_methods_equal_fused_substep():
     assert a.rho_hat == b.rho_hat
 
 
-def test_one_frame_against_f32_oracle_larger_grid():
+@pytest.mark.parametrize("scatter", ["atomic", "patch"])
+def test_one_frame_against_f32_oracle_larger_grid(scatter):
     """A 6x6x6 Kuhn body (1,296 tets) dropped on the plane + sphere scene, one
     frame of 5 substeps x 20 iterations, against the float64 oracle."""
     from oracle.xpbd_oracle import OracleSdf, OracleSolver
@@ -127,7 +134,8 @@ def test_one_frame_against_f32_oracle_larger_grid():
     o = OracleSolver(m.points, m.tets, [OracleSdf("plane", point=[0, 0, 0], dir=[0, 1, 0], fixed=True),
                                         OracleSdf("sphere", center=[0.5, 0.3, 0.5], radius=0.3, fixed=True)],
                      dtype=np.float64, **kw)
-    s = XPBDNeoHookeanSolver(m, [PlaneSdf([0, 0, 0], [0, 1, 0], True), SphereSdf([0.5, 0.3, 0.5], 0.3, True)], **kw)
+    s = XPBDNeoHookeanSolver(m, [PlaneSdf([0, 0, 0], [0, 1, 0], True), SphereSdf([0.5, 0.3, 0.5], 0.3, True)],
+                             scatter=scatter, **kw)
     diag = gc.bbox_diag(m.points)
     for f in range(8):
         o.solve()
