@@ -207,7 +207,7 @@ def run_gb300(args):
 
     mesh, specs, kw, desc = workload(args.workload)
     solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
-                                  patch_pipeline=args.patch_pipeline, **kw)
+                                  patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce, **kw)
     frame_units = tet_iterations_per_frame(mesh, kw)
     n_chunks = len(frame_chunks(kw["frame_dt"], kw["dt"]))
     per_iter = 3 + (1 if args.scatter == "gather" else 0)
@@ -284,12 +284,20 @@ def run_gb300(args):
         peak, peak_src = 6800.0, "fallback"
     K = kw["constraints_iter"]
     n_proj = prof["project"]["launches"]
-    # algorithmic bytes of one projection launch: per tet 16 (ids) + 40 (inv_Dm, V0)
-    # + 8 lambda read (not on the first iteration) + 8 lambda write; per vertex
-    # 16 gather + 16 scatter
-    proj_bytes = (72.0 * T + 32.0 * V) * (K - 1) / K + (64.0 * T + 32.0 * V) / K
+    # algorithmic bytes of one projection launch (per-unit figures of the
+    # reference-semantics accounting): per tet 16 ids + 36 inv_Dm + 4 V0 +
+    # 8 lambda read + 8 lambda write = 72 B; per vertex 16 gather + 16 scatter
+    proj_bytes = 72.0 * T + 32.0 * V
     proj_ms = prof["project"]["ms"] / max(1, n_proj)
     achieved = proj_bytes / (proj_ms * 1e-3) / 1e9
+    kernel_name = {"patch": "k_project_patch1 (tile, 256-tet patches, red.global.add.v4 per corner)",
+                   "atomic": "k_project (one thread per tet, red.global.add.v4 per corner)",
+                   "gather": "k_project (per-corner buffer + deterministic vertex gather)"}[args.scatter]
+    # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this
+    # workload, from the ncu captures summarised in profiles/k_project_*_c2_64cube.md
+    traffic = {"patch": 89.4e6, "atomic": 115.2e6}.get(args.scatter)
+    if args.patch_pipeline != 0 or args.patch_reduce != 0 or args.workload != "c2":
+        traffic = None
     iter_bytes = 136.0 * T + 128.0 * V
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -301,9 +309,9 @@ def run_gb300(args):
                    "parallelism": "replicas" if world > 1 else "single GPU", "graph": "one CUDA graph per frame"},
         "frames_per_s": 1e3 / ms_per_step * world,
         "gpu_launches": launches_per_frame * args.steps,
-        "roofline": {"bound": "hbm", "kernel": "k_project (block 2x2 + red.global.add.v4)",
+        "roofline": {"bound": "hbm", "kernel": kernel_name,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "traffic": None,
+                     "peak_source": peak_src, "traffic": traffic,
                      "bytes_per_launch": proj_bytes, "ms_per_launch": proj_ms},
         "iteration_roofline": {"bytes_per_iteration": iter_bytes,
                                "achieved_GBps": iter_bytes * K * n_chunks * kw["substeps_num"] / (ms_per_step * 1e-3) / 1e9,
@@ -326,7 +334,8 @@ def run_profile(args):
     from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
     mesh, specs, kw, desc = workload(args.workload)
     solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
-                                  patch_pipeline=args.patch_pipeline, use_graph=False, **kw)
+                                  patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce,
+                                  use_graph=False, **kw)
     for _ in range(args.profile_frames):
         solver.solve()
     torch.cuda.synchronize()
@@ -344,6 +353,7 @@ def main():
     ap.add_argument("--scatter", default="patch", choices=["atomic", "gather", "patch"])
     ap.add_argument("--sweep-order", type=int, default=1, choices=[0, 1])
     ap.add_argument("--patch-pipeline", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--patch-reduce", type=int, default=0, choices=[0, 1])
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-iters", type=int, default=3)

@@ -102,7 +102,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         if self.scatter == "gather":
             self._ensure_gather_buffers()
         if self.scatter == "patch" and not self._ensure_patch_buffers():
-            raise ValueError("mesh has patches with more than 256 vertices even at 64 tets per patch")
+            # no patch size keeps every patch within 256 vertices: per-tet variant
+            self.scatter = "atomic"
         self._build_mesh_view()
         self._max_records = max(1, self._records_per_frame())
         prm = self._params()
