@@ -241,6 +241,71 @@ int xpbd_build_patch_csr(const int32_t* patch_voff, const uint32_t* tet_lid, int
 int xpbd_build_vertex_csr(const int32_t* tets, int32_t n_tets, int32_t n_verts,
                           int32_t* offsets /* [V+1] */, int32_t* slots /* [4T] */);
 
+/* ------------------------------------------------------------------------
+ * Batched form: many independent bodies of uneven size in one set of
+ * launches.  The reference steps one body per solver object
+ * (neohookean_solver.py:16-587); a batch replaces a list of such solvers that
+ * share the SDF list, time step and iteration settings, each body keeping its
+ * own Lame parameters and Chebyshev state (rho_hat persists per body).
+ * Every body's tets are padded to a multiple of 256 (one patch = 256 tets of
+ * one body) and its vertices to a multiple of 256 (one vertex block = 256
+ * vertices of one body); padding vertices have inv_m = 0 and vert_perm = -1.
+ * ------------------------------------------------------------------------ */
+typedef struct xpbd_batch {
+  int32_t n_bodies;
+  int32_t n_verts;            /* padded total, multiple of 256 */
+  int32_t n_tets;             /* padded total = 256 * n_patches */
+  int32_t n_patches;
+  int32_t n_patch_verts;      /* patch_voff[n_patches] */
+  int32_t n_out_verts;        /* caller vertices (sum of real vertex counts) */
+  float* x;                   /* [V][4] w = inv_m */
+  float* v;                   /* [V][4] */
+  float* p0;                  /* [V][4] */
+  float* p1;                  /* [V][4] */
+  float* dx;                  /* [V][4] zero at create */
+  const float* dm_a;          /* [T][4] */
+  const float* dm_b;          /* [T][4] */
+  const float* dm_c;          /* [T] */
+  float* lam;                 /* [T][2] */
+  const uint32_t* tet_lid;    /* [T] 4 u8 patch-local corner ids */
+  const int32_t* patch_voff;  /* [n_patches+1] */
+  const int32_t* patch_verts; /* [n_patch_verts] */
+  const int32_t* patch_body;  /* [n_patches] */
+  const int32_t* patch_ntets; /* [n_patches] real tets of the patch */
+  const int32_t* vblock_body; /* [V/256] */
+  const float* body_inv_mu;   /* [n_bodies] 1 / mu */
+  const float* body_inv_lambda; /* [n_bodies] 1 / lambda */
+  const int32_t* body_n_patches; /* [n_bodies] */
+  const int32_t* body_n_tets; /* [n_bodies] real tets (r_hat = sum / n) */
+  const int32_t* vert_perm;   /* [V] caller vertex of each solver vertex, -1 for padding */
+} xpbd_batch;
+
+/* Message of the last batch failure on the calling thread. */
+const char* xpbd_batch_last_error(void);
+
+/* Create a batch (params: lame_mu / lame_lambda unused, per body instead). */
+int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* batch, const xpbd_sdf* sdfs, int32_t n_sdf,
+                      int32_t max_records, void** out_handle);
+int xpbd_batch_destroy(void* handle);
+
+/* One substep of every body (neohookean_solver.py:577-579). */
+int xpbd_batch_substep(void* handle, float dt, int32_t record_base, void* stream);
+
+/* One frame of every body (neohookean_solver.py:562-587), cached CUDA graph. */
+int xpbd_batch_solve(void* handle, double frame_dt, double dt, int32_t substeps, void* stream);
+
+/* History rows [0, n) of every body, host layout [n_bodies][n][4]; synchronises. */
+int xpbd_batch_read_history(void* handle, double* host_out, int32_t n, void* stream);
+
+/* rho_hat of every body (host [n_bodies]); synchronises. */
+int xpbd_batch_get_rho_hat(void* handle, double* host_out, void* stream);
+
+int xpbd_batch_check_status(void* handle, void* stream);
+int xpbd_batch_import_vec3(void* handle, int32_t field, const float* src, void* stream);
+int xpbd_batch_export_vec3(void* handle, int32_t field, float* dst, void* stream);
+int xpbd_batch_set_profiling(void* handle, int32_t enable);
+int xpbd_batch_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, int32_t reset, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

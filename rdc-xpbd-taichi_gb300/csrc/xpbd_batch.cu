@@ -1,0 +1,771 @@
+// Batched RDC-XPBD substep: many independent bodies of uneven size stepped by
+// one launch per phase.
+//
+// Layout: every body's tets are padded to a multiple of 256 and its vertices
+// to a multiple of 256, then all bodies are concatenated.  A 256-tet patch
+// (the tile unit of the single-body kernels) therefore belongs to exactly one
+// body (patch_body), and so does every 256-vertex block (vblock_body).  Each
+// body carries its own Lame parameters, FP64 Chebyshev state (rho_hat,
+// prev_r_hat, omega) and residual accumulators; the residual sweep's per-body
+// ticket lets the last patch CTA of a body apply that body's rho_hat / omega
+// recurrence (neohookean_solver.py:495-504, :537-546), so bodies never wait
+// for each other and no grid-wide barrier is needed.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "xpbd_device.cuh"
+
+namespace xpbd {
+namespace batch {
+
+constexpr int kP = 256;
+
+struct BodyState {
+  double acc[3];
+  unsigned int ticket;
+  int has_prev;
+  double rho_hat;
+  double prev_r_hat;
+  double omega;
+};
+
+struct Flags {
+  int nonfinite;
+  int bad_mesh;
+};
+
+struct BDev {
+  int V, T, n_patches, n_bodies, n_sdf, n_pverts;
+  float4* x;
+  float4* v;
+  float4* p[2];
+  float4* dx;
+  const float4* dm_a;
+  const float4* dm_b;
+  const float* dm_c;
+  float2* lam;
+  const uint32_t* lid;
+  const int* voff;
+  const int* pverts;
+  const int* patch_body;
+  const int* patch_ntets;
+  const int* vblock_body;
+  const float* inv_mu;
+  const float* inv_la;
+  const int* body_patches;
+  const int* body_tets;
+  const int* perm;
+  const xpbd_sdf* sdfs;
+  BodyState* bs;
+  Flags* flags;
+  double* hist;  // [n_bodies][max_records][4]
+  int max_records;
+};
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+__device__ __forceinline__ float det9(const float m[9]) {
+  return m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) + m[6] * (m[1] * m[5] - m[4] * m[2]);
+}
+
+__device__ __forceinline__ float3 post_position(const float4 p, const float4 D) {
+  float3 r = make_float3(p.x, p.y, p.z);
+  if (D.w > 0.f) {
+    r.x += D.x / D.w;
+    r.y += D.y / D.w;
+    r.z += D.z / D.w;
+  }
+  return r;
+}
+
+// Begin of a substep for every body: per-body reset of prev_r_hat / omega
+// (neohookean_solver.py:461, :466) and predict + sequential SDF projection.
+__global__ void __launch_bounds__(256) kb_begin(BDev d, float dt, float gx, float gy, float gz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0)
+    for (int b = threadIdx.x; b < d.n_bodies; b += blockDim.x) {
+      d.bs[b].has_prev = 0;
+      d.bs[b].omega = 1.0;
+    }
+  if (i >= d.V) return;
+  const float4 xi = d.x[i];
+  float4 vi = d.v[i];
+  const float w = xi.w;
+  if (w > 0.f) {
+    vi.x += gx * dt;
+    vi.y += gy * dt;
+    vi.z += gz * dt;
+    d.v[i] = vi;
+  }
+  float3 p = make_float3(xi.x + vi.x * dt, xi.y + vi.y * dt, xi.z + vi.z * dt);
+  if (w > 0.f) sdf_project_all(d.sdfs, d.n_sdf, p, make_float3(vi.x, vi.y, vi.z));
+  d.p[0][i] = make_float4(p.x, p.y, p.z, w);
+}
+
+__global__ void __launch_bounds__(256) kb_end(BDev d, int cur, float dt, float damping) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.V) return;
+  const float4 xi = d.x[i];
+  if (xi.w <= 0.f) {
+    d.p[cur][i] = xi;
+    return;
+  }
+  const float4 pi = d.p[cur][i];
+  const float e = expf(-dt * damping);
+  const float4 vi = d.v[i];
+  d.v[i] = make_float4((pi.x - xi.x) / dt * e, (pi.y - xi.y) / dt * e, (pi.z - xi.z) / dt * e, vi.w);
+  d.x[i] = make_float4(pi.x, pi.y, pi.z, xi.w);
+}
+
+// Projection, one CTA per patch (the single-body tile kernel with per-body
+// compliance 1 / (mu_b dt^2), 1 / (lambda_b dt^2)).
+template <bool kBlockMode, bool kFirst, bool kPrecise>
+__global__ void __launch_bounds__(kP) kb_project(BDev d, int cur, float inv_dt2, float relax_h, float relax_d) {
+  __shared__ float4 sp[256];
+  __shared__ int sg[256];
+  const int p = blockIdx.x;
+  const int b = __ldg(d.patch_body + p);
+  const int vb = __ldg(d.voff + p);
+  const int nv = __ldg(d.voff + p + 1) - vb;
+  const int nt = __ldg(d.patch_ntets + p);
+  const int t = p * kP + threadIdx.x;
+  const bool has = threadIdx.x < nt;
+  Tet tt;
+  uint32_t lid = 0;
+  float2 L = make_float2(0.f, 0.f);
+  if (has) {
+    const float4 A = __ldg(d.dm_a + t), B = __ldg(d.dm_b + t);
+    tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+    tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+    tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
+    lid = __ldg(d.lid + t);
+    if (!kFirst) L = d.lam[t];
+  }
+  const float4* P = d.p[cur];
+  for (int j = threadIdx.x; j < nv; j += kP) {
+    const int g = __ldg(d.pverts + vb + j);
+    sg[j] = g;
+    sp[j] = ldg4(P + g);
+  }
+  __syncthreads();
+  if (!has) return;
+  const float cD = __ldg(d.inv_mu + b) * inv_dt2, cH = __ldg(d.inv_la + b) * inv_dt2;
+  const int l[4] = {(int)(lid & 0xffu), (int)((lid >> 8) & 0xffu), (int)((lid >> 16) & 0xffu), (int)(lid >> 24)};
+#pragma unroll
+  for (int c = 0; c < 4; ++c) tt.p[c] = sp[l[c]];
+  const float six_det = 6.f * det9(tt.dm);
+  float3 dp[4];
+  float cnt;
+  project_tet<kBlockMode, kPrecise>(tt, six_det * cD, six_det * cH, relax_h, relax_d, L, dp, cnt);
+  d.lam[t] = L;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) red_add_v4(d.dx + sg[l[c]], dp[c].x, dp[c].y, dp[c].z, cnt);
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+struct BSweep {
+  int cur;
+  float inv_dt2;
+  int it, warmup, rec;
+  double rho_min, rho_max, rho_beta;
+};
+
+// Residual (neohookean_solver.py:298-329) and monitoring sums (:256-296) of one
+// patch, added to its body's FP64 accumulators; the body's last patch applies
+// the rho_hat / omega recurrence and writes the body's history row.
+template <bool kRes, bool kMon, bool kPrecise>
+__global__ void __launch_bounds__(kP) kb_residual(BDev d, BSweep a) {
+  __shared__ float4 sp[256];
+  __shared__ double red[3][kP / 32];
+  __shared__ bool last;
+  const int p = blockIdx.x;
+  const int b = __ldg(d.patch_body + p);
+  const int vb = __ldg(d.voff + p);
+  const int nv = __ldg(d.voff + p + 1) - vb;
+  const int nt = __ldg(d.patch_ntets + p);
+  const int t = p * kP + threadIdx.x;
+  const bool has = threadIdx.x < nt;
+  Tet tt;
+  uint32_t lid = 0;
+  float2 L = make_float2(0.f, 0.f);
+  if (has) {
+    const float4 A = __ldg(d.dm_a + t), B = __ldg(d.dm_b + t);
+    tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+    tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+    tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
+    lid = __ldg(d.lid + t);
+    if (kRes) L = d.lam[t];
+  }
+  const float4* P = d.p[a.cur];
+  for (int j = threadIdx.x; j < nv; j += kP) {
+    const int g = __ldg(d.pverts + vb + j);
+    const float3 x = post_position(ldg4(P + g), ldg4(d.dx + g));
+    sp[j] = make_float4(x.x, x.y, x.z, 0.f);
+  }
+  __syncthreads();
+  float sr = 0.f, sh = 0.f, sd = 0.f;
+  if (has) {
+    tt.p[0] = sp[lid & 0xffu];
+    tt.p[1] = sp[(lid >> 8) & 0xffu];
+    tt.p[2] = sp[(lid >> 16) & 0xffu];
+    tt.p[3] = sp[lid >> 24];
+    float F[9];
+    deformation_gradient(tt, F);
+    float C_D, C_H;
+    invariants<kPrecise>(F, C_D, C_H);
+    if (kRes) {
+      const float six_det = 6.f * det9(tt.dm);
+      const float aD = six_det * __ldg(d.inv_mu + b) * a.inv_dt2;
+      const float aH = six_det * __ldg(d.inv_la + b) * a.inv_dt2;
+      const float rD = C_D + aD * L.x, rH = C_H + aH * L.y;
+      sr = sqrtf(rD * rD + rH * rH);
+    }
+    if (kMon) {
+      sh = fabsf(C_H);
+      sd = fabsf(C_D);
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const double r0 = warp_sum((double)sr), r1 = warp_sum((double)sh), r2 = warp_sum((double)sd);
+  if (lane == 0) {
+    red[0][warp] = r0;
+    red[1][warp] = r1;
+    red[2][warp] = r2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+    for (int k = 0; k < kP / 32; ++k) {
+      b0 += red[0][k];
+      b1 += red[1][k];
+      b2 += red[2][k];
+    }
+    BodyState* bs = d.bs + b;
+    if (kRes) atomicAdd(&bs->acc[0], b0);
+    if (kMon) {
+      atomicAdd(&bs->acc[1], b1);
+      atomicAdd(&bs->acc[2], b2);
+    }
+    __threadfence();
+    const unsigned int tk = atomicAdd(&bs->ticket, 1u);
+    last = (tk == (unsigned)__ldg(d.body_patches + b) - 1u);
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  volatile BodyState* st = d.bs + b;
+  const double S = st->acc[0], Hs = st->acc[1], Ds = st->acc[2];
+  st->acc[0] = 0.0;
+  st->acc[1] = 0.0;
+  st->acc[2] = 0.0;
+  st->ticket = 0u;
+  const int ntb = __ldg(d.body_tets + b);
+  const double n = (double)ntb;
+  double r_hat = 0.0, omega = 1.0;
+  if (kRes) {
+    r_hat = ntb > 0 ? S / n : 0.0;
+    if (!isfinite(S)) d.flags->nonfinite = 1;
+    if (st->has_prev && st->prev_r_hat > 1e-12) {
+      double rho_inst = r_hat / (st->prev_r_hat + 1e-12);
+      rho_inst = fmax(a.rho_min, fmin(a.rho_max, rho_inst));
+      st->rho_hat = (1.0 - a.rho_beta) * st->rho_hat + a.rho_beta * rho_inst;
+    }
+    st->prev_r_hat = r_hat;
+    st->has_prev = 1;
+    const double rho2 = st->rho_hat * st->rho_hat;
+    if (a.it < a.warmup) omega = 1.0;
+    else if (a.it == a.warmup) omega = 2.0 / (2.0 - rho2);
+    else omega = 4.0 / (4.0 - rho2 * st->omega);
+    st->omega = omega;
+  }
+  if (a.rec >= 0) {
+    double* h = d.hist + 4 * ((size_t)b * d.max_records + a.rec);
+    h[0] = r_hat;
+    h[1] = omega;
+    h[2] = kMon && ntb > 0 ? Hs / n : 0.0;
+    h[3] = kMon && ntb > 0 ? Ds / n : 0.0;
+  }
+}
+
+// post_solve + Chebyshev mix with the omega of the vertex block's body.
+template <bool kCheb, bool kFirstIt>
+__global__ void __launch_bounds__(256) kb_update(BDev d, int cur, float gamma) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.V) return;
+  const float4 pc = d.p[cur][i];
+  const float4 D = d.dx[i];
+  d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float3 xp = post_position(pc, D);
+  if (kCheb) {
+    const float om = (float)d.bs[__ldg(d.vblock_body + blockIdx.x)].omega;
+    const float4 yp = kFirstIt ? pc : d.p[cur ^ 1][i];
+    const float nx = gamma * (xp.x - pc.x) + pc.x;
+    const float ny = gamma * (xp.y - pc.y) + pc.y;
+    const float nz = gamma * (xp.z - pc.z) + pc.z;
+    d.p[cur ^ 1][i] = make_float4(yp.x + om * (nx - yp.x), yp.y + om * (ny - yp.y), yp.z + om * (nz - yp.z), pc.w);
+  } else {
+    d.p[cur][i] = make_float4(xp.x, xp.y, xp.z, pc.w);
+  }
+}
+
+__global__ void kb_export(BDev d, const float4* f, float* __restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.V) return;
+  const int j = d.perm[i];
+  if (j < 0) return;  // padding vertex
+  const float4 o = f[i];
+  dst[3 * (size_t)j] = o.x;
+  dst[3 * (size_t)j + 1] = o.y;
+  dst[3 * (size_t)j + 2] = o.z;
+}
+
+__global__ void kb_import(BDev d, float4* f, const float* __restrict__ src) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.V) return;
+  const int j = d.perm[i];
+  if (j < 0) return;
+  float4 o = f[i];
+  o.x = src[3 * (size_t)j];
+  o.y = src[3 * (size_t)j + 1];
+  o.z = src[3 * (size_t)j + 2];
+  f[i] = o;
+}
+
+// One-time validation of every index the kernels follow.
+__global__ void kb_validate(BDev d, int n_out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < d.n_patches) {
+    const int a = d.voff[t], e = d.voff[t + 1], b = d.patch_body[t], nt = d.patch_ntets[t];
+    if (a < 0 || e < a || e > d.n_pverts || e - a > 256 || b < 0 || b >= d.n_bodies || nt < 0 || nt > kP)
+      d.flags->bad_mesh = 1;
+    for (int q = 0; q < nt && !d.flags->bad_mesh; ++q) {
+      const uint32_t l = d.lid[t * kP + q];
+      if ((int)(l & 0xffu) >= e - a || (int)((l >> 8) & 0xffu) >= e - a || (int)((l >> 16) & 0xffu) >= e - a ||
+          (int)(l >> 24) >= e - a)
+        d.flags->bad_mesh = 1;
+    }
+    for (int k = a; k < e && !d.flags->bad_mesh; ++k)
+      if ((unsigned)d.pverts[k] >= (unsigned)d.V) d.flags->bad_mesh = 1;
+  }
+  if (t < d.V / 256) {
+    const int b = d.vblock_body[t];
+    if (b < 0 || b >= d.n_bodies) d.flags->bad_mesh = 1;
+  }
+  if (d.perm && t < d.V) {
+    if (d.perm[t] >= n_out || d.perm[t] < -1) d.flags->bad_mesh = 1;
+  }
+}
+
+}  // namespace batch
+}  // namespace xpbd
+
+using namespace xpbd;
+using namespace xpbd::batch;
+
+namespace {
+
+thread_local std::string g_err;
+
+int bfail(int st, const std::string& m) {
+  g_err = m;
+  return st;
+}
+
+#define B_CUDA(call)                                                                               \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return bfail(XPBD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct Batch {
+  xpbd_params prm{};
+  BDev d{};
+  int cur = 0;
+  int n_out = 0;
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double key_frame_dt = -1, key_dt = -1;
+  int key_sub = -1;
+  bool profiling = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[XPBD_K_COUNT];
+  double prof_ms[XPBD_K_COUNT] = {0, 0, 0, 0, 0, 0};
+  long long prof_n[XPBD_K_COUNT] = {0, 0, 0, 0, 0, 0};
+};
+
+inline cudaStream_t BS(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+inline int nblk(int n) { return (n + 255) / 256; }
+
+struct BProf {
+  Batch* s;
+  int cls;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr;
+  cudaEvent_t take() {
+    if (!s->pool.empty()) {
+      cudaEvent_t e = s->pool.back();
+      s->pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    return cudaEventCreate(&e) == cudaSuccess ? e : nullptr;
+  }
+  BProf(Batch* s_, int c, cudaStream_t st_) : s(s_), cls(c), st(st_) {
+    if (s->profiling && (a = take())) cudaEventRecord(a, st);
+  }
+  ~BProf() {
+    if (!a) return;
+    cudaEvent_t b = take();
+    if (!b) return;
+    cudaEventRecord(b, st);
+    s->pending[cls].push_back({a, b});
+  }
+};
+
+template <bool kBlock, bool kFirst>
+void project_b(Batch* s, float inv_dt2, cudaStream_t st) {
+  const xpbd_params& p = s->prm;
+  if (p.precise_hydro)
+    kb_project<kBlock, kFirst, true><<<s->d.n_patches, kP, 0, st>>>(s->d, s->cur, inv_dt2, p.hydrostatic_relaxation,
+                                                                     p.deviatoric_relaxation);
+  else
+    kb_project<kBlock, kFirst, false><<<s->d.n_patches, kP, 0, st>>>(s->d, s->cur, inv_dt2, p.hydrostatic_relaxation,
+                                                                      p.deviatoric_relaxation);
+}
+
+template <bool kRes, bool kMon>
+void residual_b(Batch* s, const BSweep& a, cudaStream_t st) {
+  if (s->prm.precise_hydro) kb_residual<kRes, kMon, true><<<s->d.n_patches, kP, 0, st>>>(s->d, a);
+  else kb_residual<kRes, kMon, false><<<s->d.n_patches, kP, 0, st>>>(s->d, a);
+}
+
+void iteration_b(Batch* s, int it, float dt, int rec, cudaStream_t st) {
+  const xpbd_params& p = s->prm;
+  const float inv_dt2 = (float)(1.0 / ((double)dt * (double)dt));
+  {
+    BProf pr(s, XPBD_K_PROJECT, st);
+    const bool blk = p.block_mode != 0;
+    if (it == 0) blk ? project_b<true, true>(s, inv_dt2, st) : project_b<false, true>(s, inv_dt2, st);
+    else blk ? project_b<true, false>(s, inv_dt2, st) : project_b<false, false>(s, inv_dt2, st);
+  }
+  const bool cheb = p.cheb_enable != 0, mon = p.monitor != 0;
+  if (cheb || mon) {
+    BSweep a;
+    a.cur = s->cur;
+    a.inv_dt2 = inv_dt2;
+    a.it = it;
+    a.warmup = p.cheb_warmup;
+    a.rec = rec;
+    a.rho_min = p.rho_min;
+    a.rho_max = p.rho_max;
+    a.rho_beta = p.rho_beta;
+    BProf pr(s, XPBD_K_RESIDUAL, st);
+    if (cheb && mon) residual_b<true, true>(s, a, st);
+    else if (cheb) residual_b<true, false>(s, a, st);
+    else residual_b<false, true>(s, a, st);
+  }
+  BProf pr(s, XPBD_K_UPDATE, st);
+  const int g = nblk(s->d.V);
+  if (cheb) {
+    if (it == 0) kb_update<true, true><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma);
+    else kb_update<true, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma);
+    s->cur ^= 1;
+  } else {
+    kb_update<false, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma);
+  }
+}
+
+int substep_b(Batch* s, float dt, int rec_base, cudaStream_t st) {
+  const int K = s->prm.constraints_iter;
+  if (rec_base >= 0 && rec_base + K > s->d.max_records) return bfail(XPBD_ERR_HISTORY_FULL, "history full");
+  s->cur = 0;
+  {
+    BProf pr(s, XPBD_K_BEGIN, st);
+    kb_begin<<<nblk(s->d.V), 256, 0, st>>>(s->d, dt, s->prm.gravity[0], s->prm.gravity[1], s->prm.gravity[2]);
+  }
+  for (int it = 0; it < K; ++it) iteration_b(s, it, dt, rec_base >= 0 ? rec_base + it : -1, st);
+  BProf pr(s, XPBD_K_END, st);
+  kb_end<<<nblk(s->d.V), 256, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
+  return XPBD_OK;
+}
+
+int frame_b(Batch* s, double frame_dt, double dt, int substeps, cudaStream_t st) {
+  double left = frame_dt;
+  int rec = 0;
+  while (left > 0.0) {
+    const double dt0 = dt < left ? dt : left;
+    left -= dt0;
+    const float sub = (float)(dt0 / substeps);
+    for (int k = 0; k < substeps; ++k) {
+      const int base = rec + s->prm.constraints_iter <= s->d.max_records ? rec : -1;
+      int r = substep_b(s, sub, base, st);
+      if (r) return r;
+      rec += s->prm.constraints_iter;
+    }
+  }
+  return XPBD_OK;
+}
+
+void drop_b(Batch* s) {
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  s->exec = nullptr;
+  s->key_frame_dt = s->key_dt = -1;
+  s->key_sub = -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* xpbd_batch_last_error(void) { return g_err.c_str(); }
+
+int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const xpbd_sdf* sdfs, int32_t n_sdf,
+                      int32_t max_records, void** out_handle) {
+  g_err.clear();
+  if (!out_handle || !body || !params) return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out_handle = nullptr;
+  if (n_sdf <= 0 || !sdfs) return bfail(XPBD_ERR_NO_SDF, "At least one SDF object must be provided.");
+  for (int k = 0; k < n_sdf; ++k)
+    if (sdfs[k].kind < XPBD_SDF_PLANE || sdfs[k].kind > XPBD_SDF_CUBE)
+      return bfail(XPBD_ERR_INVALID_ARGUMENT, "unknown SDF kind");
+  if (body->n_bodies <= 0 || body->n_verts <= 0 || body->n_tets <= 0 || body->n_patches <= 0)
+    return bfail(XPBD_ERR_BAD_MESH, "empty batch");
+  if (body->n_verts % 256 || body->n_tets != body->n_patches * kP)
+    return bfail(XPBD_ERR_BAD_MESH, "n_verts must be a multiple of 256 and n_tets = 256 n_patches");
+  if (!body->x || !body->v || !body->p0 || !body->p1 || !body->dx || !body->dm_a || !body->dm_b || !body->dm_c ||
+      !body->lam || !body->tet_lid || !body->patch_voff || !body->patch_verts || !body->patch_body ||
+      !body->patch_ntets || !body->vblock_body || !body->body_inv_mu || !body->body_inv_lambda ||
+      !body->body_n_patches || !body->body_n_tets || !body->vert_perm)
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL batch buffer");
+  if (max_records < 0) return bfail(XPBD_ERR_INVALID_ARGUMENT, "max_records < 0");
+  Batch* s = new (std::nothrow) Batch();
+  if (!s) return bfail(XPBD_ERR_INVALID_ARGUMENT, "out of host memory");
+  s->prm = *params;
+  s->n_out = body->n_out_verts;
+  BDev& d = s->d;
+  d.V = body->n_verts;
+  d.T = body->n_tets;
+  d.n_patches = body->n_patches;
+  d.n_bodies = body->n_bodies;
+  d.n_sdf = n_sdf;
+  d.n_pverts = body->n_patch_verts;
+  d.x = reinterpret_cast<float4*>(body->x);
+  d.v = reinterpret_cast<float4*>(body->v);
+  d.p[0] = reinterpret_cast<float4*>(body->p0);
+  d.p[1] = reinterpret_cast<float4*>(body->p1);
+  d.dx = reinterpret_cast<float4*>(body->dx);
+  d.dm_a = reinterpret_cast<const float4*>(body->dm_a);
+  d.dm_b = reinterpret_cast<const float4*>(body->dm_b);
+  d.dm_c = body->dm_c;
+  d.lam = reinterpret_cast<float2*>(body->lam);
+  d.lid = body->tet_lid;
+  d.voff = body->patch_voff;
+  d.pverts = body->patch_verts;
+  d.patch_body = body->patch_body;
+  d.patch_ntets = body->patch_ntets;
+  d.vblock_body = body->vblock_body;
+  d.inv_mu = body->body_inv_mu;
+  d.inv_la = body->body_inv_lambda;
+  d.body_patches = body->body_n_patches;
+  d.body_tets = body->body_n_tets;
+  d.perm = body->vert_perm;
+  d.max_records = max_records > 0 ? max_records : 1;
+  auto cleanup = [&](int st) {
+    if (d.sdfs) cudaFree(const_cast<xpbd_sdf*>(d.sdfs));
+    if (d.bs) cudaFree(d.bs);
+    if (d.flags) cudaFree(d.flags);
+    if (d.hist) cudaFree(d.hist);
+    if (s->cap) cudaStreamDestroy(s->cap);
+    delete s;
+    return st;
+  };
+  xpbd_sdf* ds = nullptr;
+  cudaError_t e = cudaMalloc(&ds, sizeof(xpbd_sdf) * n_sdf);
+  d.sdfs = ds;
+  if (e == cudaSuccess) e = cudaMemcpy(ds, sdfs, sizeof(xpbd_sdf) * n_sdf, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&d.bs, sizeof(BodyState) * d.n_bodies);
+  if (e == cudaSuccess) e = cudaMalloc(&d.flags, sizeof(Flags));
+  if (e == cudaSuccess) e = cudaMalloc(&d.hist, sizeof(double) * 4 * (size_t)d.max_records * d.n_bodies);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cleanup(bfail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
+  std::vector<BodyState> hb(d.n_bodies);
+  for (auto& b : hb) {
+    std::memset(&b, 0, sizeof(b));
+    b.rho_hat = 0.999;  // neohookean_solver.py:65
+    b.omega = 1.0;
+  }
+  Flags hf{0, 0};
+  e = cudaMemcpy(d.bs, hb.data(), sizeof(BodyState) * d.n_bodies, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d.flags, &hf, sizeof(hf), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(d.hist, 0, sizeof(double) * 4 * (size_t)d.max_records * d.n_bodies);
+  if (e != cudaSuccess) return cleanup(bfail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
+  const int nval = d.V > d.n_patches ? d.V : d.n_patches;
+  kb_validate<<<nblk(nval), 256>>>(d, s->n_out);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(&hf, d.flags, sizeof(hf), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cleanup(bfail(XPBD_ERR_CUDA, std::string("validate: ") + cudaGetErrorString(e)));
+  if (hf.bad_mesh) return cleanup(bfail(XPBD_ERR_BAD_MESH, "batch index out of range"));
+  *out_handle = s;
+  return XPBD_OK;
+}
+
+int xpbd_batch_destroy(void* h) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s) return XPBD_OK;
+  drop_b(s);
+  for (auto& v : s->pending)
+    for (auto& pr : v) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+  for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
+  cudaFree(const_cast<xpbd_sdf*>(s->d.sdfs));
+  cudaFree(s->d.bs);
+  cudaFree(s->d.flags);
+  cudaFree(s->d.hist);
+  if (s->cap) cudaStreamDestroy(s->cap);
+  delete s;
+  return XPBD_OK;
+}
+
+int xpbd_batch_substep(void* h, float dt, int32_t record_base, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s) return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle");
+  int r = substep_b(s, dt, record_base, BS(stream));
+  if (r) return r;
+  B_CUDA(cudaGetLastError());
+  return XPBD_OK;
+}
+
+int xpbd_batch_solve(void* h, double frame_dt, double dt, int32_t substeps, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s) return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle");
+  if (substeps <= 0 || !(dt > 0.0) || !(frame_dt >= 0.0) || frame_dt / dt > 1e6)
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "need substeps > 0, dt > 0, frame_dt >= 0");
+  if (!s->prm.use_graph || s->profiling) {
+    int r = frame_b(s, frame_dt, dt, substeps, BS(stream));
+    if (r) return r;
+    B_CUDA(cudaGetLastError());
+    return XPBD_OK;
+  }
+  if (!(s->exec && s->key_frame_dt == frame_dt && s->key_dt == dt && s->key_sub == substeps)) {
+    drop_b(s);
+    B_CUDA(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
+    int r = frame_b(s, frame_dt, dt, substeps, s->cap);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s->cap, &g);
+    if (r) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    if (e != cudaSuccess) return bfail(XPBD_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      s->exec = nullptr;
+      return bfail(XPBD_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+    }
+    s->key_frame_dt = frame_dt;
+    s->key_dt = dt;
+    s->key_sub = substeps;
+  }
+  B_CUDA(cudaGraphLaunch(s->exec, BS(stream)));
+  return XPBD_OK;
+}
+
+int xpbd_batch_read_history(void* h, double* out, int32_t n, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !out || n < 0 || n > s->d.max_records) return bfail(XPBD_ERR_INVALID_ARGUMENT, "bad history read");
+  B_CUDA(cudaStreamSynchronize(BS(stream)));
+  for (int b = 0; b < s->d.n_bodies; ++b)
+    B_CUDA(cudaMemcpy(out + 4 * (size_t)b * n, s->d.hist + 4 * (size_t)b * s->d.max_records,
+                      sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToHost));
+  return XPBD_OK;
+}
+
+int xpbd_batch_get_rho_hat(void* h, double* out, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !out) return bfail(XPBD_ERR_INVALID_ARGUMENT, "bad argument");
+  B_CUDA(cudaStreamSynchronize(BS(stream)));
+  std::vector<BodyState> hb(s->d.n_bodies);
+  B_CUDA(cudaMemcpy(hb.data(), s->d.bs, sizeof(BodyState) * s->d.n_bodies, cudaMemcpyDeviceToHost));
+  for (int b = 0; b < s->d.n_bodies; ++b) out[b] = hb[b].rho_hat;
+  return XPBD_OK;
+}
+
+int xpbd_batch_check_status(void* h, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s) return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle");
+  Flags f{0, 0};
+  B_CUDA(cudaStreamSynchronize(BS(stream)));
+  B_CUDA(cudaMemcpy(&f, s->d.flags, sizeof(f), cudaMemcpyDeviceToHost));
+  return f.nonfinite ? bfail(XPBD_ERR_NONFINITE, "non-finite residual") : XPBD_OK;
+}
+
+int xpbd_batch_export_vec3(void* h, int32_t field, float* dst, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !dst) return bfail(XPBD_ERR_INVALID_ARGUMENT, "bad argument");
+  const float4* f = field == XPBD_FIELD_X ? s->d.x : field == XPBD_FIELD_V ? s->d.v
+                    : field == XPBD_FIELD_PRED_X ? s->d.p[s->cur] : nullptr;
+  if (!f) return bfail(XPBD_ERR_INVALID_ARGUMENT, "unknown field");
+  kb_export<<<nblk(s->d.V), 256, 0, BS(stream)>>>(s->d, f, dst);
+  B_CUDA(cudaGetLastError());
+  return XPBD_OK;
+}
+
+int xpbd_batch_import_vec3(void* h, int32_t field, const float* src, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !src) return bfail(XPBD_ERR_INVALID_ARGUMENT, "bad argument");
+  float4* f = field == XPBD_FIELD_X ? s->d.x : field == XPBD_FIELD_V ? s->d.v
+              : field == XPBD_FIELD_PRED_X ? s->d.p[s->cur] : nullptr;
+  if (!f) return bfail(XPBD_ERR_INVALID_ARGUMENT, "unknown field");
+  kb_import<<<nblk(s->d.V), 256, 0, BS(stream)>>>(s->d, f, src);
+  B_CUDA(cudaGetLastError());
+  return XPBD_OK;
+}
+
+int xpbd_batch_set_profiling(void* h, int32_t enable) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s) return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle");
+  s->profiling = enable != 0;
+  return XPBD_OK;
+}
+
+int xpbd_batch_read_profile(void* h, double* ms, int64_t* launches, int32_t n, int32_t reset, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || n < 0 || n > XPBD_K_COUNT) return bfail(XPBD_ERR_INVALID_ARGUMENT, "bad profile read");
+  B_CUDA(cudaStreamSynchronize(BS(stream)));
+  for (int k = 0; k < XPBD_K_COUNT; ++k) {
+    for (auto& pr : s->pending[k]) {
+      float t = 0.f;
+      B_CUDA(cudaEventElapsedTime(&t, pr.first, pr.second));
+      s->prof_ms[k] += t;
+      s->prof_n[k] += 1;
+      s->pool.push_back(pr.first);
+      s->pool.push_back(pr.second);
+    }
+    s->pending[k].clear();
+  }
+  for (int k = 0; k < n; ++k) {
+    if (ms) ms[k] = s->prof_ms[k];
+    if (launches) launches[k] = s->prof_n[k];
+  }
+  if (reset)
+    for (int k = 0; k < XPBD_K_COUNT; ++k) {
+      s->prof_ms[k] = 0.0;
+      s->prof_n[k] = 0;
+    }
+  return XPBD_OK;
+}
+
+}  // extern "C"

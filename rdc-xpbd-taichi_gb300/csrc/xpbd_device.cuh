@@ -114,6 +114,88 @@ __device__ __forceinline__ bool solve2x2_pivot_lu(float A00, float A01, float A1
   return true;
 }
 
+// One tet of solve_neohookean_block (neohookean_solver.py:358-451) when
+// kBlockMode, else of the split pair solve_hydrostatic + solve_deviatoric
+// (:196-254, :144-194), both reading the same predicted positions.  Updates L
+// = (lambda_D, lambda_H) and returns the four corner displacements and the
+// constraint count added to each corner.
+// aD, aH: the time-scaled compliances alpha / dt^2 of the tet (:413-416).
+template <bool kBlockMode, bool kPrecise>
+__device__ __forceinline__ void project_tet(const Tet& tt, float aD, float aH, float relax_h, float relax_d, float2& L,
+                                            float3 dp[4], float& cnt) {
+  const float w[4] = {tt.p[0].w, tt.p[1].w, tt.p[2].w, tt.p[3].w};
+  float F[9];
+  deformation_gradient(tt, F);
+  float C_D, C_H;
+  invariants<kPrecise>(F, C_D, C_H);
+  float gF[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) gF[k] = F[k] * 2.f;
+  float3 gD[4];
+  corner_gradients(gF, tt.dm, gD);
+  float H[9];
+  cofactor(F, H);
+  float3 gH[4];
+  corner_gradients(H, tt.dm, gH);
+
+  if (kBlockMode) {
+    float A11 = w[0] * dot3(gD[0], gD[0]) + w[1] * dot3(gD[1], gD[1]) + w[2] * dot3(gD[2], gD[2]) +
+                w[3] * dot3(gD[3], gD[3]);
+    float A22 = w[0] * dot3(gH[0], gH[0]) + w[1] * dot3(gH[1], gH[1]) + w[2] * dot3(gH[2], gH[2]) +
+                w[3] * dot3(gH[3], gH[3]);
+    const float A12 = w[0] * dot3(gD[0], gH[0]) + w[1] * dot3(gD[1], gH[1]) + w[2] * dot3(gD[2], gH[2]) +
+                      w[3] * dot3(gD[3], gH[3]);
+    A11 += aD;
+    A22 += aH;
+    const float b1 = -(C_D + aD * L.x);
+    const float b2 = -(C_H + aH * L.y);
+    float dD, dH;
+    if (!solve2x2_pivot_lu(A11, A12, A12, A22, b1, b2, dD, dH)) {
+      // :425-432 ill-conditioned fallback: diagonal scalar updates
+      dD = fabsf(A11) > kEps ? b1 / A11 : 0.f;
+      dH = fabsf(A22) > kEps ? b2 / A22 : 0.f;
+    }
+    L.x += dD;
+    L.y += dH;
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      dp[c] = make_float3(w[c] * (gD[c].x * dD + gH[c].x * dH), w[c] * (gD[c].y * dD + gH[c].y * dH),
+                          w[c] * (gD[c].z * dD + gH[c].z * dH));
+    cnt = 1.f;  // :448-451 count every corner
+  } else {
+    // hydrostatic then deviatoric, each gated by w_sum > EPS (:237, :177)
+    float wsH = w[0] * dot3(gH[0], gH[0]);
+    wsH += w[1] * dot3(gH[1], gH[1]);
+    wsH += w[2] * dot3(gH[2], gH[2]);
+    wsH += w[3] * dot3(gH[3], gH[3]);
+    float wsD = w[0] * dot3(gD[0], gD[0]);
+    wsD += w[1] * dot3(gD[1], gD[1]);
+    wsD += w[2] * dot3(gD[2], gD[2]);
+    wsD += w[3] * dot3(gD[3], gD[3]);
+    float dlH = 0.f, dlD = 0.f, cH = 0.f, cD = 0.f;
+    if (wsH > kEps) {
+      const float at = aH;
+      dlH = -(C_H + at * L.y) / (wsH + at);
+      dlH *= relax_h;
+      cH = 1.f;
+    }
+    if (wsD > kEps) {
+      const float at = aD;
+      dlD = -(C_D + at * L.x) / (wsD + at);
+      dlD *= relax_d;
+      cD = 1.f;
+    }
+    L.x += dlD;
+    L.y += dlH;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float sH = dlH * w[c], sD = dlD * w[c];
+      dp[c] = make_float3(sH * gH[c].x + sD * gD[c].x, sH * gH[c].y + sD * gD[c].y, sH * gH[c].z + sD * gD[c].z);
+    }
+    cnt = cH + cD;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // SDFs (sdf.py)
 // ---------------------------------------------------------------------------

@@ -21,7 +21,7 @@ BUILD_DIR = os.path.join(os.path.dirname(PKG_DIR), "_build")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
-SOURCES = ["xpbd_solver.cu", "xpbd_mesh.cpp"]
+SOURCES = ["xpbd_solver.cu", "xpbd_batch.cu", "xpbd_mesh.cpp"]
 
 XPBD_OK = 0
 STATUS_NAMES = {
@@ -72,6 +72,16 @@ class XpbdBody(ctypes.Structure):
                 ("pv_start", _P), ("pv_slots", _P)]
 
 
+class XpbdBatch(ctypes.Structure):
+    _fields_ = [("n_bodies", ctypes.c_int32), ("n_verts", ctypes.c_int32), ("n_tets", ctypes.c_int32),
+                ("n_patches", ctypes.c_int32), ("n_patch_verts", ctypes.c_int32), ("n_out_verts", ctypes.c_int32),
+                ("x", _P), ("v", _P), ("p0", _P), ("p1", _P), ("dx", _P),
+                ("dm_a", _P), ("dm_b", _P), ("dm_c", _P), ("lam", _P), ("tet_lid", _P),
+                ("patch_voff", _P), ("patch_verts", _P), ("patch_body", _P), ("patch_ntets", _P),
+                ("vblock_body", _P), ("body_inv_mu", _P), ("body_inv_lambda", _P),
+                ("body_n_patches", _P), ("body_n_tets", _P), ("vert_perm", _P)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/xpbd_gb300.h
 _SIGNATURES = {
     "xpbd_abi_version": (ctypes.c_int, []),
@@ -101,6 +111,21 @@ _SIGNATURES = {
                                          ctypes.c_int32, ctypes.c_int32, _P]),
     "xpbd_morton_order": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int32, _P, _P]),
     "xpbd_build_vertex_csr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
+    "xpbd_batch_last_error": (ctypes.c_char_p, []),
+    "xpbd_batch_create": (ctypes.c_int, [ctypes.POINTER(XpbdParams), ctypes.POINTER(XpbdBatch),
+                                         ctypes.POINTER(XpbdSdf), ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "xpbd_batch_destroy": (ctypes.c_int, [_P]),
+    "xpbd_batch_substep": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int32, _P]),
+    "xpbd_batch_solve": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_int32, _P]),
+    "xpbd_batch_read_history": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P]),
+    "xpbd_batch_get_rho_hat": (ctypes.c_int, [_P, _P, _P]),
+    "xpbd_batch_check_status": (ctypes.c_int, [_P, _P]),
+    "xpbd_batch_import_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
+    "xpbd_batch_export_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
+    "xpbd_batch_set_profiling": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "xpbd_batch_read_profile": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
+                                               ctypes.c_int32, ctypes.c_int32, _P]),
     "xpbd_build_patch_csr": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "xpbd_build_patches": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P,
                                           ctypes.POINTER(ctypes.c_int32)]),
@@ -185,12 +210,13 @@ class XpbdError(RuntimeError):
         self.status = status
 
 
-def check(status):
+def check(status, batch=False):
     """Raise for a non-zero status with the library's last error message."""
     if status == XPBD_OK:
         return
     lib = load()
-    msg = lib.xpbd_last_error().decode() or lib.xpbd_status_string(status).decode()
+    last = lib.xpbd_batch_last_error() if batch else lib.xpbd_last_error()
+    msg = last.decode() or lib.xpbd_status_string(status).decode()
     if status == 4:  # XPBD_ERR_NO_SDF mirrors xpbd_base.py:66-67
         raise ValueError(msg)
     raise XpbdError(status, msg)
