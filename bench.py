@@ -68,6 +68,150 @@ def workload(name, seed=0):
     raise ValueError("unknown workload %r" % name)
 
 
+def workload_c3(seed=0, n_bodies=256, h=0.03):
+    """256 Kuhn bodies with per-axis cell counts U{4..32}, E log-U[1e4, 1e7], nu U[0.30, 0.495],
+    rho U[500, 2000], random rotation, non-overlapping placement (rejection sampling on bounding
+    spheres) in a 16 x 4 x 16 m arena above the plane y = 0 and 32 random spheres."""
+    from xpbd_gpu.batched import Body
+    from xpbd_gpu.mesh import kuhn_grid, random_rotation
+    rng = np.random.default_rng(seed)
+    dims = rng.integers(4, 33, size=(n_bodies, 3))
+    E = np.exp(rng.uniform(np.log(1e4), np.log(1e7), n_bodies))
+    nu = rng.uniform(0.30, 0.495, n_bodies)
+    rho = rng.uniform(500.0, 2000.0, n_bodies)
+    radius = 0.5 * h * np.linalg.norm(dims, axis=1)
+    order = np.argsort(-radius)
+    centers = np.zeros((n_bodies, 3))
+    placed = []
+    for k in order:
+        r = radius[k]
+        for _ in range(20000):
+            c = np.array([rng.uniform(r, 16.0 - r), rng.uniform(r + 0.9, 4.0 - r), rng.uniform(r, 16.0 - r)])
+            if all(np.linalg.norm(c - centers[j]) > r + radius[j] for j in placed):
+                break
+        else:
+            raise RuntimeError("could not place body %d" % k)
+        centers[k] = c
+        placed.append(k)
+    bodies = []
+    for k in range(n_bodies):
+        nx, ny, nz = (int(v) for v in dims[k])
+        mesh = kuhn_grid(nx, ny, nz, h, origin=(-0.5 * nx * h, -0.5 * ny * h, -0.5 * nz * h), jitter=0.1,
+                         seed=seed * 1000 + k)
+        bodies.append(Body(mesh, young_modulus=float(E[k]), poisson_ratio=float(nu[k]), density=float(rho[k]),
+                           rotation=random_rotation(rng), offset=tuple(centers[k])))
+    sdfs = [("plane", dict(point=[0.0, 0.0, 0.0], dir=[0.0, 1.0, 0.0], fixed=True))]
+    for _ in range(32):
+        sdfs.append(("sphere", dict(center=[float(rng.uniform(0, 16)), float(rng.uniform(-0.6, 0.0)),
+                                            float(rng.uniform(0, 16))], radius=float(rng.uniform(0.3, 0.8)),
+                                    fixed=True)))
+    kw = dict(frame_dt=1.0 / 60, dt=1.0 / 60, substeps_num=5, constraints_iter=30, cheb_enable=True,
+              cheb_warmup=5, cheb_gamma=0.6666, block_neohookean_enable=True)
+    desc = ("256 uneven Kuhn bodies (cells U{4..32}^3, %d tets, %d verts), E log-U[1e4,1e7], nu U[0.30,0.495], "
+            "rho U[500,2000], plane + 32 spheres, 5 substeps x 30 it" % (
+                sum(6 * int(np.prod(d)) for d in dims), sum(int(np.prod(d + 1)) for d in dims)))
+    return bodies, sdfs, kw, desc
+
+
+def relative_residuals(hist, substeps, iters, floor=1e-5):
+    """Per body and substep r_hat_K / r_hat_0 from a (bodies, rows, 4) history; NaN where
+    r_hat_0 is below `floor` (a free-falling body, residual at FP32 round-off)."""
+    r = hist[:, :substeps * iters, 0].reshape(hist.shape[0], substeps, iters)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel = r[:, :, -1] / r[:, :, 0]
+    rel[r[:, :, 0] <= floor] = np.nan
+    return rel
+
+
+def run_c3(args):
+    """Batched form vs the plain one-body-per-launch form on the 256-body batch."""
+    import torch
+    from xpbd_gpu.batched import XPBDBatchedSolver
+    from xpbd_gpu.mesh import TetMesh
+    from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
+    torch.cuda.set_device(0)
+    bodies, specs, kw, desc = workload_c3()
+    units = sum(b.rest_pose.n_tets for b in bodies) * kw["substeps_num"] * kw["constraints_iter"]
+    batch = XPBDBatchedSolver(bodies, product_sdfs(specs), **kw)
+    plain = []
+    for b in bodies:
+        mesh = TetMesh(b.rest_pose.points @ b.rotation.T, b.rest_pose.tets)
+        plain.append(XPBDNeoHookeanSolver(mesh, product_sdfs(specs), young_modulus=b.young_modulus,
+                                          poisson_ratio=b.poisson_ratio, offset=b.offset, density=b.density,
+                                          scatter="patch", **kw))
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def timed(step):
+        for _ in range(max(args.warmup, 3)):
+            step()
+        torch.cuda.synchronize()
+        total = 0.0
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            for _ in range(args.steps):
+                flush.fill_(1.0)
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                step()
+                b.record(stream)
+                torch.cuda.synchronize()
+                total += a.elapsed_time(b)
+        return total / args.steps, clk.summary()
+
+    def plain_step():
+        for s in plain:
+            s.solve()
+
+    ms_batch, clk_b = timed(batch.solve)
+    ms_plain, clk_p = timed(plain_step)
+    batch.check_status()
+    S, K = kw["substeps_num"], kw["constraints_iter"]
+    rel_b = relative_residuals(batch.read_history(), S, K)
+    rel_p = np.stack([relative_residuals(s.read_history()[None], S, K)[0] for s in plain])
+    batch.set_profiling(True)
+    batch.read_profile(reset=True)
+    flush.fill_(1.0)
+    batch.solve()
+    prof = batch.read_profile(reset=True)
+    batch.set_profiling(False)
+    T = batch.n_tets
+    V = batch.n_verts
+    proj_ms = prof["project"]["ms"] / max(1, prof["project"]["launches"])
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak = float(json.load(open(peaks_path))["hbm_gbs"]) if os.path.exists(peaks_path) else 6800.0
+    iter_bytes = 136.0 * T + 128.0 * V
+    line = {
+        "metric": METRIC, "value": units / (ms_batch * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": desc, "step": "one frame of all 256 bodies (%d tet-iterations)" % units,
+                   "form": "batched (one launch per phase over all bodies, CUDA graph per frame)",
+                   "l2": "flushed between steps"},
+        "frames_per_s": 1e3 / ms_batch,
+        "plain": {"form": "one body per launch sequence (256 single-body solvers, one CUDA graph each)",
+                  "value": units / (ms_plain * 1e-3), "ms_per_step": ms_plain, "clocks": clk_p},
+        "batched_over_plain": ms_plain / ms_batch,
+        "equal_residual": {"relative_residual_rK_over_r0_median": [float(np.nanmedian(rel_b)),
+                                                                    float(np.nanmedian(rel_p))],
+                           "max_abs_difference_batched_vs_plain": float(np.nanmax(np.abs(rel_b - rel_p))),
+                           "fraction_substeps_at_or_below_1e-3": [float(np.nanmean(rel_b <= 1e-3)),
+                                                                  float(np.nanmean(rel_p <= 1e-3))],
+                           "substeps_compared": int(np.sum(~np.isnan(rel_b))),
+                           "note": "substeps whose initial r_hat is below 1e-5 (bodies in free fall) excluded"},
+        "roofline": {"bound": "hbm", "kernel": "kb_project (batched tile projection)",
+                     "achieved": (72.0 * T + 32.0 * V) / (proj_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": (72.0 * T + 32.0 * V) / (proj_ms * 1e-3) / 1e9 / peak, "traffic": None,
+                     "ms_per_launch": proj_ms},
+        "iteration_roofline": {"achieved_GBps": iter_bytes * S * K / (ms_batch * 1e-3) / 1e9,
+                               "frac": iter_bytes * S * K / (ms_batch * 1e-3) / 1e9 / peak},
+        "kernel_profile": {k: {"ms_per_launch": v["ms"] / max(1, v["launches"]), "launches": v["launches"]}
+                           for k, v in prof.items() if v["launches"]},
+        "clocks": clk_b,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def product_sdfs(specs):
     from xpbd_gpu.sdf import CubeSdf, PlaneSdf, SphereSdf
     out = []
@@ -349,7 +493,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3"])
     ap.add_argument("--scatter", default="patch", choices=["atomic", "gather", "patch"])
     ap.add_argument("--sweep-order", type=int, default=1, choices=[0, 1])
     ap.add_argument("--patch-pipeline", type=int, default=0, choices=[0, 1])
@@ -364,6 +508,8 @@ def main():
     args = ap.parse_args()
     if args.mode == "profile":
         run_profile(args)
+    elif args.workload == "c3" and args.impl != "reference":
+        run_c3(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -179,90 +179,40 @@ struct BSweep {
   double rho_min, rho_max, rho_beta;
 };
 
-// Residual (neohookean_solver.py:298-329) and monitoring sums (:256-296) of one
-// patch, added to its body's FP64 accumulators; the body's last patch applies
-// the rho_hat / omega recurrence and writes the body's history row.
-template <bool kRes, bool kMon, bool kPrecise>
-__global__ void __launch_bounds__(kP) kb_residual(BDev d, BSweep a) {
-  __shared__ float4 sp[256];
-  __shared__ double red[3][kP / 32];
-  __shared__ bool last;
-  const int p = blockIdx.x;
-  const int b = __ldg(d.patch_body + p);
-  const int vb = __ldg(d.voff + p);
-  const int nv = __ldg(d.voff + p + 1) - vb;
-  const int nt = __ldg(d.patch_ntets + p);
-  const int t = p * kP + threadIdx.x;
-  const bool has = threadIdx.x < nt;
-  Tet tt;
-  uint32_t lid = 0;
-  float2 L = make_float2(0.f, 0.f);
-  if (has) {
-    const float4 A = __ldg(d.dm_a + t), B = __ldg(d.dm_b + t);
-    tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
-    tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
-    tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
-    lid = __ldg(d.lid + t);
-    if (kRes) L = d.lam[t];
-  }
-  const float4* P = d.p[a.cur];
-  for (int j = threadIdx.x; j < nv; j += kP) {
-    const int g = __ldg(d.pverts + vb + j);
-    const float3 x = post_position(ldg4(P + g), ldg4(d.dx + g));
-    sp[j] = make_float4(x.x, x.y, x.z, 0.f);
-  }
-  __syncthreads();
-  float sr = 0.f, sh = 0.f, sd = 0.f;
-  if (has) {
-    tt.p[0] = sp[lid & 0xffu];
-    tt.p[1] = sp[(lid >> 8) & 0xffu];
-    tt.p[2] = sp[(lid >> 16) & 0xffu];
-    tt.p[3] = sp[lid >> 24];
-    float F[9];
-    deformation_gradient(tt, F);
-    float C_D, C_H;
-    invariants<kPrecise>(F, C_D, C_H);
-    if (kRes) {
-      const float six_det = 6.f * det9(tt.dm);
-      const float aD = six_det * __ldg(d.inv_mu + b) * a.inv_dt2;
-      const float aH = six_det * __ldg(d.inv_la + b) * a.inv_dt2;
-      const float rD = C_D + aD * L.x, rH = C_H + aH * L.y;
-      sr = sqrtf(rD * rD + rH * rH);
-    }
-    if (kMon) {
-      sh = fabsf(C_H);
-      sd = fabsf(C_D);
-    }
-  }
+// Add a CTA's partial sums over `npatch` patches of body b to the body's FP64
+// accumulators; the CTA that completes the body's patch count applies the
+// rho_hat / omega recurrence (neohookean_solver.py:495-504, :537-546) and
+// writes the body's history row.  All threads of the CTA call it.
+template <bool kRes, bool kMon>
+__device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int b, int npatch, float sr, float sh,
+                                           float sd, double (*red)[kP / 32]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const double r0 = warp_sum((double)sr), r1 = warp_sum((double)sh), r2 = warp_sum((double)sd);
+  __syncthreads();  // red[] of the previous flush has been consumed
   if (lane == 0) {
     red[0][warp] = r0;
     red[1][warp] = r1;
     red[2][warp] = r2;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
-    for (int k = 0; k < kP / 32; ++k) {
-      b0 += red[0][k];
-      b1 += red[1][k];
-      b2 += red[2][k];
-    }
-    BodyState* bs = d.bs + b;
-    if (kRes) atomicAdd(&bs->acc[0], b0);
-    if (kMon) {
-      atomicAdd(&bs->acc[1], b1);
-      atomicAdd(&bs->acc[2], b2);
-    }
-    __threadfence();
-    const unsigned int tk = atomicAdd(&bs->ticket, 1u);
-    last = (tk == (unsigned)__ldg(d.body_patches + b) - 1u);
+  if (threadIdx.x != 0) return;
+  double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+  for (int k = 0; k < kP / 32; ++k) {
+    b0 += red[0][k];
+    b1 += red[1][k];
+    b2 += red[2][k];
   }
-  __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  BodyState* bs = d.bs + b;
+  if (kRes) atomicAdd(&bs->acc[0], b0);
+  if (kMon) {
+    atomicAdd(&bs->acc[1], b1);
+    atomicAdd(&bs->acc[2], b2);
+  }
   __threadfence();
-  volatile BodyState* st = d.bs + b;
+  const unsigned int tk = atomicAdd(&bs->ticket, (unsigned)npatch);
+  if (tk + (unsigned)npatch != (unsigned)__ldg(d.body_patches + b)) return;
+  __threadfence();
+  volatile BodyState* st = bs;
   const double S = st->acc[0], Hs = st->acc[1], Ds = st->acc[2];
   st->acc[0] = 0.0;
   st->acc[1] = 0.0;
@@ -293,6 +243,73 @@ __global__ void __launch_bounds__(kP) kb_residual(BDev d, BSweep a) {
     h[1] = omega;
     h[2] = kMon && ntb > 0 ? Hs / n : 0.0;
     h[3] = kMon && ntb > 0 ? Ds / n : 0.0;
+  }
+}
+
+// Residual (neohookean_solver.py:298-329) and monitoring sums (:256-296).
+// Each CTA walks a contiguous run of `chunk` patches (patches are ordered by
+// body) and flushes its partial sums whenever the body changes.
+template <bool kRes, bool kMon, bool kPrecise>
+__global__ void __launch_bounds__(kP) kb_residual(BDev d, BSweep a, int chunk) {
+  __shared__ float4 sp[256];
+  __shared__ double red[3][kP / 32];
+  const int c0 = blockIdx.x * chunk;
+  const int c1 = c0 + chunk < d.n_patches ? c0 + chunk : d.n_patches;
+  const float4* P = d.p[a.cur];
+  float sr = 0.f, sh = 0.f, sd = 0.f;
+  int run = 0;
+  for (int p = c0; p < c1; ++p) {
+    const int b = __ldg(d.patch_body + p);
+    const int vb = __ldg(d.voff + p);
+    const int nv = __ldg(d.voff + p + 1) - vb;
+    const int nt = __ldg(d.patch_ntets + p);
+    const int t = p * kP + threadIdx.x;
+    const bool has = threadIdx.x < nt;
+    Tet tt;
+    uint32_t lid = 0;
+    float2 L = make_float2(0.f, 0.f);
+    if (has) {
+      const float4 A = __ldg(d.dm_a + t), B = __ldg(d.dm_b + t);
+      tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+      tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+      tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
+      lid = __ldg(d.lid + t);
+      if (kRes) L = d.lam[t];
+    }
+    __syncthreads();  // the previous patch's readers are done with sp
+    for (int j = threadIdx.x; j < nv; j += kP) {
+      const int g = __ldg(d.pverts + vb + j);
+      const float3 x = post_position(ldg4(P + g), ldg4(d.dx + g));
+      sp[j] = make_float4(x.x, x.y, x.z, 0.f);
+    }
+    __syncthreads();
+    if (has) {
+      tt.p[0] = sp[lid & 0xffu];
+      tt.p[1] = sp[(lid >> 8) & 0xffu];
+      tt.p[2] = sp[(lid >> 16) & 0xffu];
+      tt.p[3] = sp[lid >> 24];
+      float F[9];
+      deformation_gradient(tt, F);
+      float C_D, C_H;
+      invariants<kPrecise>(F, C_D, C_H);
+      if (kRes) {
+        const float six_det = 6.f * det9(tt.dm);
+        const float aD = six_det * __ldg(d.inv_mu + b) * a.inv_dt2;
+        const float aH = six_det * __ldg(d.inv_la + b) * a.inv_dt2;
+        const float rD = C_D + aD * L.x, rH = C_H + aH * L.y;
+        sr += sqrtf(rD * rD + rH * rH);
+      }
+      if (kMon) {
+        sh += fabsf(C_H);
+        sd += fabsf(C_D);
+      }
+    }
+    ++run;
+    if (p + 1 == c1 || __ldg(d.patch_body + p + 1) != b) {
+      flush_body<kRes, kMon>(d, a, b, run, sr, sh, sd, red);
+      sr = sh = sd = 0.f;
+      run = 0;
+    }
   }
 }
 
@@ -387,6 +404,7 @@ int bfail(int st, const std::string& m) {
   } while (0)
 
 struct Batch {
+  int res_ctas = 1;  // CTAs of the residual sweep (resident CTAs of the GPU)
   xpbd_params prm{};
   BDev d{};
   int cur = 0;
@@ -444,8 +462,10 @@ void project_b(Batch* s, float inv_dt2, cudaStream_t st) {
 
 template <bool kRes, bool kMon>
 void residual_b(Batch* s, const BSweep& a, cudaStream_t st) {
-  if (s->prm.precise_hydro) kb_residual<kRes, kMon, true><<<s->d.n_patches, kP, 0, st>>>(s->d, a);
-  else kb_residual<kRes, kMon, false><<<s->d.n_patches, kP, 0, st>>>(s->d, a);
+  const int chunk = (s->d.n_patches + s->res_ctas - 1) / s->res_ctas;
+  const int grid = (s->d.n_patches + chunk - 1) / chunk;
+  if (s->prm.precise_hydro) kb_residual<kRes, kMon, true><<<grid, kP, 0, st>>>(s->d, a, chunk);
+  else kb_residual<kRes, kMon, false><<<grid, kP, 0, st>>>(s->d, a, chunk);
 }
 
 void iteration_b(Batch* s, int it, float dt, int rec, cudaStream_t st) {
@@ -608,6 +628,15 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
   if (e == cudaSuccess) e = cudaMemcpy(d.flags, &hf, sizeof(hf), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(d.hist, 0, sizeof(double) * 4 * (size_t)d.max_records * d.n_bodies);
   if (e != cudaSuccess) return cleanup(bfail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
+  {
+    int dev = 0, sms = 0, bps = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kb_residual<true, false, true>, kP, 0) != cudaSuccess ||
+        bps < 1)
+      bps = 2;
+    s->res_ctas = sms * bps > 0 ? sms * bps : 1;
+  }
   const int nval = d.V > d.n_patches ? d.V : d.n_patches;
   kb_validate<<<nblk(nval), 256>>>(d, s->n_out);
   e = cudaGetLastError();
