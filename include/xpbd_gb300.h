@@ -217,6 +217,30 @@ int xpbd_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, in
  * synchronises. */
 int xpbd_check_status(void* handle, void* stream);
 
+/* Residual sweep that allocates nothing.  No counterpart in the reference.
+ * For callers that may not allocate device memory -- an engine or plugin host
+ * that owns every device allocation and hands this library only its buffers,
+ * or a frame loop that cannot afford cudaMalloc's implicit device
+ * synchronisation -- this computes, over the tets of `body` at the post-Jacobi
+ * positions pred_x + dx / count, the three FP64 means
+ *   out[0] = r_hat  (compute_xpbd_residual, neohookean_solver.py:298-329),
+ *   out[1] = mean |det F - 1|, out[2] = mean |tr F^T F - 3|
+ * into the caller's device array `out` (3 doubles), using only body->tets,
+ * dm_a, dm_b, dm_c, v0, lam and dx (atomic-variant layout) and pred_x
+ * ([V][4]); tet ids are not re-checked, so pass a body that xpbd_create has
+ * validated.  It calls no cudaMalloc, cudaFree or allocating library routine:
+ * its scratch is a static device array of (3 * 8192 + 1) doubles (192 KiB)
+ * that every GPU loading the library keeps until the process exits, so one
+ * call handles at most 8192 * 256 = 2,097,152 tets; larger meshes get
+ * XPBD_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls share the array and it
+ * keeps the last call's contents (the call clears the ticket it needs), so
+ * calls that overlap on the GPU -- on different streams, or from different
+ * threads -- race and must be serialised by the caller. */
+int xpbd_residual_noalloc(const xpbd_body* body, const float* pred_x, float dt, float lame_mu, float lame_lambda,
+                          int32_t precise_hydro, double* out, void* stream);
+
 /* Host mesh preprocessing (replaces the patcher's reorder, xpbd_base.py:42).
  * Permutations perm[new] = old: tets in Morton (Z-order) order of their
  * centroids; vertices in order of first use by the sorted tets (unused

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -812,6 +813,96 @@ __global__ void k_validate(Dev d) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Residual sweep that allocates nothing (xpbd_residual_noalloc).
+//
+// Its scratch -- one FP64 partial triple per CTA and the CTA ticket -- lives in
+// the file-scope array below, which every GPU that loads the library holds
+// until the process exits.  One CTA covers 256 tets, so a call handles at most
+// kNoAllocMaxBlocks * 256 tets.  The last CTA sums the partials in CTA order,
+// so the result does not depend on which CTAs finish first.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocMaxBlocks = 8192;
+constexpr long long kNoAllocMaxTets = (long long)kNoAllocMaxBlocks * kBlock;  // 2,097,152
+constexpr int kNoAllocTicket = 3 * kNoAllocMaxBlocks;  // slot of the CTA ticket (as a u64)
+static __device__ __align__(256) double g_noalloc_scratch[3 * kNoAllocMaxBlocks + 1];
+
+template <bool kPrecise>
+__global__ void __launch_bounds__(kBlock) k_residual_noalloc(Dev d, float cD, float cH, double* scratch,
+                                                             double* out) {
+  __shared__ double red[3][kBlock / 32];
+  __shared__ bool last;
+  const int t = blockIdx.x * kBlock + threadIdx.x;
+  float sr = 0.f, sh = 0.f, sd = 0.f;
+  if (t < d.T) {
+    int4 id;
+    Tet tt;
+    load_tet(d, t, id, tt);
+    const int vid[4] = {id.x, id.y, id.z, id.w};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float3 q = post_position(ldg4(d.p[0] + vid[c]), ldg4(d.dx + vid[c]));
+      tt.p[c] = make_float4(q.x, q.y, q.z, 0.f);
+    }
+    const float inv_v0 = 1.f / tt.V0;
+    residual_terms<true, true, kPrecise>(tt, d.lam[t], cD * inv_v0, cH * inv_v0, sr, sh, sd);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const double r0 = warp_sum((double)sr), r1 = warp_sum((double)sh), r2 = warp_sum((double)sd);
+  if (lane == 0) {
+    red[0][warp] = r0;
+    red[1][warp] = r1;
+    red[2][warp] = r2;
+  }
+  __syncthreads();
+  unsigned long long* ticket = reinterpret_cast<unsigned long long*>(scratch + kNoAllocTicket);
+  if (threadIdx.x == 0) {
+    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+    for (int k = 0; k < kBlock / 32; ++k) {
+      b0 += red[0][k];
+      b1 += red[1][k];
+      b2 += red[2][k];
+    }
+    scratch[3 * blockIdx.x + 0] = b0;
+    scratch[3 * blockIdx.x + 1] = b1;
+    scratch[3 * blockIdx.x + 2] = b2;
+    __threadfence();
+    last = atomicAdd(ticket, 1ull) == (unsigned long long)(gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // fixed-order sum of the CTA partials: thread j takes CTAs j, j + 256, ...
+  const volatile double* part = scratch;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int k = threadIdx.x; k < (int)gridDim.x; k += kBlock) {
+    a0 += part[3 * k + 0];
+    a1 += part[3 * k + 1];
+    a2 += part[3 * k + 2];
+  }
+  __syncthreads();
+  const double w0 = warp_sum(a0), w1 = warp_sum(a1), w2 = warp_sum(a2);
+  if (lane == 0) {
+    red[0][warp] = w0;
+    red[1][warp] = w1;
+    red[2][warp] = w2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double S = 0.0, H = 0.0, D = 0.0;
+    for (int k = 0; k < kBlock / 32; ++k) {
+      S += red[0][k];
+      H += red[1][k];
+      D += red[2][k];
+    }
+    const double n = (double)d.T;
+    out[0] = S / n;
+    out[1] = H / n;
+    out[2] = D / n;
+    *ticket = 0ull;
+  }
+}
+
 }  // namespace xpbd
 
 // ===========================================================================
@@ -1497,4 +1588,61 @@ int xpbd_check_status(void* handle, void* stream) {
   return flag ? fail(XPBD_ERR_NONFINITE, "non-finite residual") : XPBD_OK;
 }
 
+// Per-device address of g_noalloc_scratch, looked up once per device (with
+// that device current) on the first call made on it.
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_ptr[256] = {nullptr};
+
+int xpbd_residual_noalloc(const xpbd_body* body, const float* pred_x, float dt, float lame_mu, float lame_lambda,
+                          int32_t precise_hydro, double* out, void* stream) {
+  if (!body || !pred_x || !out) return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL body, pred_x or out");
+  if (body->n_tets <= 0 || body->n_verts <= 0) return fail(XPBD_ERR_BAD_MESH, "empty mesh");
+  if ((long long)body->n_tets > kNoAllocMaxTets)
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "xpbd_residual_noalloc handles at most " +
+                                               std::to_string(kNoAllocMaxTets) + " tets per call, got " +
+                                               std::to_string(body->n_tets));
+  if (!body->tets || !body->dm_a || !body->dm_b || !body->dm_c || !body->v0 || !body->lam || !body->dx)
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL body buffer");
+  if (!(dt > 0.f) || !(lame_mu != 0.f) || !(lame_lambda != 0.f))
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "need dt > 0 and non-zero Lame parameters");
+  int dev = 0;
+  XPBD_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return fail(XPBD_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+  double* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess)
+        return fail(XPBD_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      g_noalloc_ptr[dev] = static_cast<double*>(ptr);
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  Dev d{};
+  d.V = body->n_verts;
+  d.T = body->n_tets;
+  d.p[0] = const_cast<float4*>(reinterpret_cast<const float4*>(pred_x));
+  d.dx = reinterpret_cast<float4*>(body->dx);
+  d.tets = reinterpret_cast<const int4*>(body->tets);
+  d.dm_a = reinterpret_cast<const float4*>(body->dm_a);
+  d.dm_b = reinterpret_cast<const float4*>(body->dm_b);
+  d.dm_c = body->dm_c;
+  d.v0 = body->v0;
+  d.lam = reinterpret_cast<float2*>(body->lam);
+  const double dt2 = (double)dt * (double)dt;
+  const float cD = (float)(1.0 / ((double)lame_mu * dt2));
+  const float cH = (float)(1.0 / ((double)lame_lambda * dt2));
+  cudaStream_t st = S(stream);
+  // the ticket must start at zero; a clear, not an allocation
+  XPBD_CUDA(cudaMemsetAsync(scratch + kNoAllocTicket, 0, sizeof(unsigned long long), st));
+  const int grid = blocks_for(d.T);
+  if (precise_hydro) k_residual_noalloc<true><<<grid, kBlock, 0, st>>>(d, cD, cH, scratch, out);
+  else k_residual_noalloc<false><<<grid, kBlock, 0, st>>>(d, cD, cH, scratch, out);
+  XPBD_CUDA(cudaGetLastError());
+  return XPBD_OK;
+}
+
 }  // extern "C"
+

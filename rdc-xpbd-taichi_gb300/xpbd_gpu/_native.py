@@ -106,6 +106,8 @@ _SIGNATURES = {
     "xpbd_import_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "xpbd_export_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "xpbd_check_status": (ctypes.c_int, [_P, _P]),
+    "xpbd_residual_noalloc": (ctypes.c_int, [ctypes.POINTER(XpbdBody), _P, ctypes.c_float, ctypes.c_float,
+                                             ctypes.c_float, ctypes.c_int32, _P, _P]),
     "xpbd_set_profiling": (ctypes.c_int, [_P, ctypes.c_int32]),
     "xpbd_read_profile": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
                                          ctypes.c_int32, ctypes.c_int32, _P]),
