@@ -234,22 +234,37 @@ def tet_iterations_per_frame(mesh, kw):
 # CPU baseline: the oracle on a bounded sample
 # ---------------------------------------------------------------------------
 
-def cpu_baseline(mesh, specs, kw, iters=3):
-    """Time ``iters`` Jacobi iterations of one substep of the workload with the
-    CPU oracle (float32); returns tet-iterations/s and the sample text."""
-    from oracle.xpbd_oracle import OracleSdf, OracleSolver
-    okw = dict(kw)
-    okw.update(substeps_num=1, constraints_iter=iters, frame_dt=kw["dt"] / kw["substeps_num"],
-               dt=kw["dt"] / kw["substeps_num"])
-    o = OracleSolver(mesh.points, mesh.tets, [OracleSdf(k, **p) for k, p in specs], dtype=np.float32,
-                     total_mass=1000.0, **{k: v for k, v in okw.items() if k != "density"})
+def cpu_oracle(mesh, specs, kw, substeps, threads=None):
+    """The threaded FP32 C restatement of the reference substep on the workload's mesh,
+    stepping `substeps` substeps of the workload's substep length per call."""
+    from oracle.xpbd_oracle import OracleSdf
+    from oracle.xpbd_oracle_c import COracle
+    sub_dt = kw["dt"] / kw["substeps_num"]
+    okw = {k: v for k, v in kw.items() if k != "density"}
+    okw.update(substeps_num=substeps, frame_dt=sub_dt * substeps, dt=sub_dt * substeps)
+    total = kw.get("density", 1.0) * float(np.abs(_volume(mesh)).sum()) if "density" in kw else 1.0
+    return COracle(mesh.points, mesh.tets, [OracleSdf(k, **p) for k, p in specs], threads=threads,
+                   total_mass=total, **okw)
+
+
+def _volume(mesh):
+    P = mesh.points[mesh.tets]
+    return np.einsum("ij,ij->i", np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]), P[:, 3] - P[:, 0]) / 6.0
+
+
+def cpu_baseline(mesh, specs, kw, substeps=5):
+    """Time `substeps` substeps (x constraints_iter Jacobi iterations) of the workload with
+    the C restatement on every host core; returns tet-iterations/s and the sample text."""
+    threads = os.cpu_count() or 1
+    c = cpu_oracle(mesh, specs, kw, substeps, threads)
     t0 = time.perf_counter()
-    o.solve()
+    c.solve()
     el = time.perf_counter() - t0
-    units = mesh.n_tets * iters
-    return dict(value=units / el, unit=UNIT, cores=1, kind="port",
-                sample="NumPy float32 oracle, 1 substep x %d iterations of the same mesh (%d tet-iterations, %.1f s)"
-                % (iters, units, el))
+    units = mesh.n_tets * substeps * kw["constraints_iter"]
+    return dict(value=units / el, unit=UNIT, cores=threads, kind="port",
+                sample="C restatement (FP32, %d threads), %d substeps x %d iterations of the same mesh and "
+                       "substep length (%d tet-iterations, %.1f s)" % (threads, substeps, kw["constraints_iter"],
+                                                                        units, el))
 
 
 # ---------------------------------------------------------------------------
@@ -319,22 +334,34 @@ def dist_info():
 
 
 def run_reference(args):
+    """The reference arm: the reference's algorithm on the host cores.  The reference's
+    own Taichi CPU backend cannot be installed on this machine (no Taichi wheel for
+    Python 3.12, no network), so this times the C restatement on all host threads;
+    one step = one substep of the workload (constraints_iter Jacobi iterations)."""
     rank, _, world = dist_info()
     if rank != 0:
         return
     mesh, specs, kw, desc = workload(args.workload)
-    vals = []
+    threads = os.cpu_count() or 1
+    c = cpu_oracle(mesh, specs, kw, 1, threads)
     for _ in range(args.warmup):
-        cpu_baseline(mesh, specs, kw, iters=1)
+        c.solve()
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(mesh, specs, kw, iters=args.ref_iters))
-    v = float(np.mean([r["value"] for r in vals]))
+        c.solve()
+    el = time.perf_counter() - t0
+    units = mesh.n_tets * kw["constraints_iter"] * args.steps
+    v = units / el
     frame_units = tet_iterations_per_frame(mesh, kw)
+    sample = ("C restatement of the reference substep (FP32, %d threads): %d substeps x %d iterations, %.1f s"
+              % (threads, args.steps, kw["constraints_iter"], el))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": frame_units / v * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": desc},
-            "cpu_baseline": dict(vals[-1], value=v),
+            "data": "synthetic", "config": {"workload": desc, "step": "one substep (%d tet-iterations)"
+                                            % (mesh.n_tets * kw["constraints_iter"])},
+            "frames_per_s": v / frame_units,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -468,7 +495,7 @@ def run_gb300(args):
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(mesh, specs, kw, iters=args.cpu_iters)
+        line["cpu_baseline"] = cpu_baseline(mesh, specs, kw, substeps=args.cpu_substeps)
     print(json.dumps(line), flush=True)
 
 
@@ -500,8 +527,7 @@ def main():
     ap.add_argument("--patch-reduce", type=int, default=0, choices=[0, 1])
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-iters", type=int, default=3)
-    ap.add_argument("--ref-iters", type=int, default=2)
+    ap.add_argument("--cpu-substeps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     ap.add_argument("--profile-frames", type=int, default=1)
