@@ -527,7 +527,7 @@ def main():
     ap.add_argument("--patch-reduce", type=int, default=0, choices=[0, 1])
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-substeps", type=int, default=5)
+    ap.add_argument("--cpu-substeps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     ap.add_argument("--profile-frames", type=int, default=1)
