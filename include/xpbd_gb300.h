@@ -104,6 +104,10 @@ typedef struct xpbd_body {
   const float* dm_c;     /* [T] inv_Dm[2][2] */
   const float* v0;       /* [T] rest volume V0 */
   float* lam;            /* [T][2] lambda_D, lambda_H */
+  /* optional per-tet materials (ATOMIC / GATHER variants): 1 / mu and
+   * 1 / lambda of every tet; NULL = the uniform lame_mu / lame_lambda */
+  const float* tet_inv_mu;     /* [T] */
+  const float* tet_inv_lambda; /* [T] */
   /* deterministic gather variant (XPBD_SCATTER_GATHER); may be NULL otherwise */
   const int32_t* v2t_offsets; /* [V+1] CSR row offsets */
   const int32_t* v2t_slots;   /* [4T] tet*4+corner, ascending per vertex */
@@ -216,6 +220,40 @@ int xpbd_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, in
 /* Sticky device error flags (XPBD_OK, XPBD_ERR_NONFINITE or XPBD_ERR_TIMEOUT);
  * synchronises. */
 int xpbd_check_status(void* handle, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Differentiation of one substep (block mode, ATOMIC or GATHER variant,
+ * per-tet materials).  No counterpart in the reference, which has no
+ * gradients; the adjoint follows the forward of neohookean_solver.py:453-587.
+ * omega is a stop-gradient; contact sets and the pivot branch are piecewise
+ * constant.
+ * ------------------------------------------------------------------------ */
+typedef struct xpbd_tape {
+  float* xs;   /* [(K+1)][V][4] predicted positions entering every iteration */
+  float* lams; /* [K][T][2] multipliers entering every iteration */
+  float* xpre; /* [V][4] predicted positions before the SDF list */
+  float* v1;   /* [V][4] velocities after gravity */
+} xpbd_tape;
+
+typedef struct xpbd_adjoint {
+  float* gx;            /* [V][4] in: dL/dx after the substep; out: before it */
+  float* gv;            /* [V][4] likewise for v */
+  double* g_inv_mu;     /* [T] += dL/d(1/mu) of every tet */
+  double* g_inv_lambda; /* [T] += dL/d(1/lambda) */
+  float* work0;         /* [V][4] scratch */
+  float* work1;         /* [V][4] scratch */
+  float* ybar;          /* [V][4] scratch */
+  float* dxbar;         /* [V][4] scratch */
+  float* lambar;        /* [T][2] scratch */
+  const float* cnt;     /* [V] constraints per vertex (vertex valence) */
+} xpbd_adjoint;
+
+/* One substep (as xpbd_substep) that records `tape`; history rows [0, K)
+ * receive its omegas for xpbd_substep_adjoint. */
+int xpbd_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* stream);
+
+/* Reverse of the substep last run by xpbd_substep_tape with the same tape. */
+int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xpbd_adjoint* adj, void* stream);
 
 /* Residual sweep that allocates nothing.  No counterpart in the reference.
  * For callers that may not allocate device memory -- an engine or plugin host

@@ -1,0 +1,309 @@
+// Adjoint (reverse-mode) kernels of one block Neo-Hookean substep.
+//
+// The forward substep is recomputed from a per-substep checkpoint with its
+// intermediate states recorded on a tape (predicted positions before every
+// Jacobi iteration, the multipliers entering it, the predicted positions
+// before the SDF list and the velocities after gravity); the kernels below
+// then run the substep backwards:
+//   ka_end      advance            (xpbd_base.py:148-160)
+//   per iteration k = K-1 .. 0:
+//     ka_cheb   Chebyshev mix + post_solve (neohookean_solver.py:115-142, :548)
+//     ka_project block projection: Jacobian-transpose of F -> (C, grad C) ->
+//                2x2 compliance solve -> dx (:358-451), with the material
+//                adjoints accumulated per tet in FP64
+//   ka_begin    SDF list in reverse order + predict (xpbd_base.py:139-178)
+// Conventions: omega is a stop-gradient (a control heuristic of the
+// residual ratio); the contact sets and the pivot branch are piecewise
+// constant; the derivative of the 2x2 solve is that of A^-1 b.
+#pragma once
+
+namespace xpbd {
+
+struct Tape {
+  float4* xs;    // [(K+1)][V] predicted positions entering iteration k (w = inv_m)
+  float2* lams;  // [K][T] multipliers entering iteration k
+  float4* xpre;  // [V] predicted positions before the SDF list
+  float4* v1;    // [V] velocities after gravity
+};
+
+struct Adj {
+  float4* gx;        // [V] in: dL/dx at the end of the substep, out: at its start
+  float4* gv;        // [V] in / out, likewise for v
+  double* g_mu;      // [T] accumulated dL/d(1/mu)
+  double* g_la;      // [T] accumulated dL/d(1/lambda)
+  float4* abuf[2];   // [V] adjoint of the predicted positions (ping-pong)
+  float4* ybar;      // [V] adjoint of the Chebyshev y_prev
+  float4* dxbar;     // [V] adjoint of the Jacobi accumulator
+  float2* lambar;    // [T] adjoint of the multipliers
+  const float* cnt;  // [V] constraints per vertex (valence in block mode)
+};
+
+__device__ __forceinline__ float3 f3(const float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 cross3(const float3 a, const float3 b) {
+  return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+
+// Velocities after gravity and predicted positions before the SDF list.
+__global__ void __launch_bounds__(256) k_tape_begin(Dev d, Tape tp, float dt, float gx, float gy, float gz) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.V) return;
+  const float4 xi = d.x[i];
+  float4 vi = d.v[i];
+  if (xi.w > 0.f) {
+    vi.x += gx * dt;
+    vi.y += gy * dt;
+    vi.z += gz * dt;
+  }
+  tp.v1[i] = vi;
+  tp.xpre[i] = make_float4(xi.x + vi.x * dt, xi.y + vi.y * dt, xi.z + vi.z * dt, xi.w);
+}
+
+// Reverse of advance: live vertices x' = x~_K, v' = (x~_K - x) e / dt; pinned
+// vertices keep x and v.
+__global__ void __launch_bounds__(256) ka_end(Dev d, Adj a, float e_over_dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.V) return;
+  const float4 gx = a.gx[i], gv = a.gv[i];
+  if (d.x[i].w > 0.f) {
+    a.abuf[0][i] = make_float4(gx.x + gv.x * e_over_dt, gx.y + gv.y * e_over_dt, gx.z + gv.z * e_over_dt, 0.f);
+    a.gx[i] = make_float4(-gv.x * e_over_dt, -gv.y * e_over_dt, -gv.z * e_over_dt, 0.f);
+    a.gv[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  } else {
+    a.abuf[0][i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  a.ybar[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Reverse of the Chebyshev mix and post_solve of iteration k:
+//   post = x~_k + dx / cnt,  xn = gamma (post - x~_k) + x~_k,
+//   x~_{k+1} = y_prev + omega (xn - y_prev),  y_prev(k+1) = x~_k,
+// with y_prev(0) = x~_0.  Reads abuf[src] (adjoint of x~_{k+1}), writes
+// abuf[src^1] (direct part of the adjoint of x~_k), ybar and dxbar.
+template <bool kCheb>
+__global__ void __launch_bounds__(256) ka_cheb(Dev d, Adj a, int k, float gamma, int src) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.V) return;
+  const float4 xb = a.abuf[src][i];
+  float3 post, cur, yn;
+  if (kCheb) {
+    const float om = (float)d.hist[4 * k + 1];
+    const float4 yb = a.ybar[i];
+    post = make_float3(om * gamma * xb.x, om * gamma * xb.y, om * gamma * xb.z);
+    const float c = om * (1.f - gamma);
+    cur = make_float3(c * xb.x + post.x + yb.x, c * xb.y + post.y + yb.y, c * xb.z + post.z + yb.z);
+    yn = make_float3((1.f - om) * xb.x, (1.f - om) * xb.y, (1.f - om) * xb.z);
+    if (k == 0) {
+      cur.x += yn.x;
+      cur.y += yn.y;
+      cur.z += yn.z;
+    }
+  } else {
+    post = f3(xb);
+    cur = post;
+    yn = make_float3(0.f, 0.f, 0.f);
+  }
+  a.abuf[src ^ 1][i] = make_float4(cur.x, cur.y, cur.z, 0.f);
+  a.ybar[i] = make_float4(yn.x, yn.y, yn.z, 0.f);
+  const float c = a.cnt[i];
+  const float ic = c > 0.f ? 1.f / c : 0.f;
+  a.dxbar[i] = make_float4(post.x * ic, post.y * ic, post.z * ic, 0.f);
+}
+
+// Reverse of the block projection of iteration k for one tet; scatters the
+// position adjoints into abuf[dst] and updates the multiplier adjoint.
+template <bool kPrecise>
+__global__ void __launch_bounds__(128) ka_project(Dev d, Tape tp, Adj a, int k, float cD, float cH, int dst) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= d.T) return;
+  int4 id;
+  Tet tt;
+  load_tet(d, t, id, tt);
+  const float4* X = tp.xs + (size_t)k * d.V;
+  tt.p[0] = __ldg(X + id.x);
+  tt.p[1] = __ldg(X + id.y);
+  tt.p[2] = __ldg(X + id.z);
+  tt.p[3] = __ldg(X + id.w);
+  const float2 L = tp.lams[(size_t)k * d.T + t];
+  const float w[4] = {tt.p[0].w, tt.p[1].w, tt.p[2].w, tt.p[3].w};
+  const int vid[4] = {id.x, id.y, id.z, id.w};
+  const float inv_v0 = 1.f / tt.V0;
+  float sD = cD * inv_v0, sH = cH * inv_v0;  // d aD / d(1/mu) (per-tet materials) or aD itself
+  float aD = sD, aH = sH;
+  if (d.tinv_mu) {
+    aD *= __ldg(d.tinv_mu + t);
+    aH *= __ldg(d.tinv_la + t);
+  }
+  // ---- forward recompute ----
+  float F[9];
+  deformation_gradient(tt, F);
+  float C_D, C_H;
+  invariants<kPrecise>(F, C_D, C_H);
+  float gF[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) gF[q] = 2.f * F[q];
+  float3 gD[4], gH[4];
+  corner_gradients(gF, tt.dm, gD);
+  float H[9];
+  cofactor(F, H);
+  corner_gradients(H, tt.dm, gH);
+  float A11 = aD, A22 = aH, A12 = 0.f;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    A11 += w[c] * dot3(gD[c], gD[c]);
+    A22 += w[c] * dot3(gH[c], gH[c]);
+    A12 += w[c] * dot3(gD[c], gH[c]);
+  }
+  const float b1 = -(C_D + aD * L.x), b2 = -(C_H + aH * L.y);
+  const float det = A11 * A22 - A12 * A12;
+  const float idet = 1.f / det;
+  const float dD = (A22 * b1 - A12 * b2) * idet;
+  const float dH = (A11 * b2 - A12 * b1) * idet;
+  // ---- reverse ----
+  const float2 lb_next = a.lambar[t];
+  float dDb = lb_next.x, dHb = lb_next.y;
+  float3 dpb[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    dpb[c] = f3(a.dxbar[vid[c]]);
+    dDb += w[c] * dot3(gD[c], dpb[c]);
+    dHb += w[c] * dot3(gH[c], dpb[c]);
+  }
+  const float bb1 = (A22 * dDb - A12 * dHb) * idet;
+  const float bb2 = (A11 * dHb - A12 * dDb) * idet;
+  const float A11b = -bb1 * dD, A22b = -bb2 * dH, A12b = -(bb1 * dH + bb2 * dD);
+  const float CDb = -bb1, CHb = -bb2;
+  const float aDb = -L.x * bb1 + A11b, aHb = -L.y * bb2 + A22b;
+  a.lambar[t] = make_float2(lb_next.x - aD * bb1, lb_next.y - aH * bb2);
+  // adjoints of the corner gradients
+  float3 gDb[4], gHb[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float wd = w[c] * dD, wh = w[c] * dH, a1 = 2.f * w[c] * A11b, a2 = 2.f * w[c] * A22b, a3 = w[c] * A12b;
+    gDb[c] = make_float3(wd * dpb[c].x + a1 * gD[c].x + a3 * gH[c].x, wd * dpb[c].y + a1 * gD[c].y + a3 * gH[c].y,
+                         wd * dpb[c].z + a1 * gD[c].z + a3 * gH[c].z);
+    gHb[c] = make_float3(wh * dpb[c].x + a2 * gH[c].x + a3 * gD[c].x, wh * dpb[c].y + a2 * gH[c].y + a3 * gD[c].y,
+                         wh * dpb[c].z + a2 * gH[c].z + a3 * gD[c].z);
+  }
+  // g_{c+1}[r] = sum_q G[r][q] dm[c][q], g_0 = -sum  =>  G_bar[r][q] = sum_c (gb_{c+1} - gb_0)[r] dm[c][q]
+  float GDb[9], Hb[9];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      float sd = 0.f, sh = 0.f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float ed = (r == 0 ? gDb[c + 1].x - gDb[0].x : r == 1 ? gDb[c + 1].y - gDb[0].y : gDb[c + 1].z - gDb[0].z);
+        const float eh = (r == 0 ? gHb[c + 1].x - gHb[0].x : r == 1 ? gHb[c + 1].y - gHb[0].y : gHb[c + 1].z - gHb[0].z);
+        sd += ed * tt.dm[c * 3 + q];
+        sh += eh * tt.dm[c * 3 + q];
+      }
+      GDb[r * 3 + q] = sd;
+      Hb[r * 3 + q] = sh;
+    }
+  // F_bar = 2 GD_bar + 2 C_D_bar F + C_H_bar cof(F) + (d cof)^T H_bar
+  float Fb[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) Fb[q] = 2.f * GDb[q] + 2.f * CDb * F[q] + CHb * H[q];
+  {
+    const float3 F0 = make_float3(F[0], F[3], F[6]), F1 = make_float3(F[1], F[4], F[7]), F2 = make_float3(F[2], F[5], F[8]);
+    const float3 H0b = make_float3(Hb[0], Hb[3], Hb[6]), H1b = make_float3(Hb[1], Hb[4], Hb[7]),
+                 H2b = make_float3(Hb[2], Hb[5], Hb[8]);
+    const float3 c0 = cross3(H1b, F2), c0b = cross3(F1, H2b);
+    const float3 c1 = cross3(F2, H0b), c1b = cross3(H2b, F0);
+    const float3 c2 = cross3(H0b, F1), c2b = cross3(F0, H1b);
+    Fb[0] += c0.x + c0b.x; Fb[3] += c0.y + c0b.y; Fb[6] += c0.z + c0b.z;
+    Fb[1] += c1.x + c1b.x; Fb[4] += c1.y + c1b.y; Fb[7] += c1.z + c1b.z;
+    Fb[2] += c2.x + c2b.x; Fb[5] += c2.y + c2b.y; Fb[8] += c2.z + c2b.z;
+  }
+  // F = E Dm (E[r][c] = e_c[r])  =>  E_bar[r][c] = sum_q F_bar[r][q] dm[c][q]
+  float3 eb[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    eb[c] = make_float3(Fb[0] * tt.dm[c * 3] + Fb[1] * tt.dm[c * 3 + 1] + Fb[2] * tt.dm[c * 3 + 2],
+                        Fb[3] * tt.dm[c * 3] + Fb[4] * tt.dm[c * 3 + 1] + Fb[5] * tt.dm[c * 3 + 2],
+                        Fb[6] * tt.dm[c * 3] + Fb[7] * tt.dm[c * 3 + 1] + Fb[8] * tt.dm[c * 3 + 2]);
+  float4* G = a.abuf[dst];
+  red_add_v4(G + vid[0], -(eb[0].x + eb[1].x + eb[2].x), -(eb[0].y + eb[1].y + eb[2].y),
+             -(eb[0].z + eb[1].z + eb[2].z), 0.f);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) red_add_v4(G + vid[c + 1], eb[c].x, eb[c].y, eb[c].z, 0.f);
+  // materials: aD = (1/mu) sD, aH = (1/lambda) sH
+  a.g_mu[t] += (double)(aDb * sD);
+  a.g_la[t] += (double)(aHb * sH);
+}
+
+// q_bar = J^T q_bar for the SDF projection q' = q + n(q) (-phi(q)) at q.
+__device__ __forceinline__ float3 sdf_adjoint(const xpbd_sdf& s, const float3 q, float3 gb) {
+  if (s.kind == XPBD_SDF_PLANE) {
+    const float dn = gb.x * s.b[0] + gb.y * s.b[1] + gb.z * s.b[2];
+    return make_float3(gb.x - s.b[0] * dn, gb.y - s.b[1] * dn, gb.z - s.b[2] * dn);
+  }
+  const float dx = q.x - s.a[0], dy = q.y - s.a[1], dz = q.z - s.a[2];
+  if (s.kind == XPBD_SDF_SPHERE) {  // J = (r + eps) / (|d| + eps) (I - |d| / (|d| + eps) u u^T)
+    const float sl = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float iu = 1.f / sl;
+    const float ux = dx * iu, uy = dy * iu, uz = dz * iu;
+    const float kk = (s.b[0] + kEps) / (sl + kEps), cc = sl / (sl + kEps);
+    const float ug = ux * gb.x + uy * gb.y + uz * gb.z;
+    return make_float3(kk * (gb.x - cc * ux * ug), kk * (gb.y - cc * uy * ug), kk * (gb.z - cc * uz * ug));
+  }
+  // cube: J = I - n grad(phi)^T; n on the dominant axis of (q - c), grad(phi)
+  // on the largest (|q - c| - half size), both signed like (q - c)
+  const float ad[3] = {fabsf(dx), fabsf(dy), fabsf(dz)};
+  const float dv[3] = {dx, dy, dz};
+  int na = 0;
+  float amax = ad[0];
+  if (ad[1] > ad[0]) { na = 1; amax = ad[1]; }
+  if (ad[2] > amax) na = 2;
+  const float e[3] = {ad[0] - s.b[0], ad[1] - s.b[1], ad[2] - s.b[2]};
+  int ga = 0;
+  if (e[1] > e[ga]) ga = 1;
+  if (e[2] > e[ga]) ga = 2;
+  const float sn = dv[na] > 0.f ? 1.f : -1.f, sg = dv[ga] > 0.f ? 1.f : -1.f;
+  float g[3] = {gb.x, gb.y, gb.z};
+  g[ga] -= sg * sn * g[na];
+  return make_float3(g[0], g[1], g[2]);
+}
+
+// Reverse of the SDF list (in reverse order) and of predict; adds into gx, gv.
+__global__ void __launch_bounds__(256) ka_begin(Dev d, Tape tp, Adj a, int src, float dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.V) return;
+  float3 gb = f3(a.abuf[src][i]);
+  const float4 pre = tp.xpre[i];
+  if (pre.w > 0.f) {
+    const float3 vel = f3(tp.v1[i]);
+    for (int s = d.n_sdf - 1; s >= 0; --s) {
+      // positions entering SDF s: replay the list up to s
+      float3 q = f3(pre);
+      for (int r = 0; r < s; ++r) {
+        const xpbd_sdf sd = d.sdfs[r];
+        const float phi = sdf_dist(sd, q);
+        if (phi < 0.f) {
+          const float3 n = sdf_normal(sd, q);
+          const float dotnv = n.x * (sd.vel[0] - vel.x) + n.y * (sd.vel[1] - vel.y) + n.z * (sd.vel[2] - vel.z);
+          if (dotnv > 0.f || sd.fixed) {
+            q.x -= n.x * phi;
+            q.y -= n.y * phi;
+            q.z -= n.z * phi;
+          }
+        }
+      }
+      const xpbd_sdf sd = d.sdfs[s];
+      const float phi = sdf_dist(sd, q);
+      if (phi < 0.f) {
+        const float3 n = sdf_normal(sd, q);
+        const float dotnv = n.x * (sd.vel[0] - vel.x) + n.y * (sd.vel[1] - vel.y) + n.z * (sd.vel[2] - vel.z);
+        if (dotnv > 0.f || sd.fixed) gb = sdf_adjoint(sd, q, gb);
+      }
+    }
+  }
+  float4 gx = a.gx[i], gv = a.gv[i];
+  gx.x += gb.x; gx.y += gb.y; gx.z += gb.z;
+  gv.x += gb.x * dt; gv.y += gb.y * dt; gv.z += gb.z * dt;
+  a.gx[i] = gx;
+  a.gv[i] = gv;
+}
+
+}  // namespace xpbd

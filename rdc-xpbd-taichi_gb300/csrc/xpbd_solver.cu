@@ -56,6 +56,8 @@ struct Dev {
   const float* dm_c;
   const float* v0;
   float2* lam;
+  const float* tinv_mu;  // per-tet 1 / mu (nullptr: uniform)
+  const float* tinv_la;  // per-tet 1 / lambda
   const int* v2t_off;
   const int* v2t_slot;
   float4* corner;
@@ -219,7 +221,12 @@ __global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float cD, fl
   float3 dp[4];
   float cnt;
   const float inv_v0 = 1.f / tt.V0;
-  project_tet<kBlockMode, kPrecise>(tt, cD * inv_v0, cH * inv_v0, relax_h, relax_d, L, dp, cnt);
+  float aD = cD * inv_v0, aH = cH * inv_v0;
+  if (d.tinv_mu) {  // per-tet materials: cD = cH = 1 / dt^2
+    aD *= __ldg(d.tinv_mu + t);
+    aH *= __ldg(d.tinv_la + t);
+  }
+  project_tet<kBlockMode, kPrecise>(tt, aD, aH, relax_h, relax_d, L, dp, cnt);
   d.lam[t] = L;
 #pragma unroll
   for (int c = 0; c < 4; ++c) emit<kGather>(d, t, c, vid[c], dp[c], cnt);
@@ -511,7 +518,12 @@ __global__ void __launch_bounds__(kBlock) k_residual(Dev d, SweepArgs a) {
     }
     const float2 L = kRes ? d.lam[t] : make_float2(0.f, 0.f);
     const float inv_v0 = 1.f / tt.V0;
-    residual_terms<kRes, kMon, kPrecise>(tt, L, a.cD * inv_v0, a.cH * inv_v0, sr, sh, sd);
+    float aD = a.cD * inv_v0, aH = a.cH * inv_v0;
+    if (d.tinv_mu) {
+      aD *= __ldg(d.tinv_mu + t);
+      aH *= __ldg(d.tinv_la + t);
+    }
+    residual_terms<kRes, kMon, kPrecise>(tt, L, aD, aH, sr, sh, sd);
   }
   finish_residual<kRes, kMon>(d, a, sr, sh, sd);
 }
@@ -905,6 +917,8 @@ __global__ void __launch_bounds__(kBlock) k_residual_noalloc(Dev d, float cD, fl
 
 }  // namespace xpbd
 
+#include "xpbd_adjoint.cuh"
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
@@ -1049,11 +1063,16 @@ void launch_project_patch_t(Solver* s, float cD, float cH, cudaStream_t st) {
   }
 }
 
-// 1 / (mu dt^2) and 1 / (lambda dt^2), rounded once from double
-inline void compliance_factors(const xpbd_params& p, float dt, float& cD, float& cH) {
+// 1 / (mu dt^2) and 1 / (lambda dt^2), rounded once from double; with per-tet
+// materials both are 1 / dt^2 and the kernels multiply by the tet's 1 / mu, 1 / lambda
+inline void compliance_factors(const Solver* s, float dt, float& cD, float& cH) {
   const double dt2 = (double)dt * (double)dt;
-  cD = (float)(1.0 / ((double)p.lame_mu * dt2));
-  cH = (float)(1.0 / ((double)p.lame_lambda * dt2));
+  if (s->d.tinv_mu) {
+    cD = cH = (float)(1.0 / dt2);
+    return;
+  }
+  cD = (float)(1.0 / ((double)s->prm.lame_mu * dt2));
+  cH = (float)(1.0 / ((double)s->prm.lame_lambda * dt2));
 }
 
 template <bool kBlockMode, bool kFirst, bool kPrecise>
@@ -1066,7 +1085,7 @@ void launch_project(Solver* s, bool first, float dt, cudaStream_t st) {
   Prof prof(s, XPBD_K_PROJECT, st);
   const bool blk = s->prm.block_mode != 0, pr = s->prm.precise_hydro != 0;
   float cD, cH;
-  compliance_factors(s->prm, dt, cD, cH);
+  compliance_factors(s, dt, cD, cH);
   if (blk) {
     if (first) pr ? launch_project_any<true, true, true>(s, cD, cH, st) : launch_project_any<true, true, false>(s, cD, cH, st);
     else pr ? launch_project_any<true, false, true>(s, cD, cH, st) : launch_project_any<true, false, false>(s, cD, cH, st);
@@ -1120,7 +1139,7 @@ void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
   if (cheb || mon) {
     SweepArgs a;
     a.cur = s->cur;
-    compliance_factors(p, dt, a.cD, a.cH);
+    compliance_factors(s, dt, a.cD, a.cH);
     a.it = it;
     a.warmup = p.cheb_warmup;
     a.rec = rec;
@@ -1279,6 +1298,16 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
   d.dm_c = body->dm_c;
   d.v0 = body->v0;
   d.lam = reinterpret_cast<float2*>(body->lam);
+  d.tinv_mu = body->tet_inv_mu;
+  d.tinv_la = body->tet_inv_lambda;
+  if ((d.tinv_mu == nullptr) != (d.tinv_la == nullptr)) {
+    delete s;
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "tet_inv_mu and tet_inv_lambda must be given together");
+  }
+  if (d.tinv_mu && params->scatter == XPBD_SCATTER_PATCH) {
+    delete s;
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "per-tet materials need the ATOMIC or GATHER variant");
+  }
   d.v2t_off = body->v2t_offsets;
   d.v2t_slot = body->v2t_slots;
   d.corner = reinterpret_cast<float4*>(body->corner_dx);
@@ -1387,6 +1416,8 @@ int xpbd_set_params(void* handle, const xpbd_params* params) {
     return fail(XPBD_ERR_INVALID_ARGUMENT, "gather variant needs CSR buffers given at create");
   if (params->scatter == XPBD_SCATTER_PATCH && !s->d.lid)
     return fail(XPBD_ERR_INVALID_ARGUMENT, "patch variant needs the patch layout given at create");
+  if (params->scatter == XPBD_SCATTER_PATCH && s->d.tinv_mu)
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "per-tet materials need the ATOMIC or GATHER variant");
   if (std::memcmp(&s->prm, params, sizeof(xpbd_params)) != 0) drop_graph(s);
   s->prm = *params;
   return XPBD_OK;
@@ -1586,6 +1617,83 @@ int xpbd_check_status(void* handle, void* stream) {
   XPBD_CUDA(cudaStreamSynchronize(S(stream)));
   if (tmo) return fail(XPBD_ERR_TIMEOUT, "a bounded mbarrier wait timed out; results are invalid");
   return flag ? fail(XPBD_ERR_NONFINITE, "non-finite residual") : XPBD_OK;
+}
+
+static int check_diff(Solver* s) {
+  if (!s->prm.block_mode) return fail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint supports block mode only");
+  if (s->prm.scatter == XPBD_SCATTER_PATCH) return fail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint needs ATOMIC or GATHER");
+  if (!s->d.tinv_mu) return fail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint needs per-tet materials");
+  if (s->prm.constraints_iter > s->max_records)
+    return fail(XPBD_ERR_HISTORY_FULL, "history shorter than constraints_iter");
+  return XPBD_OK;
+}
+
+int xpbd_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* stream) {
+  Solver* s = static_cast<Solver*>(handle);
+  if (!s || !tape || !tape->xs || !tape->lams || !tape->xpre || !tape->v1)
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or tape buffer");
+  int r = check_diff(s);
+  if (r != XPBD_OK) return r;
+  cudaStream_t st = S(stream);
+  const int K = s->prm.constraints_iter, V = s->d.V, T = s->d.T;
+  Tape tp{reinterpret_cast<float4*>(tape->xs), reinterpret_cast<float2*>(tape->lams),
+          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1)};
+  const float* g = s->prm.gravity;
+  k_tape_begin<<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, dt, g[0], g[1], g[2]);
+  s->cur = 0;
+  launch_begin(s, true, true, dt, st);
+  for (int it = 0; it < K; ++it) {
+    XPBD_CUDA(cudaMemcpyAsync(tp.xs + (size_t)it * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
+    if (it == 0) XPBD_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
+    else
+      XPBD_CUDA(cudaMemcpyAsync(tp.lams + (size_t)it * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
+    launch_iteration(s, it, dt, it, st);
+  }
+  XPBD_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
+  k_end<<<blocks_for(V), kBlock, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
+  XPBD_CUDA(cudaGetLastError());
+  return XPBD_OK;
+}
+
+int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xpbd_adjoint* adj, void* stream) {
+  Solver* s = static_cast<Solver*>(handle);
+  if (!s || !tape || !adj || !adj->gx || !adj->gv || !adj->g_inv_mu || !adj->g_inv_lambda || !adj->work0 ||
+      !adj->work1 || !adj->ybar || !adj->dxbar || !adj->lambar || !adj->cnt)
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle, tape or adjoint buffer");
+  int r = check_diff(s);
+  if (r != XPBD_OK) return r;
+  cudaStream_t st = S(stream);
+  const int K = s->prm.constraints_iter, V = s->d.V, T = s->d.T;
+  Tape tp{reinterpret_cast<float4*>(tape->xs), reinterpret_cast<float2*>(tape->lams),
+          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1)};
+  Adj a;
+  a.gx = reinterpret_cast<float4*>(adj->gx);
+  a.gv = reinterpret_cast<float4*>(adj->gv);
+  a.g_mu = adj->g_inv_mu;
+  a.g_la = adj->g_inv_lambda;
+  a.abuf[0] = reinterpret_cast<float4*>(adj->work0);
+  a.abuf[1] = reinterpret_cast<float4*>(adj->work1);
+  a.ybar = reinterpret_cast<float4*>(adj->ybar);
+  a.dxbar = reinterpret_cast<float4*>(adj->dxbar);
+  a.lambar = reinterpret_cast<float2*>(adj->lambar);
+  a.cnt = adj->cnt;
+  XPBD_CUDA(cudaMemsetAsync(a.lambar, 0, sizeof(float2) * T, st));
+  const float e_over_dt = expf(-dt * s->prm.damping) / dt;
+  ka_end<<<blocks_for(V), kBlock, 0, st>>>(s->d, a, e_over_dt);
+  float cD, cH;
+  compliance_factors(s, dt, cD, cH);
+  int src = 0;
+  for (int k = K - 1; k >= 0; --k) {
+    if (s->prm.cheb_enable) ka_cheb<true><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
+    else ka_cheb<false><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
+    const int g = (T + 127) / 128;
+    if (s->prm.precise_hydro) ka_project<true><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
+    else ka_project<false><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
+    src ^= 1;
+  }
+  ka_begin<<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, src, dt);
+  XPBD_CUDA(cudaGetLastError());
+  return XPBD_OK;
 }
 
 // Per-device address of g_noalloc_scratch, looked up once per device (with

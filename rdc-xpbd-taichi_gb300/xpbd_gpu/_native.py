@@ -65,6 +65,7 @@ class XpbdBody(ctypes.Structure):
     _fields_ = [("n_verts", ctypes.c_int32), ("n_tets", ctypes.c_int32),
                 ("x", _P), ("v", _P), ("p0", _P), ("p1", _P), ("dx", _P),
                 ("tets", _P), ("dm_a", _P), ("dm_b", _P), ("dm_c", _P), ("v0", _P), ("lam", _P),
+                ("tet_inv_mu", _P), ("tet_inv_lambda", _P),
                 ("v2t_offsets", _P), ("v2t_slots", _P), ("corner_dx", _P),
                 ("vert_perm", _P),
                 ("n_patches", ctypes.c_int32), ("patch_tets", ctypes.c_int32),
@@ -80,6 +81,15 @@ class XpbdBatch(ctypes.Structure):
                 ("patch_voff", _P), ("patch_verts", _P), ("patch_body", _P), ("patch_ntets", _P),
                 ("vblock_body", _P), ("body_inv_mu", _P), ("body_inv_lambda", _P),
                 ("body_n_patches", _P), ("body_n_tets", _P), ("vert_perm", _P)]
+
+
+class XpbdTape(ctypes.Structure):
+    _fields_ = [("xs", _P), ("lams", _P), ("xpre", _P), ("v1", _P)]
+
+
+class XpbdAdjoint(ctypes.Structure):
+    _fields_ = [("gx", _P), ("gv", _P), ("g_inv_mu", _P), ("g_inv_lambda", _P), ("work0", _P), ("work1", _P),
+                ("ybar", _P), ("dxbar", _P), ("lambar", _P), ("cnt", _P)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/xpbd_gb300.h
@@ -106,6 +116,9 @@ _SIGNATURES = {
     "xpbd_import_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "xpbd_export_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "xpbd_check_status": (ctypes.c_int, [_P, _P]),
+    "xpbd_substep_tape": (ctypes.c_int, [_P, ctypes.c_float, ctypes.POINTER(XpbdTape), _P]),
+    "xpbd_substep_adjoint": (ctypes.c_int, [_P, ctypes.c_float, ctypes.POINTER(XpbdTape),
+                                            ctypes.POINTER(XpbdAdjoint), _P]),
     "xpbd_residual_noalloc": (ctypes.c_int, [ctypes.POINTER(XpbdBody), _P, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_float, ctypes.c_int32, _P, _P]),
     "xpbd_set_profiling": (ctypes.c_int, [_P, ctypes.c_int32]),

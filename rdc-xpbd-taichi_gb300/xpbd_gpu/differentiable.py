@@ -1,0 +1,141 @@
+"""Differentiable XPBD simulation: gradients of a loss on the final positions
+w.r.t. per-tet log Young's modulus and Poisson ratio, initial positions and
+initial velocities.
+
+The reference has no gradients.  The forward is the reference's substep
+(``neohookean_solver.py:453-587``) run on the GPU with per-tet materials;
+``xpbd_simulate`` wraps it in a ``torch.autograd.Function`` whose backward
+runs hand-written adjoint kernels (``xpbd_substep_adjoint``).  The state is
+checkpointed once per substep (positions, velocities, rho_hat) and every
+substep's Jacobi iterations are recomputed on a tape before its reverse pass.
+
+Differentiation conventions: the Chebyshev factor omega is a stop-gradient
+(it is a control heuristic of the residual ratio, neohookean_solver.py:
+495-546); active contact sets and the 2x2 pivot branch are piecewise
+constant.
+"""
+import numpy as np
+
+from xpbd_gpu import _native
+from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver, frame_chunks
+from xpbd_gpu.xpbd_base import _torch
+
+
+class DiffSim:
+    """A single body with per-tet materials and the buffers of its adjoint."""
+
+    def __init__(self, rest_pose, sdf, log_E, nu, scatter="atomic", **kw):
+        kw.setdefault("block_neohookean_enable", True)
+        if not kw["block_neohookean_enable"]:
+            raise ValueError("the adjoint supports the block projection only")
+        log_E = np.asarray(log_E, dtype=np.float64)
+        self.solver = XPBDNeoHookeanSolver(rest_pose, sdf, tet_young_modulus=np.exp(log_E),
+                                           tet_poisson_ratio=np.asarray(nu, dtype=np.float64), scatter=scatter,
+                                           use_graph=False, **kw)
+        s = self.solver
+        torch = _torch()
+        dev = s._device
+        V, T, K = s.n_verts, s.n_tets, s.constraints_iter
+        self.V, self.T, self.K = V, T, K
+        f4 = lambda n: torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        self._xs = torch.zeros(((K + 1) * V, 4), dtype=torch.float32, device=dev)
+        self._lams = torch.zeros((max(K, 1) * T, 2), dtype=torch.float32, device=dev)
+        self._xpre, self._v1 = f4(V), f4(V)
+        self._gx, self._gv = f4(V), f4(V)
+        self._w0, self._w1, self._yb, self._dxb = f4(V), f4(V), f4(V), f4(V)
+        self._lamb = torch.zeros((T, 2), dtype=torch.float32, device=dev)
+        self._gmu = torch.zeros(T, dtype=torch.float64, device=dev)
+        self._gla = torch.zeros(T, dtype=torch.float64, device=dev)
+        cnt = np.bincount(s._tets_solver.reshape(-1), minlength=V).astype(np.float32)
+        self._cnt = torch.from_numpy(cnt).to(dev)
+        self._vperm = torch.as_tensor(s._vperm, dtype=torch.int64, device=dev)
+        self._tperm = torch.as_tensor(s._tperm, dtype=torch.int64, device=dev)
+        self.tape = _native.XpbdTape(self._xs.data_ptr(), self._lams.data_ptr(), self._xpre.data_ptr(),
+                                     self._v1.data_ptr())
+        self.adj = _native.XpbdAdjoint(self._gx.data_ptr(), self._gv.data_ptr(), self._gmu.data_ptr(),
+                                       self._gla.data_ptr(), self._w0.data_ptr(), self._w1.data_ptr(),
+                                       self._yb.data_ptr(), self._dxb.data_ptr(), self._lamb.data_ptr(),
+                                       self._cnt.data_ptr())
+        self.initial_rho_hat = s.rho_hat
+
+    def substep_dts(self, frames):
+        s = self.solver
+        out = []
+        for _ in range(frames):
+            for d in frame_chunks(s.frame_dt, s.dt):
+                out.extend([d / s.substeps_num] * s.substeps_num)
+        return out
+
+    # caller order (V, 3) <-> solver order (V, 4) with w = inv_m
+    def set_state(self, x, v):
+        s = self.solver
+        s._x4[:, :3] = x.to(s._x4)[self._vperm]
+        s._v4[:, :3] = v.to(s._v4)[self._vperm]
+
+    def positions(self):
+        s = self.solver
+        out = s._x4.new_empty((self.V, 3))
+        out[self._vperm] = s._x4[:, :3]
+        return out
+
+
+class _Simulate(_torch().autograd.Function):
+    @staticmethod
+    def forward(ctx, x0, v0, log_E, nu, sim, frames):
+        torch = _torch()
+        s = sim.solver
+        lib, stream = s._lib, s._stream()
+        s.set_tet_materials(log_E.detach(), nu.detach())
+        sim.set_state(x0.detach(), v0.detach())
+        s.rho_hat = sim.initial_rho_hat
+        dts = sim.substep_dts(frames)
+        ckpts = []
+        for dt in dts:
+            ckpts.append((s._x4.clone(), s._v4.clone(), s.rho_hat))
+            _native.check(lib.xpbd_substep(s._handle, float(dt), 0, stream))
+        ctx.sim, ctx.dts, ctx.ckpts = sim, dts, ckpts
+        ctx.save_for_backward(log_E, nu)
+        return sim.positions()
+
+    @staticmethod
+    def backward(ctx, g_out):
+        torch = _torch()
+        sim, dts, ckpts = ctx.sim, ctx.dts, ctx.ckpts
+        log_E, nu = ctx.saved_tensors
+        s = sim.solver
+        lib, stream = s._lib, s._stream()
+        sim._gx.zero_()
+        sim._gv.zero_()
+        sim._gx[:, :3] = g_out.to(torch.float32)[sim._vperm]
+        sim._gmu.zero_()
+        sim._gla.zero_()
+        for dt, (x4, v4, rho) in zip(reversed(dts), reversed(ckpts)):
+            s._x4.copy_(x4)
+            s._v4.copy_(v4)
+            s.rho_hat = rho
+            _native.check(lib.xpbd_substep_tape(s._handle, float(dt), sim.tape, stream))
+            _native.check(lib.xpbd_substep_adjoint(s._handle, float(dt), sim.tape, sim.adj, stream))
+        gx = torch.empty((sim.V, 3), dtype=torch.float32, device=g_out.device)
+        gv = torch.empty_like(gx)
+        gx[sim._vperm] = sim._gx[:, :3]
+        gv[sim._vperm] = sim._gv[:, :3]
+        # d/d(1/mu), d/d(1/lambda) (solver tet order) -> d/dlog E, d/dnu (file order)
+        gmu = torch.empty_like(sim._gmu)
+        gla = torch.empty_like(sim._gla)
+        gmu[sim._tperm] = sim._gmu
+        gla[sim._tperm] = sim._gla
+        E = torch.exp(log_E.detach().to(torch.float64))
+        n = nu.detach().to(torch.float64).expand_as(E)
+        inv_mu = 2.0 * (1.0 + n) / E
+        inv_la = (1.0 + n) * (1.0 - 2.0 * n) / (E * n)
+        g_logE = -(gmu * inv_mu + gla * inv_la)
+        g_nu = gmu * 2.0 / E + gla * (-1.0 - 2.0 * n * n) / (n * n * E)
+        if nu.numel() == 1:
+            g_nu = g_nu.sum().reshape(nu.shape)
+        return (gx.to(g_out.dtype), gv.to(g_out.dtype), g_logE.to(log_E.dtype), g_nu.to(nu.dtype), None, None)
+
+
+def xpbd_simulate(sim, x0, v0, log_E, nu, frames):
+    """Final positions (V, 3) after `frames` frames from (x0, v0) with per-tet
+    log E and nu; differentiable w.r.t. all four tensors."""
+    return _Simulate.apply(x0, v0, log_E, nu, sim, frames)

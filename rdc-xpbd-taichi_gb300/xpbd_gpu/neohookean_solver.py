@@ -56,7 +56,7 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
                  cheb_enable=True, cheb_warmup=5, cheb_gamma=0.6666, block_neohookean_enable=False,
                  monitor_convergence=False, *, total_mass=1.0, density=None, gravity=(0.0, -9.8, 0.0),
                  scatter="patch", precise_hydro=None, use_graph=True, reorder=True, sweep_order=1,
-                 patch_pipeline=0, patch_reduce=0):
+                 patch_pipeline=0, patch_reduce=0, tet_young_modulus=None, tet_poisson_ratio=None):
         self.constraints_iter = constraints_iter
         self.hydrostatic_relaxation = hydrostatic_relaxation
         self.deviatoric_relaxation = deviatoric_relaxation
@@ -88,6 +88,15 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         self.sweep_order = int(sweep_order)
         self.patch_pipeline = int(patch_pipeline)
         self.patch_reduce = int(patch_reduce)
+        # per-tet materials (file tet order); they need a per-tet scatter variant
+        self._tet_E = None if tet_young_modulus is None else np.asarray(tet_young_modulus, dtype=np.float64)
+        self._tet_nu = None
+        if self._tet_E is not None:
+            nu_t = poisson_ratio if tet_poisson_ratio is None else tet_poisson_ratio
+            self._tet_nu = np.broadcast_to(np.asarray(nu_t, dtype=np.float64), self._tet_E.shape).copy()
+            if scatter == "patch":
+                scatter = "atomic"
+                self.scatter = scatter
         self.precise_hydro = (poisson_ratio >= 0.49) if precise_hydro is None else bool(precise_hydro)
         self.use_graph = bool(use_graph)
         self.block_size = block_size
@@ -101,6 +110,15 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         self._upload(x, V0, inv_Dm, m, inv_m)
         if self.scatter == "gather":
             self._ensure_gather_buffers()
+        self._tinv_mu = self._tinv_la = None
+        if self._tet_E is not None:
+            torch = _torch()
+            T = self.n_tets
+            if self._tet_E.shape != (T,):
+                raise ValueError("tet_young_modulus must have one entry per tet")
+            self._tinv_mu = torch.empty(T, dtype=torch.float32, device=self._device)
+            self._tinv_la = torch.empty(T, dtype=torch.float32, device=self._device)
+            self.set_tet_materials(np.log(self._tet_E), self._tet_nu)
         if self.scatter == "patch" and not self._ensure_patch_buffers():
             # no patch size keeps every patch within 256 vertices: per-tet variant
             self.scatter = "atomic"
@@ -114,6 +132,21 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         _native.check(self._lib.xpbd_create(prm, body, table, len(self.sdfs), self._max_records,
                                             _native.ctypes.byref(h)))
         self._handle = h.value
+
+    def set_tet_materials(self, log_E, nu):
+        """Per-tet log Young's modulus and Poisson ratio (file tet order; numpy or
+        torch).  Uploads 1/mu and 1/lambda in solver order."""
+        torch = _torch()
+        if self._tinv_mu is None:
+            raise RuntimeError("the solver was built without per-tet materials")
+        le = torch.as_tensor(log_E, dtype=torch.float64, device=self._device).reshape(-1)
+        nu_t = torch.as_tensor(nu, dtype=torch.float64, device=self._device).reshape(-1).expand(le.shape[0])
+        E = torch.exp(le)
+        inv_mu = 2.0 * (1.0 + nu_t) / E
+        inv_la = (1.0 + nu_t) * (1.0 - 2.0 * nu_t) / (E * nu_t)
+        perm = torch.as_tensor(self._tperm, dtype=torch.int64, device=self._device)
+        self._tinv_mu.copy_(inv_mu[perm].to(torch.float32))
+        self._tinv_la.copy_(inv_la[perm].to(torch.float32))
 
     def _records_per_frame(self):
         return len(frame_chunks(self.frame_dt, self.dt)) * self.substeps_num * self.constraints_iter

@@ -346,6 +346,9 @@ class XPBDSolverBase:
         b.dm_a, b.dm_b, b.dm_c = self._dm_a.data_ptr(), self._dm_b.data_ptr(), self._dm_c.data_ptr()
         b.v0 = self._v0.data_ptr()
         b.lam = self._lam.data_ptr()
+        if getattr(self, "_tinv_mu", None) is not None:
+            b.tet_inv_mu = self._tinv_mu.data_ptr()
+            b.tet_inv_lambda = self._tinv_la.data_ptr()
         if self._tet_lid is not None:
             b.n_patches, b.patch_tets = self._n_patches, self._patch_tets
             b.tet_lid = self._tet_lid.data_ptr()
