@@ -113,6 +113,120 @@ def workload_c3(seed=0, n_bodies=256, h=0.03):
     return bodies, sdfs, kw, desc
 
 
+def smooth_field(shape, sigma, rng):
+    """Unit-variance Gaussian random field: Gaussian-filtered white noise on a grid."""
+    from scipy.ndimage import gaussian_filter
+    g = gaussian_filter(rng.normal(size=shape), sigma=sigma, mode="wrap")
+    return (g - g.mean()) / g.std()
+
+
+def workload_c4(seed=0, n=16, sigma=2.0):
+    """16^3 Kuhn cube (edge 1/16 m) above the plane y = 0; per-tet log E = log 1e5 + 0.5 g with g a
+    unit-variance Gaussian field (Gaussian filter of sigma cells on white noise), nu = 0.45."""
+    from xpbd_gpu.mesh import kuhn_grid
+    rng = np.random.default_rng(seed)
+    mesh = kuhn_grid(n, n, n, 1.0 / n, origin=(0.0, 0.3, 0.0), jitter=0.1, seed=seed)
+    g = smooth_field((n, n, n), sigma, rng)
+    cell = g.ravel(order="F")  # cell (i, j, k), i fastest, as the Kuhn tets
+    log_E = np.log(1e5) + 0.5 * np.repeat(cell, 6)
+    specs = [("plane", dict(point=[0.0, 0.0, 0.0], dir=[0.0, 1.0, 0.0], fixed=True))]
+    kw = dict(frame_dt=1.0 / 60, dt=1.0 / 60, substeps_num=5, constraints_iter=20, cheb_enable=True,
+              cheb_warmup=5, cheb_gamma=0.6666, block_neohookean_enable=True, total_mass=1000.0)
+    desc = ("16^3 Kuhn cube (24,576 tets, 4,913 verts), per-tet log E = log 1e5 + 0.5 g (Gaussian field, "
+            "sigma %.1f cells), nu 0.45, 60 frames x 5 substeps x 20 it, MSE of final positions" % sigma)
+    return mesh, specs, kw, log_E, desc
+
+
+def run_c4(args):
+    """Differentiable single body: forward (checkpointed) vs adjoint cost, gradient checks."""
+    import torch
+    from oracle.xpbd_adjoint import DiffOracle, lame_inverse, lame_inverse_grad
+    from oracle.xpbd_oracle import OracleSdf
+    from xpbd_gpu.differentiable import DiffSim, xpbd_simulate
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda")
+    mesh, specs, kw, log_E_target, desc = workload_c4()
+    T = mesh.n_tets
+    frames = args.c4_frames
+    nu = np.full(T, 0.45)
+    sim = DiffSim(mesh, product_sdfs(specs), log_E_target, nu, **kw)
+    x0 = torch.tensor(mesh.points, dtype=torch.float32, device=dev)
+    v0 = torch.zeros_like(x0)
+    with torch.no_grad():
+        x_target = xpbd_simulate(sim, x0, v0, torch.tensor(log_E_target, device=dev),
+                                 torch.tensor(nu, device=dev), frames).clone()
+    le = torch.full((T,), float(np.log(1e5)), dtype=torch.float64, device=dev, requires_grad=True)
+    nu_t = torch.tensor([0.45], dtype=torch.float64, device=dev, requires_grad=True)
+    v0r = v0.clone().requires_grad_(True)
+    fwd, bwd = [], []
+    for k in range(args.c4_reps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        xf = xpbd_simulate(sim, x0, v0r, le, nu_t, frames)
+        loss = ((xf - x_target) ** 2).sum() / xf.shape[0]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        le.grad = None
+        nu_t.grad = None
+        v0r.grad = None
+        loss.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if k > 0:
+            fwd.append(t1 - t0)
+            bwd.append(t2 - t1)
+    fwd_ms, bwd_ms = 1e3 * float(np.mean(fwd)), 1e3 * float(np.mean(bwd))
+    units = T * frames * kw["substeps_num"] * kw["constraints_iter"]
+
+    # gradient check on a short horizon that starts in contact (after c4_check_start
+    # frames of the forward), against the FD-checked float64 adjoint
+    hf = args.c4_check_frames
+    rng = np.random.default_rng(123)
+    le0 = np.log(1e5) + 0.2 * rng.normal(size=T)
+    sim2 = DiffSim(mesh, product_sdfs(specs), le0, nu, **kw)
+    with torch.no_grad():
+        sim2.set_state(x0, v0)
+        x_s = xpbd_simulate(sim2, x0, v0, torch.tensor(le0, device=dev), torch.tensor(nu, device=dev),
+                            args.c4_check_start).clone()
+        v_s = sim2.solver.mesh.verts.v.to_torch().clone()
+    rho0 = sim2.solver.rho_hat
+    sim2.initial_rho_hat = rho0
+    xt = x_s.clone().requires_grad_(True)
+    vt = v_s.clone().requires_grad_(True)
+    let = torch.tensor(le0, dtype=torch.float64, device=dev, requires_grad=True)
+    nut = torch.tensor([0.45], dtype=torch.float64, device=dev, requires_grad=True)
+    c = rng.normal(size=mesh.points.shape)
+    xf = xpbd_simulate(sim2, xt, vt, let, nut, hf)
+    (xf.double() * torch.tensor(c, device=dev)).sum().backward()
+    okw = {k: v for k, v in kw.items() if k != "block_neohookean_enable"}
+    o = DiffOracle(mesh.points, mesh.tets, [OracleSdf(k, **p) for k, p in specs], *lame_inverse(le0, 0.45), **okw)
+    o.rho_hat = rho0
+    _, xb, vb, gm, gl, _ = o.gradient(x_s.cpu().numpy().astype(np.float64), v_s.cpu().numpy().astype(np.float64),
+                                      hf, c)
+    g_le64, g_nu64 = lame_inverse_grad(le0, np.full(T, 0.45), gm, gl)
+    g_le, g_v = let.grad.cpu().numpy(), vt.grad.cpu().numpy()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+    errs = {"log_E": [], "v0": []}
+    for _ in range(32):
+        d = rng.normal(size=T)
+        errs["log_E"].append(abs(float((g_le - g_le64) @ d)) / (np.linalg.norm(g_le64) * np.linalg.norm(d) / np.sqrt(T)))
+        dv = rng.normal(size=mesh.points.shape)
+        errs["v0"].append(abs(float(((g_v - vb) * dv).sum())) / (np.linalg.norm(vb) * np.linalg.norm(dv) / np.sqrt(dv.size)))
+    nu_err = abs(float(nut.grad.cpu().numpy().sum()) - float(g_nu64.sum())) / max(abs(float(g_nu64.sum())), 1e-30)
+    line = {"metric": METRIC, "value": units / (fwd_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.c4_reps,
+            "warmup": 1, "ms_per_step": fwd_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "step": "forward of %d frames with per-substep checkpoints" % frames},
+            "adjoint": {"backward_ms": bwd_ms, "backward_over_forward": bwd_ms / fwd_ms,
+                        "note": "backward = per-substep tape recompute + reverse kernels"},
+            "gradient_check": {"start_frame": args.c4_check_start, "horizon_frames": hf, "directions": 32,
+                               "reference": "float64 adjoint (oracle/xpbd_adjoint.py, itself checked against "
+                                            "central finite differences), started from the GPU state",
+                               "rel_l2_err": {"log_E": rel(g_le, g_le64), "v0": rel(g_v, vb), "nu": nu_err},
+                               "max_directional_err_over_rms": {k: float(np.max(v)) for k, v in errs.items()}}}
+    print(json.dumps(line), flush=True)
+
+
 def relative_residuals(hist, substeps, iters, floor=1e-5):
     """Per body and substep r_hat_K / r_hat_0 from a (bodies, rows, 4) history; NaN where
     r_hat_0 is below `floor` (a free-falling body, residual at FP32 round-off)."""
@@ -520,7 +634,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4"])
+    ap.add_argument("--c4-frames", type=int, default=60)
+    ap.add_argument("--c4-reps", type=int, default=2)
+    ap.add_argument("--c4-check-frames", type=int, default=1)
+    ap.add_argument("--c4-check-start", type=int, default=20)
     ap.add_argument("--scatter", default="patch", choices=["atomic", "gather", "patch"])
     ap.add_argument("--sweep-order", type=int, default=1, choices=[0, 1])
     ap.add_argument("--patch-pipeline", type=int, default=0, choices=[0, 1])
@@ -536,6 +654,8 @@ def main():
         run_profile(args)
     elif args.workload == "c3" and args.impl != "reference":
         run_c3(args)
+    elif args.workload == "c4" and args.impl != "reference":
+        run_c4(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -217,6 +217,11 @@ int xpbd_set_profiling(void* handle, int32_t enable);
  * (arrays of n <= XPBD_K_COUNT); synchronises `stream`; `reset` clears. */
 int xpbd_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, int32_t reset, void* stream);
 
+/* Stream-ordered device-to-device copies of the FP64 rho_hat to / from a
+ * caller's device double (checkpoints of a differentiable forward). */
+int xpbd_save_rho_hat(void* handle, double* dst_device, void* stream);
+int xpbd_load_rho_hat(void* handle, const double* src_device, void* stream);
+
 /* Sticky device error flags (XPBD_OK, XPBD_ERR_NONFINITE or XPBD_ERR_TIMEOUT);
  * synchronises. */
 int xpbd_check_status(void* handle, void* stream);

@@ -1607,6 +1607,20 @@ int xpbd_export_vec3(void* handle, int32_t field, float* dst, void* stream) {
   return XPBD_OK;
 }
 
+int xpbd_save_rho_hat(void* handle, double* dst_device, void* stream) {
+  Solver* s = static_cast<Solver*>(handle);
+  if (!s || !dst_device) return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or destination");
+  XPBD_CUDA(cudaMemcpyAsync(dst_device, &s->d.st->rho_hat, sizeof(double), cudaMemcpyDeviceToDevice, S(stream)));
+  return XPBD_OK;
+}
+
+int xpbd_load_rho_hat(void* handle, const double* src_device, void* stream) {
+  Solver* s = static_cast<Solver*>(handle);
+  if (!s || !src_device) return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or source");
+  XPBD_CUDA(cudaMemcpyAsync(&s->d.st->rho_hat, src_device, sizeof(double), cudaMemcpyDeviceToDevice, S(stream)));
+  return XPBD_OK;
+}
+
 int xpbd_check_status(void* handle, void* stream) {
   Solver* s = static_cast<Solver*>(handle);
   if (!s) return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle");

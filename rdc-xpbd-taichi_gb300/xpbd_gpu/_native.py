@@ -116,6 +116,8 @@ _SIGNATURES = {
     "xpbd_import_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "xpbd_export_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
     "xpbd_check_status": (ctypes.c_int, [_P, _P]),
+    "xpbd_save_rho_hat": (ctypes.c_int, [_P, _P, _P]),
+    "xpbd_load_rho_hat": (ctypes.c_int, [_P, _P, _P]),
     "xpbd_substep_tape": (ctypes.c_int, [_P, ctypes.c_float, ctypes.POINTER(XpbdTape), _P]),
     "xpbd_substep_adjoint": (ctypes.c_int, [_P, ctypes.c_float, ctypes.POINTER(XpbdTape),
                                             ctypes.POINTER(XpbdAdjoint), _P]),

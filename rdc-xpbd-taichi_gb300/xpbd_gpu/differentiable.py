@@ -58,6 +58,15 @@ class DiffSim:
                                        self._cnt.data_ptr())
         self.initial_rho_hat = s.rho_hat
 
+    def rho_copy_to(self, dst):
+        """Stream-ordered copy of the device rho_hat into a 1-element float64 tensor."""
+        s = self.solver
+        _native.check(s._lib.xpbd_save_rho_hat(s._handle, dst.data_ptr(), s._stream()))
+
+    def rho_load_from(self, src):
+        s = self.solver
+        _native.check(s._lib.xpbd_load_rho_hat(s._handle, src.data_ptr(), s._stream()))
+
     def substep_dts(self, frames):
         s = self.solver
         out = []
@@ -90,8 +99,10 @@ class _Simulate(_torch().autograd.Function):
         s.rho_hat = sim.initial_rho_hat
         dts = sim.substep_dts(frames)
         ckpts = []
-        for dt in dts:
-            ckpts.append((s._x4.clone(), s._v4.clone(), s.rho_hat))
+        rho = torch.empty(len(dts), dtype=torch.float64, device=s._device)
+        for k, dt in enumerate(dts):
+            sim.rho_copy_to(rho[k:k + 1])
+            ckpts.append((s._x4.clone(), s._v4.clone(), rho[k:k + 1]))
             _native.check(lib.xpbd_substep(s._handle, float(dt), 0, stream))
         ctx.sim, ctx.dts, ctx.ckpts = sim, dts, ckpts
         ctx.save_for_backward(log_E, nu)
@@ -112,7 +123,7 @@ class _Simulate(_torch().autograd.Function):
         for dt, (x4, v4, rho) in zip(reversed(dts), reversed(ckpts)):
             s._x4.copy_(x4)
             s._v4.copy_(v4)
-            s.rho_hat = rho
+            sim.rho_load_from(rho)
             _native.check(lib.xpbd_substep_tape(s._handle, float(dt), sim.tape, stream))
             _native.check(lib.xpbd_substep_adjoint(s._handle, float(dt), sim.tape, sim.adj, stream))
         gx = torch.empty((sim.V, 3), dtype=torch.float32, device=g_out.device)
