@@ -492,11 +492,12 @@ def run_gb300(args):
 
     mesh, specs, kw, desc = workload(args.workload)
     solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
-                                  patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce, **kw)
+                                  patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce,
+                                  tets_per_thread=args.tets_per_thread, **kw)
     frame_units = tet_iterations_per_frame(mesh, kw)
     n_chunks = len(frame_chunks(kw["frame_dt"], kw["dt"]))
-    per_iter = 3 + (1 if args.scatter == "gather" else 0)
-    launches_per_frame = n_chunks * kw["substeps_num"] * (2 + kw["constraints_iter"] * per_iter)
+    per_substep = 2 + kw["constraints_iter"] * (3 + (1 if args.scatter == "gather" else 0))
+    launches_per_frame = n_chunks * kw["substeps_num"] * per_substep
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
@@ -540,6 +541,7 @@ def run_gb300(args):
         solver.solve()
     prof = solver.read_profile(reset=True)
     solver.set_profiling(False)
+    assert sum(v["launches"] for v in prof.values()) == launches_per_frame * args.profile_steps, prof
 
     # end to end through the public API with pinned host buffers
     x_host = torch.from_numpy(solver.mesh.verts.x.to_numpy()).pin_memory()
@@ -575,12 +577,18 @@ def run_gb300(args):
     proj_bytes = 72.0 * T + 32.0 * V
     proj_ms = prof["project"]["ms"] / max(1, n_proj)
     achieved = proj_bytes / (proj_ms * 1e-3) / 1e9
-    kernel_name = {"patch": "k_project_patch1 (tile, 256-tet patches, red.global.add.v4 per corner)",
+    kernel_name = {"patch": ("k_project_patchN (tile, 256-tet patches, %d consecutive tets per thread, "
+                             "shared corners merged before red.global.add.v4)" % args.tets_per_thread
+                             if args.tets_per_thread > 1 and not args.patch_reduce and not args.patch_pipeline
+                             else "k_project_patch1 (tile, 256-tet patches, red.global.add.v4 per corner)"),
                    "atomic": "k_project (one thread per tet, red.global.add.v4 per corner)",
                    "gather": "k_project (per-corner buffer + deterministic vertex gather)"}[args.scatter]
     # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this
     # workload, from the ncu captures summarised in profiles/k_project_*_c2_64cube.md
-    traffic = {"patch": 89.4e6, "atomic": 115.2e6}.get(args.scatter)
+    # (k_project_patchN for 2 tets per thread, k_project_patch1 for 1)
+    traffic = {("patch", 2): 88.98e6, ("patch", 1): 89.4e6}.get((args.scatter, args.tets_per_thread))
+    if args.scatter == "atomic":
+        traffic = 115.2e6
     if args.patch_pipeline != 0 or args.patch_reduce != 0 or args.workload != "c2":
         traffic = None
     iter_bytes = 136.0 * T + 128.0 * V
@@ -590,7 +598,7 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc, "step": "one frame (%d tet-iterations)" % frame_units,
                    "scatter": args.scatter, "sweep_order": args.sweep_order,
-                   "patch_pipeline": args.patch_pipeline, "l2": "flushed between steps (%d MiB write)" % (L2_FLUSH_BYTES >> 20),
+                   "patch_pipeline": args.patch_pipeline, "tets_per_thread": args.tets_per_thread, "l2": "flushed between steps (%d MiB write)" % (L2_FLUSH_BYTES >> 20),
                    "parallelism": "replicas" if world > 1 else "single GPU", "graph": "one CUDA graph per frame"},
         "frames_per_s": 1e3 / ms_per_step * world,
         "gpu_launches": launches_per_frame * args.steps,
@@ -620,7 +628,7 @@ def run_profile(args):
     mesh, specs, kw, desc = workload(args.workload)
     solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
                                   patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce,
-                                  use_graph=False, **kw)
+                                  tets_per_thread=args.tets_per_thread, use_graph=False, **kw)
     for _ in range(args.profile_frames):
         solver.solve()
     torch.cuda.synchronize()
@@ -643,6 +651,7 @@ def main():
     ap.add_argument("--sweep-order", type=int, default=1, choices=[0, 1])
     ap.add_argument("--patch-pipeline", type=int, default=0, choices=[0, 1])
     ap.add_argument("--patch-reduce", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--tets-per-thread", type=int, default=2, choices=[1, 2, 4])
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-substeps", type=int, default=20)

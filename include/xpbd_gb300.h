@@ -86,6 +86,9 @@ typedef struct xpbd_params {
                                    streaming tet records with cp.async.bulk */
   int32_t patch_reduce;         /* PATCH, pipeline 0: 1 = reduce per patch vertex in shared
                                    memory before the global reduction */
+  int32_t tets_per_thread;      /* PATCH, pipeline 0, reduce 0: 0/1 = one tet per thread;
+                                   2 or 4 = that many consecutive tets per thread, corners
+                                   shared along the chain summed in registers */
   double rho_min, rho_max, rho_beta; /* neohookean_solver.py:66-68 */
 } xpbd_params;
 

@@ -706,6 +706,100 @@ __global__ void __launch_bounds__(kP) k_project_patch1(Dev d, int cur, float cD,
   }
 }
 
+// Tile variant, one CTA per patch, kTPT Morton-consecutive tets per thread.
+// Consecutive tets of a patch usually share a face, so the thread keeps the
+// previous tet's four corner sums in registers: a corner of the next tet that
+// matches one of them is added there, and a held corner the next tet does not
+// touch is flushed with red.global.add.v4.  A chain of kTPT tets sharing s
+// corners per step issues 4 + (kTPT - 1)(4 - s) reductions instead of 4 kTPT.
+template <bool kBlockMode, bool kFirst, bool kPrecise, int kP, int kTPT>
+__global__ void __launch_bounds__(kP / kTPT) k_project_patchN(Dev d, int cur, float cD, float cH, float relax_h,
+                                                             float relax_d) {
+  constexpr int kThreads = kP / kTPT;
+  __shared__ float4 sp[256];
+  __shared__ int sg[256];
+  const int p = blockIdx.x;
+  const int vb = __ldg(d.voff + p);
+  const int nv = __ldg(d.voff + p + 1) - vb;
+  const int t0 = p * kP;
+  const int nt = d.T - t0 < kP ? d.T - t0 : kP;
+  const int l0 = kTPT * threadIdx.x;
+  float4 A[kTPT], B[kTPT];
+  float C[kTPT];
+  uint32_t lid[kTPT];
+  float2 L[kTPT];
+#pragma unroll
+  for (int k = 0; k < kTPT; ++k) {
+    A[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    B[k] = A[k];
+    C[k] = 0.f;
+    lid[k] = 0u;
+    L[k] = make_float2(0.f, 0.f);
+    if (l0 + k < nt) {
+      A[k] = __ldg(d.dm_a + t0 + l0 + k);
+      B[k] = __ldg(d.dm_b + t0 + l0 + k);
+      C[k] = __ldg(d.dm_c + t0 + l0 + k);
+      lid[k] = __ldg(d.lid + t0 + l0 + k);
+      if (!kFirst) L[k] = d.lam[t0 + l0 + k];
+    }
+  }
+  const float4* P = d.p[cur];
+  for (int j = threadIdx.x; j < nv; j += kThreads) {
+    const int g = __ldg(d.pverts + vb + j);
+    sg[j] = g;
+    sp[j] = ldg4(P + g);
+  }
+  __syncthreads();
+  float4 acc[4];
+  int hid[4] = {-1, -1, -1, -1};
+#pragma unroll
+  for (int k = 0; k < kTPT; ++k) {
+    if (l0 + k >= nt) break;
+    Tet tt;
+    tt.dm[0] = A[k].x; tt.dm[1] = A[k].y; tt.dm[2] = A[k].z;
+    tt.dm[3] = A[k].w; tt.dm[4] = B[k].x; tt.dm[5] = B[k].y;
+    tt.dm[6] = B[k].z; tt.dm[7] = B[k].w; tt.dm[8] = C[k];
+    int id[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      id[c] = (int)((lid[k] >> (8 * c)) & 0xffu);
+      tt.p[c] = sp[id[c]];
+    }
+    const float six_det = 6.f * det9(tt.dm);
+    float3 dp[4];
+    float cnt;
+    project_tet<kBlockMode, kPrecise>(tt, six_det * cD, six_det * cH, relax_h, relax_d, L[k], dp, cnt);
+    d.lam[t0 + l0 + k] = L[k];
+    float4 nacc[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) nacc[c] = make_float4(dp[c].x, dp[c].y, dp[c].z, cnt);
+    // Held corners: merge into the matching new corner, or flush.  A tet's
+    // corners are distinct vertices, so a held corner matches at most one.
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      bool used = false;
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (hid[q] == id[c]) {
+          nacc[c].x += acc[q].x;
+          nacc[c].y += acc[q].y;
+          nacc[c].z += acc[q].z;
+          nacc[c].w += acc[q].w;
+          used = true;
+        }
+      if (hid[q] >= 0 && !used) red_add_v4(d.dx + sg[hid[q]], acc[q].x, acc[q].y, acc[q].z, acc[q].w);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      acc[c] = nacc[c];
+      hid[c] = id[c];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (hid[q] >= 0) red_add_v4(d.dx + sg[hid[q]], acc[q].x, acc[q].y, acc[q].z, acc[q].w);
+}
+
 template <bool kRes, bool kMon, bool kPrecise, int kP>
 __global__ void __launch_bounds__(kP) k_residual_patch1(Dev d, SweepArgs a) {
   __shared__ float4 sp[256];
@@ -743,6 +837,61 @@ __global__ void __launch_bounds__(kP) k_residual_patch1(Dev d, SweepArgs a) {
       tt.p[3] = sp[lid >> 24];
       const float six_det = 6.f * det9(tt.dm);
       residual_terms<kRes, kMon, kPrecise>(tt, L, six_det * a.cD, six_det * a.cH, sr, sh, sd);
+    }
+  }
+  finish_residual<kRes, kMon>(d, a, sr, sh, sd);
+}
+
+// Residual over patches with kTPT consecutive tets per thread (one CTA per
+// patch at a time, kP / kTPT threads).  Loading the patch's records before
+// the vertex tile lets both sets of loads be in flight together.
+template <bool kRes, bool kMon, bool kPrecise, int kP, int kTPT>
+__global__ void __launch_bounds__(kP / kTPT) k_residual_patchN(Dev d, SweepArgs a) {
+  constexpr int kThreads = kP / kTPT;
+  __shared__ float4 sp[256];
+  float sr = 0.f, sh = 0.f, sd = 0.f;
+  const float4* P = d.p[a.cur];
+  const int n = d.n_patches;
+  const int l0 = kTPT * threadIdx.x;
+  for (int q = blockIdx.x; q < n; q += gridDim.x) {
+    const int p = a.reverse ? n - 1 - q : q;
+    const int vb = __ldg(d.voff + p);
+    const int nv = __ldg(d.voff + p + 1) - vb;
+    const int t0 = p * kP + l0;
+    float4 A[kTPT], B[kTPT];
+    float C[kTPT];
+    uint32_t lid[kTPT];
+    float2 L[kTPT];
+#pragma unroll
+    for (int k = 0; k < kTPT; ++k) {
+      if (t0 + k < d.T) {
+        A[k] = __ldg(d.dm_a + t0 + k);
+        B[k] = __ldg(d.dm_b + t0 + k);
+        C[k] = __ldg(d.dm_c + t0 + k);
+        lid[k] = __ldg(d.lid + t0 + k);
+        L[k] = kRes ? d.lam[t0 + k] : make_float2(0.f, 0.f);
+      }
+    }
+    __syncthreads();  // the previous patch's readers are done with sp
+    for (int j = threadIdx.x; j < nv; j += kThreads) {
+      const int g = __ldg(d.pverts + vb + j);
+      const float3 x = post_position(ldg4(P + g), ldg4(d.dx + g));
+      sp[j] = make_float4(x.x, x.y, x.z, 0.f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kTPT; ++k) {
+      if (t0 + k >= d.T) break;
+      Tet tt;
+      tt.dm[0] = A[k].x; tt.dm[1] = A[k].y; tt.dm[2] = A[k].z;
+      tt.dm[3] = A[k].w; tt.dm[4] = B[k].x; tt.dm[5] = B[k].y;
+      tt.dm[6] = B[k].z; tt.dm[7] = B[k].w; tt.dm[8] = C[k];
+      tt.p[0] = sp[lid[k] & 0xffu];
+      tt.p[1] = sp[(lid[k] >> 8) & 0xffu];
+      tt.p[2] = sp[(lid[k] >> 16) & 0xffu];
+      tt.p[3] = sp[lid[k] >> 24];
+      const float six_det = 6.f * det9(tt.dm);
+      residual_terms<kRes, kMon, kPrecise>(tt, L[k], six_det * a.cD, six_det * a.cH, sr, sh, sd);
     }
   }
   finish_residual<kRes, kMon>(d, a, sr, sh, sd);
@@ -959,6 +1108,7 @@ struct Solver {
   int res_grid = 0;        // grid of the grid-stride residual kernels
   int patch_grid = 0;      // grid of the persistent tile kernels
   int patch1_grid = 0;     // grid of the one-CTA-per-patch residual
+  int patchN_grid = 0;     // grid of the two-tets-per-thread residual
   int tile_res_grid = 0;   // grid of the pipelined tile residual
   int max_records = 0;
   int cur = 0;  // buffer holding the current predicted positions
@@ -1008,6 +1158,8 @@ int check_params(const xpbd_params* p) {
   if (p->constraints_iter < 0) return fail(XPBD_ERR_INVALID_ARGUMENT, "constraints_iter < 0");
   if (p->scatter != XPBD_SCATTER_ATOMIC && p->scatter != XPBD_SCATTER_GATHER && p->scatter != XPBD_SCATTER_PATCH)
     return fail(XPBD_ERR_INVALID_ARGUMENT, "unknown scatter variant");
+  if (p->tets_per_thread != 0 && p->tets_per_thread != 1 && p->tets_per_thread != 2 && p->tets_per_thread != 4)
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "tets_per_thread must be 0, 1, 2 or 4");
   if (!(p->lame_mu != 0.f) || !(p->lame_lambda != 0.f))
     return fail(XPBD_ERR_INVALID_ARGUMENT, "Lame parameters must be non-zero");
   return XPBD_OK;
@@ -1043,6 +1195,12 @@ void launch_project_patch_p(Solver* s, float cD, float cH, cudaStream_t st) {
   if (p.patch_pipeline == 1 && kP == 256) {
     const int g = s->d.n_patches < s->patch_grid ? s->d.n_patches : s->patch_grid;
     k_project_tile<kBlockMode, kFirst, kPrecise><<<g, 256, sizeof(TileSmem<false>), st>>>(
+        s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
+  } else if (p.tets_per_thread == 2 && !p.patch_reduce) {
+    k_project_patchN<kBlockMode, kFirst, kPrecise, kP, 2><<<s->d.n_patches, kP / 2, 0, st>>>(
+        s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
+  } else if (p.tets_per_thread == 4 && !p.patch_reduce) {
+    k_project_patchN<kBlockMode, kFirst, kPrecise, kP, 4><<<s->d.n_patches, kP / 4, 0, st>>>(
         s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
   } else {
     if (p.patch_reduce)
@@ -1101,6 +1259,9 @@ void launch_residual_patch_p(Solver* s, const SweepArgs& a, cudaStream_t st) {
   if (s->prm.patch_pipeline == 1 && kP == 256) {
     const int g = n < s->tile_res_grid ? n : s->tile_res_grid;
     k_residual_tile<kRes, kMon, kPrecise><<<g, 256, sizeof(TileSmem<true>), st>>>(s->d, a);
+  } else if (s->prm.tets_per_thread == 2 && !s->prm.patch_reduce) {
+    const int g = n < s->patchN_grid ? n : s->patchN_grid;
+    k_residual_patchN<kRes, kMon, kPrecise, kP, 2><<<g, kP / 2, 0, st>>>(s->d, a);
   } else {
     const int g = n < s->patch1_grid ? n : s->patch1_grid;
     k_residual_patch1<kRes, kMon, kPrecise, kP><<<g, kP, 0, st>>>(s->d, a);
@@ -1127,6 +1288,32 @@ void launch_residual_t(Solver* s, const SweepArgs& a, int grid, cudaStream_t st)
   else k_residual<kRes, kMon, false><<<grid, kBlock, 0, st>>>(s->d, a);
 }
 
+SweepArgs sweep_args(Solver* s, int it, float dt, int rec) {
+  const xpbd_params& p = s->prm;
+  SweepArgs a;
+  a.cur = s->cur;
+  compliance_factors(s, dt, a.cD, a.cH);
+  a.it = it;
+  a.warmup = p.cheb_warmup;
+  a.rec = rec;
+  a.reverse = p.sweep_order == 1 ? 1 : 0;
+  a.rho_min = p.rho_min;
+  a.rho_max = p.rho_max;
+  a.rho_beta = p.rho_beta;
+  return a;
+}
+
+void launch_residual(Solver* s, const SweepArgs& a, cudaStream_t st) {
+  const bool cheb = s->prm.cheb_enable != 0, mon = s->prm.monitor != 0;
+  int grid = blocks_for(s->d.T);
+  if (grid > s->res_grid) grid = s->res_grid;
+  if (grid < 1) grid = 1;
+  Prof prof(s, XPBD_K_RESIDUAL, st);
+  if (cheb && mon) launch_residual_t<true, true>(s, a, grid, st);
+  else if (cheb) launch_residual_t<true, false>(s, a, grid, st);
+  else launch_residual_t<false, true>(s, a, grid, st);
+}
+
 // One Jacobi iteration (neohookean_solver.py:474-556).
 void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
   const xpbd_params& p = s->prm;
@@ -1136,25 +1323,7 @@ void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
     k_gather<<<blocks_for(s->d.V), kBlock, 0, st>>>(s->d);
   }
   const bool cheb = p.cheb_enable != 0, mon = p.monitor != 0;
-  if (cheb || mon) {
-    SweepArgs a;
-    a.cur = s->cur;
-    compliance_factors(s, dt, a.cD, a.cH);
-    a.it = it;
-    a.warmup = p.cheb_warmup;
-    a.rec = rec;
-    a.reverse = p.sweep_order == 1 ? 1 : 0;
-    a.rho_min = p.rho_min;
-    a.rho_max = p.rho_max;
-    a.rho_beta = p.rho_beta;
-    int grid = blocks_for(s->d.T);
-    if (grid > s->res_grid) grid = s->res_grid;
-    if (grid < 1) grid = 1;
-    Prof prof(s, XPBD_K_RESIDUAL, st);
-    if (cheb && mon) launch_residual_t<true, true>(s, a, grid, st);
-    else if (cheb) launch_residual_t<true, false>(s, a, grid, st);
-    else launch_residual_t<false, true>(s, a, grid, st);
-  }
+  if (cheb || mon) launch_residual(s, sweep_args(s, it, dt, rec), st);
   const int g = blocks_for(s->d.V);
   const bool reset = p.scatter != XPBD_SCATTER_GATHER;
   Prof prof(s, XPBD_K_UPDATE, st);
@@ -1173,12 +1342,16 @@ void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
   }
 }
 
+void launch_iterations(Solver* s, int K, float dt, int record_base, cudaStream_t st) {
+  for (int it = 0; it < K; ++it) launch_iteration(s, it, dt, record_base >= 0 ? record_base + it : -1, st);
+}
+
 int do_solve_step(Solver* s, float dt, int record_base, cudaStream_t st) {
   const int K = s->prm.constraints_iter;
   if (record_base >= 0 && record_base + K > s->max_records)
     return fail(XPBD_ERR_HISTORY_FULL, "history holds " + std::to_string(s->max_records) + " records");
   launch_begin(s, false, true, dt, st);
-  for (int it = 0; it < K; ++it) launch_iteration(s, it, dt, record_base >= 0 ? record_base + it : -1, st);
+  launch_iterations(s, K, dt, record_base, st);
   return XPBD_OK;
 }
 
@@ -1188,7 +1361,7 @@ int do_substep(Solver* s, float dt, int record_base, cudaStream_t st) {
     return fail(XPBD_ERR_HISTORY_FULL, "history holds " + std::to_string(s->max_records) + " records");
   s->cur = 0;
   launch_begin(s, true, true, dt, st);
-  for (int it = 0; it < K; ++it) launch_iteration(s, it, dt, record_base >= 0 ? record_base + it : -1, st);
+  launch_iterations(s, K, dt, record_base, st);
   {
     Prof prof(s, XPBD_K_END, st);
     k_end<<<blocks_for(s->d.V), kBlock, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
@@ -1369,6 +1542,12 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
         bps < 1)
       bps = 2;
     s->patch1_grid = s->sm_count * bps;
+    bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &bps, k_residual_patchN<true, false, true, 256, 2>, 128, 0) != cudaSuccess ||
+        bps < 1)
+      bps = 4;
+    s->patchN_grid = s->sm_count * bps;
   }
   DevState h{};
   h.rho_hat = 0.999;  // neohookean_solver.py:65

@@ -53,7 +53,7 @@ class XpbdParams(ctypes.Structure):
                 ("monitor", ctypes.c_int32), ("precise_hydro", ctypes.c_int32),
                 ("scatter", ctypes.c_int32), ("use_graph", ctypes.c_int32),
                 ("sweep_order", ctypes.c_int32), ("patch_pipeline", ctypes.c_int32),
-                ("patch_reduce", ctypes.c_int32),
+                ("patch_reduce", ctypes.c_int32), ("tets_per_thread", ctypes.c_int32),
                 ("rho_min", ctypes.c_double), ("rho_max", ctypes.c_double),
                 ("rho_beta", ctypes.c_double)]
 

@@ -56,7 +56,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
                  cheb_enable=True, cheb_warmup=5, cheb_gamma=0.6666, block_neohookean_enable=False,
                  monitor_convergence=False, *, total_mass=1.0, density=None, gravity=(0.0, -9.8, 0.0),
                  scatter="patch", precise_hydro=None, use_graph=True, reorder=True, sweep_order=1,
-                 patch_pipeline=0, patch_reduce=0, tet_young_modulus=None, tet_poisson_ratio=None):
+                 patch_pipeline=0, patch_reduce=0, tets_per_thread=2, tet_young_modulus=None,
+                 tet_poisson_ratio=None):
         self.constraints_iter = constraints_iter
         self.hydrostatic_relaxation = hydrostatic_relaxation
         self.deviatoric_relaxation = deviatoric_relaxation
@@ -88,6 +89,7 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         self.sweep_order = int(sweep_order)
         self.patch_pipeline = int(patch_pipeline)
         self.patch_reduce = int(patch_reduce)
+        self.tets_per_thread = int(tets_per_thread)
         # per-tet materials (file tet order); they need a per-tet scatter variant
         self._tet_E = None if tet_young_modulus is None else np.asarray(tet_young_modulus, dtype=np.float64)
         self._tet_nu = None
@@ -171,6 +173,7 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         p.sweep_order = self.sweep_order
         p.patch_pipeline = self.patch_pipeline
         p.patch_reduce = self.patch_reduce
+        p.tets_per_thread = self.tets_per_thread
         p.rho_min, p.rho_max, p.rho_beta = self.rho_min, self.rho_max, self.rho_beta
         return p
 

@@ -49,6 +49,11 @@ def test_no_sdf_raises_value_error():
         XPBDNeoHookeanSolver(rest_pose=(d["points"], d["tets"]), sdf=None)
 
 
+def test_bad_tets_per_thread_is_rejected():
+    with pytest.raises(RuntimeError, match="tets_per_thread"):
+        _solver(tets_per_thread=3)
+
+
 def test_rho_hat_persists_across_frames_and_is_settable():
     _, s = _solver(monitor_convergence=False)
     assert abs(s.rho_hat - 0.999) < 1e-15

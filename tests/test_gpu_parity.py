@@ -29,13 +29,18 @@ def make_solver(d, **over):
 
 
 @pytest.mark.parametrize("name", gc.golden_names())
-@pytest.mark.parametrize("scatter", ["atomic", "gather", "patch", "patch-tma", "patch-reduce"])
+@pytest.mark.parametrize("scatter", ["atomic", "gather", "patch", "patch-tma", "patch-reduce", "patch-1tpt",
+                                     "patch-4tpt"])
 def test_frames_match_reference(name, scatter):
     d = gc.load(name)
     if scatter == "patch-tma":
         s = make_solver(d, scatter="patch", patch_pipeline=1, monitor_convergence=False)
     elif scatter == "patch-reduce":
         s = make_solver(d, scatter="patch", patch_reduce=1, monitor_convergence=False)
+    elif scatter == "patch-1tpt":
+        s = make_solver(d, scatter="patch", tets_per_thread=1, monitor_convergence=False)
+    elif scatter == "patch-4tpt":
+        s = make_solver(d, scatter="patch", tets_per_thread=4, monitor_convergence=False)
     else:
         s = make_solver(d, scatter=scatter, monitor_convergence=False)
     diag = gc.bbox_diag(d["x_init"])
@@ -59,10 +64,13 @@ def test_frames_match_reference(name, scatter):
 
 
 @pytest.mark.parametrize("name", ["kuhn2_block_cheb", "kuhn2_split_nocheb", "kuhn3_block_cheb_nu049"])
-@pytest.mark.parametrize("scatter", ["atomic", "patch"])
+@pytest.mark.parametrize("scatter", ["atomic", "patch", "patch-1tpt"])
 def test_monitoring_records_match_reference(name, scatter):
     d = gc.load(name)
-    s = make_solver(d, monitor_convergence=True, scatter=scatter)
+    if scatter == "patch-1tpt":
+        s = make_solver(d, monitor_convergence=True, scatter="patch", tets_per_thread=1)
+    else:
+        s = make_solver(d, monitor_convergence=True, scatter=scatter)
     seen = []
     s.convergence_callback = lambda frame, substep, recs: seen.append((frame, substep, len(recs)))
     for _ in range(int(d["frames"])):
@@ -142,3 +150,4 @@ def test_one_frame_against_f32_oracle_larger_grid(scatter):
         s.solve()
         err = np.abs(s.mesh.verts.x.to_numpy() - o.x).max()
         assert err <= POS_TOL * diag, "frame %d: %.3e" % (f, err)
+
