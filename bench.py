@@ -246,13 +246,13 @@ def run_c3(args):
     torch.cuda.set_device(0)
     bodies, specs, kw, desc = workload_c3()
     units = sum(b.rest_pose.n_tets for b in bodies) * kw["substeps_num"] * kw["constraints_iter"]
-    batch = XPBDBatchedSolver(bodies, product_sdfs(specs), **kw)
+    batch = XPBDBatchedSolver(bodies, product_sdfs(specs), tets_per_thread=min(args.tets_per_thread, 2), **kw)
     plain = []
     for b in bodies:
         mesh = TetMesh(b.rest_pose.points @ b.rotation.T, b.rest_pose.tets)
         plain.append(XPBDNeoHookeanSolver(mesh, product_sdfs(specs), young_modulus=b.young_modulus,
                                           poisson_ratio=b.poisson_ratio, offset=b.offset, density=b.density,
-                                          scatter="patch", **kw))
+                                          scatter="patch", tets_per_thread=args.tets_per_thread, **kw))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
@@ -533,7 +533,8 @@ def run_gb300(args):
     value = frame_units * args.steps * world / (total_ms * 1e-3)
     solver.check_status()
 
-    # per-kernel durations: the same frames with direct launches bracketed by events
+    # per-kernel durations: the same frames, each launch bracketed by events (event record
+    # nodes in the frame graph)
     solver.set_profiling(True)
     solver.read_profile(reset=True)
     for _ in range(args.profile_steps):
@@ -605,7 +606,10 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "kernel": kernel_name,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "traffic": traffic,
-                     "bytes_per_launch": proj_bytes, "ms_per_launch": proj_ms},
+                     "bytes_per_launch": proj_bytes, "ms_per_launch": proj_ms,
+                     "timing": "CUDA events recorded by event nodes inside the frame graph (the timed "
+                               "region's graph plus those nodes), %d frames after the timed region"
+                               % args.profile_steps},
         "iteration_roofline": {"bytes_per_iteration": iter_bytes,
                                "achieved_GBps": iter_bytes * K * n_chunks * kw["substeps_num"] / (ms_per_step * 1e-3) / 1e9,
                                "frac": iter_bytes * K * n_chunks * kw["substeps_num"] / (ms_per_step * 1e-3) / 1e9 / peak},
@@ -625,6 +629,17 @@ def run_profile(args):
     """Frames with direct launches and no timing, for an external profiler."""
     import torch
     from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
+    if args.workload == "c3":  # the batched form alone
+        from xpbd_gpu.batched import XPBDBatchedSolver
+        bodies, specs, kw, desc = workload_c3()
+        batch = XPBDBatchedSolver(bodies, product_sdfs(specs), tets_per_thread=min(args.tets_per_thread, 2),
+                                  use_graph=False, **kw)
+        for _ in range(args.profile_frames):
+            batch.solve()
+        torch.cuda.synchronize()
+        batch.check_status()
+        print("profile mode: %d frame(s) of %s (batched)" % (args.profile_frames, desc))
+        return
     mesh, specs, kw, desc = workload(args.workload)
     solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
                                   patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce,

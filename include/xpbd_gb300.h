@@ -211,8 +211,10 @@ enum xpbd_kernel_class {
 };
 
 /* Profiling: with `enable`, every kernel launch is bracketed by CUDA events
- * on its stream and xpbd_solve launches directly instead of replaying its
- * graph.  (The reference's counterpart is the host perf_counter brackets of
+ * on its stream.  With use_graph, xpbd_solve replays a frame graph that
+ * carries those events as event record nodes, and waits for the previous
+ * profiled replay before launching the next; without it the launches are
+ * direct.  (The reference's counterpart is the host perf_counter brackets of
  * solve_step, neohookean_solver.py:454-560.) */
 int xpbd_set_profiling(void* handle, int32_t enable);
 

@@ -68,9 +68,6 @@ struct BDev {
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
-__device__ __forceinline__ float det9(const float m[9]) {
-  return m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) + m[6] * (m[1] * m[5] - m[4] * m[2]);
-}
 
 __device__ __forceinline__ float3 post_position(const float4 p, const float4 D) {
   float3 r = make_float3(p.x, p.y, p.z);
@@ -121,10 +118,12 @@ __global__ void __launch_bounds__(256) kb_end(BDev d, int cur, float dt, float d
   d.x[i] = make_float4(pi.x, pi.y, pi.z, xi.w);
 }
 
-// Projection, one CTA per patch (the single-body tile kernel with per-body
-// compliance 1 / (mu_b dt^2), 1 / (lambda_b dt^2)).
-template <bool kBlockMode, bool kFirst, bool kPrecise>
-__global__ void __launch_bounds__(kP) kb_project(BDev d, int cur, float inv_dt2, float relax_h, float relax_d) {
+// Projection, one CTA of kP / kTPT threads per patch (the single-body tile
+// kernel with per-body compliance 1 / (mu_b dt^2), 1 / (lambda_b dt^2)); each
+// thread projects kTPT consecutive tets (project_chain).
+template <bool kBlockMode, bool kFirst, bool kPrecise, int kTPT>
+__global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_project(BDev d, int cur, float inv_dt2, float relax_h, float relax_d) {
+  constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
   __shared__ int sg[256];
   const int p = blockIdx.x;
@@ -132,38 +131,39 @@ __global__ void __launch_bounds__(kP) kb_project(BDev d, int cur, float inv_dt2,
   const int vb = __ldg(d.voff + p);
   const int nv = __ldg(d.voff + p + 1) - vb;
   const int nt = __ldg(d.patch_ntets + p);
-  const int t = p * kP + threadIdx.x;
-  const bool has = threadIdx.x < nt;
-  Tet tt;
-  uint32_t lid = 0;
-  float2 L = make_float2(0.f, 0.f);
-  if (has) {
-    const float4 A = __ldg(d.dm_a + t), B = __ldg(d.dm_b + t);
-    tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
-    tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
-    tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
-    lid = __ldg(d.lid + t);
-    if (!kFirst) L = d.lam[t];
+  const int l0 = kTPT * threadIdx.x;
+  const int t0 = p * kP + l0;
+  float4 A[kTPT], B[kTPT];
+  float C[kTPT];
+  uint32_t lid[kTPT];
+  float2 L[kTPT];
+#pragma unroll
+  for (int k = 0; k < kTPT; ++k) {
+    A[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    B[k] = A[k];
+    C[k] = 0.f;
+    lid[k] = 0u;
+    L[k] = make_float2(0.f, 0.f);
+    if (l0 + k < nt) {
+      A[k] = __ldg(d.dm_a + t0 + k);
+      B[k] = __ldg(d.dm_b + t0 + k);
+      C[k] = __ldg(d.dm_c + t0 + k);
+      lid[k] = __ldg(d.lid + t0 + k);
+      if (!kFirst) L[k] = d.lam[t0 + k];
+    }
   }
   const float4* P = d.p[cur];
-  for (int j = threadIdx.x; j < nv; j += kP) {
+  for (int j = threadIdx.x; j < nv; j += kThreads) {
     const int g = __ldg(d.pverts + vb + j);
     sg[j] = g;
     sp[j] = ldg4(P + g);
   }
   __syncthreads();
-  if (!has) return;
+  const int n = nt - l0 < kTPT ? nt - l0 : kTPT;
+  if (n <= 0) return;
   const float cD = __ldg(d.inv_mu + b) * inv_dt2, cH = __ldg(d.inv_la + b) * inv_dt2;
-  const int l[4] = {(int)(lid & 0xffu), (int)((lid >> 8) & 0xffu), (int)((lid >> 16) & 0xffu), (int)(lid >> 24)};
-#pragma unroll
-  for (int c = 0; c < 4; ++c) tt.p[c] = sp[l[c]];
-  const float six_det = 6.f * det9(tt.dm);
-  float3 dp[4];
-  float cnt;
-  project_tet<kBlockMode, kPrecise>(tt, six_det * cD, six_det * cH, relax_h, relax_d, L, dp, cnt);
-  d.lam[t] = L;
-#pragma unroll
-  for (int c = 0; c < 4; ++c) red_add_v4(d.dx + sg[l[c]], dp[c].x, dp[c].y, dp[c].z, cnt);
+  project_chain<kBlockMode, kPrecise, kTPT>(A, B, C, lid, L, d.lam + t0, n, sp, sg, d.dx, cD, cH, relax_h,
+                                            relax_d);
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -183,9 +183,9 @@ struct BSweep {
 // accumulators; the CTA that completes the body's patch count applies the
 // rho_hat / omega recurrence (neohookean_solver.py:495-504, :537-546) and
 // writes the body's history row.  All threads of the CTA call it.
-template <bool kRes, bool kMon>
+template <bool kRes, bool kMon, int kWarps>
 __device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int b, int npatch, float sr, float sh,
-                                           float sd, double (*red)[kP / 32]) {
+                                           float sd, double (*red)[kWarps]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const double r0 = warp_sum((double)sr), r1 = warp_sum((double)sh), r2 = warp_sum((double)sd);
   __syncthreads();  // red[] of the previous flush has been consumed
@@ -197,7 +197,7 @@ __device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int b
   __syncthreads();
   if (threadIdx.x != 0) return;
   double b0 = 0.0, b1 = 0.0, b2 = 0.0;
-  for (int k = 0; k < kP / 32; ++k) {
+  for (int k = 0; k < kWarps; ++k) {
     b0 += red[0][k];
     b1 += red[1][k];
     b2 += red[2][k];
@@ -249,13 +249,15 @@ __device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int b
 // Residual (neohookean_solver.py:298-329) and monitoring sums (:256-296).
 // Each CTA walks a contiguous run of `chunk` patches (patches are ordered by
 // body) and flushes its partial sums whenever the body changes.
-template <bool kRes, bool kMon, bool kPrecise>
-__global__ void __launch_bounds__(kP) kb_residual(BDev d, BSweep a, int chunk) {
+template <bool kRes, bool kMon, bool kPrecise, int kTPT>
+__global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int chunk) {
+  constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
-  __shared__ double red[3][kP / 32];
+  __shared__ double red[3][kThreads / 32];
   const int c0 = blockIdx.x * chunk;
   const int c1 = c0 + chunk < d.n_patches ? c0 + chunk : d.n_patches;
   const float4* P = d.p[a.cur];
+  const int l0 = kTPT * threadIdx.x;
   float sr = 0.f, sh = 0.f, sd = 0.f;
   int run = 0;
   for (int p = c0; p < c1; ++p) {
@@ -263,40 +265,48 @@ __global__ void __launch_bounds__(kP) kb_residual(BDev d, BSweep a, int chunk) {
     const int vb = __ldg(d.voff + p);
     const int nv = __ldg(d.voff + p + 1) - vb;
     const int nt = __ldg(d.patch_ntets + p);
-    const int t = p * kP + threadIdx.x;
-    const bool has = threadIdx.x < nt;
-    Tet tt;
-    uint32_t lid = 0;
-    float2 L = make_float2(0.f, 0.f);
-    if (has) {
-      const float4 A = __ldg(d.dm_a + t), B = __ldg(d.dm_b + t);
-      tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
-      tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
-      tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
-      lid = __ldg(d.lid + t);
-      if (kRes) L = d.lam[t];
+    const int t0 = p * kP + l0;
+    float4 A[kTPT], B[kTPT];
+    float C[kTPT];
+    uint32_t lid[kTPT];
+    float2 L[kTPT];
+#pragma unroll
+    for (int k = 0; k < kTPT; ++k) {
+      if (l0 + k < nt) {
+        A[k] = __ldg(d.dm_a + t0 + k);
+        B[k] = __ldg(d.dm_b + t0 + k);
+        C[k] = __ldg(d.dm_c + t0 + k);
+        lid[k] = __ldg(d.lid + t0 + k);
+        L[k] = kRes ? d.lam[t0 + k] : make_float2(0.f, 0.f);
+      }
     }
     __syncthreads();  // the previous patch's readers are done with sp
-    for (int j = threadIdx.x; j < nv; j += kP) {
+    for (int j = threadIdx.x; j < nv; j += kThreads) {
       const int g = __ldg(d.pverts + vb + j);
       const float3 x = post_position(ldg4(P + g), ldg4(d.dx + g));
       sp[j] = make_float4(x.x, x.y, x.z, 0.f);
     }
     __syncthreads();
-    if (has) {
-      tt.p[0] = sp[lid & 0xffu];
-      tt.p[1] = sp[(lid >> 8) & 0xffu];
-      tt.p[2] = sp[(lid >> 16) & 0xffu];
-      tt.p[3] = sp[lid >> 24];
+    const float aDs = kRes ? __ldg(d.inv_mu + b) * a.inv_dt2 : 0.f;
+    const float aHs = kRes ? __ldg(d.inv_la + b) * a.inv_dt2 : 0.f;
+#pragma unroll
+    for (int k = 0; k < kTPT; ++k) {
+      if (l0 + k >= nt) break;
+      Tet tt;
+      tt.dm[0] = A[k].x; tt.dm[1] = A[k].y; tt.dm[2] = A[k].z;
+      tt.dm[3] = A[k].w; tt.dm[4] = B[k].x; tt.dm[5] = B[k].y;
+      tt.dm[6] = B[k].z; tt.dm[7] = B[k].w; tt.dm[8] = C[k];
+      tt.p[0] = sp[lid[k] & 0xffu];
+      tt.p[1] = sp[(lid[k] >> 8) & 0xffu];
+      tt.p[2] = sp[(lid[k] >> 16) & 0xffu];
+      tt.p[3] = sp[lid[k] >> 24];
       float F[9];
       deformation_gradient(tt, F);
       float C_D, C_H;
       invariants<kPrecise>(F, C_D, C_H);
       if (kRes) {
         const float six_det = 6.f * det9(tt.dm);
-        const float aD = six_det * __ldg(d.inv_mu + b) * a.inv_dt2;
-        const float aH = six_det * __ldg(d.inv_la + b) * a.inv_dt2;
-        const float rD = C_D + aD * L.x, rH = C_H + aH * L.y;
+        const float rD = C_D + six_det * aDs * L[k].x, rH = C_H + six_det * aHs * L[k].y;
         sr += sqrtf(rD * rD + rH * rH);
       }
       if (kMon) {
@@ -306,7 +316,7 @@ __global__ void __launch_bounds__(kP) kb_residual(BDev d, BSweep a, int chunk) {
     }
     ++run;
     if (p + 1 == c1 || __ldg(d.patch_body + p + 1) != b) {
-      flush_body<kRes, kMon>(d, a, b, run, sr, sh, sd, red);
+      flush_body<kRes, kMon, kThreads / 32>(d, a, b, run, sr, sh, sd, red);
       sr = sh = sd = 0.f;
       run = 0;
     }
@@ -318,13 +328,19 @@ template <bool kCheb, bool kFirstIt>
 __global__ void __launch_bounds__(256) kb_update(BDev d, int cur, float gamma) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.V) return;
+  // every load is issued before the first store: as far as the compiler
+  // knows the buffers may alias, so a load after a store would wait for it
   const float4 pc = d.p[cur][i];
   const float4 D = d.dx[i];
+  float4 yp = pc;
+  float om = 1.f;
+  if (kCheb) {
+    if (!kFirstIt) yp = d.p[cur ^ 1][i];
+    om = (float)d.bs[__ldg(d.vblock_body + blockIdx.x)].omega;
+  }
   d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   const float3 xp = post_position(pc, D);
   if (kCheb) {
-    const float om = (float)d.bs[__ldg(d.vblock_body + blockIdx.x)].omega;
-    const float4 yp = kFirstIt ? pc : d.p[cur ^ 1][i];
     const float nx = gamma * (xp.x - pc.x) + pc.x;
     const float ny = gamma * (xp.y - pc.y) + pc.y;
     const float nz = gamma * (xp.z - pc.z) + pc.z;
@@ -397,14 +413,19 @@ int bfail(int st, const std::string& m) {
   return st;
 }
 
-#define B_CUDA(call)                                                                               \
-  do {                                                                                             \
-    cudaError_t e_ = (call);                                                                       \
-    if (e_ != cudaSuccess) return bfail(XPBD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+// On failure the runtime's per-thread last error is cleared as well.
+#define B_CUDA(call)                                                                \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      cudaGetLastError();                                                           \
+      return bfail(XPBD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    }                                                                               \
   } while (0)
 
 struct Batch {
-  int res_ctas = 1;  // CTAs of the residual sweep (resident CTAs of the GPU)
+  int res_ctas = 1;   // CTAs of the residual sweep (resident CTAs of the GPU)
+  int res_ctas2 = 1;  // the same for the two-tets-per-thread residual
   xpbd_params prm{};
   BDev d{};
   int cur = 0;
@@ -449,23 +470,39 @@ struct BProf {
   }
 };
 
+// tets per thread of the batched tile kernels: 1, or 2 (params 2 and 4)
+inline int batch_tpt(const xpbd_params& p) { return p.tets_per_thread >= 2 ? 2 : 1; }
+
+template <bool kBlock, bool kFirst, int kTPT>
+void project_bt(Batch* s, float inv_dt2, cudaStream_t st) {
+  const xpbd_params& p = s->prm;
+  const float rh = p.hydrostatic_relaxation, rd = p.deviatoric_relaxation;
+  if (p.precise_hydro)
+    kb_project<kBlock, kFirst, true, kTPT><<<s->d.n_patches, kP / kTPT, 0, st>>>(s->d, s->cur, inv_dt2, rh, rd);
+  else
+    kb_project<kBlock, kFirst, false, kTPT><<<s->d.n_patches, kP / kTPT, 0, st>>>(s->d, s->cur, inv_dt2, rh, rd);
+}
+
 template <bool kBlock, bool kFirst>
 void project_b(Batch* s, float inv_dt2, cudaStream_t st) {
-  const xpbd_params& p = s->prm;
-  if (p.precise_hydro)
-    kb_project<kBlock, kFirst, true><<<s->d.n_patches, kP, 0, st>>>(s->d, s->cur, inv_dt2, p.hydrostatic_relaxation,
-                                                                     p.deviatoric_relaxation);
-  else
-    kb_project<kBlock, kFirst, false><<<s->d.n_patches, kP, 0, st>>>(s->d, s->cur, inv_dt2, p.hydrostatic_relaxation,
-                                                                      p.deviatoric_relaxation);
+  if (batch_tpt(s->prm) == 2) project_bt<kBlock, kFirst, 2>(s, inv_dt2, st);
+  else project_bt<kBlock, kFirst, 1>(s, inv_dt2, st);
 }
 
 template <bool kRes, bool kMon>
 void residual_b(Batch* s, const BSweep& a, cudaStream_t st) {
-  const int chunk = (s->d.n_patches + s->res_ctas - 1) / s->res_ctas;
+  const bool two = batch_tpt(s->prm) == 2;
+  const int ctas = two ? s->res_ctas2 : s->res_ctas;
+  const int chunk = (s->d.n_patches + ctas - 1) / ctas;
   const int grid = (s->d.n_patches + chunk - 1) / chunk;
-  if (s->prm.precise_hydro) kb_residual<kRes, kMon, true><<<grid, kP, 0, st>>>(s->d, a, chunk);
-  else kb_residual<kRes, kMon, false><<<grid, kP, 0, st>>>(s->d, a, chunk);
+  const bool pr = s->prm.precise_hydro != 0;
+  if (two) {
+    if (pr) kb_residual<kRes, kMon, true, 2><<<grid, kP / 2, 0, st>>>(s->d, a, chunk);
+    else kb_residual<kRes, kMon, false, 2><<<grid, kP / 2, 0, st>>>(s->d, a, chunk);
+  } else {
+    if (pr) kb_residual<kRes, kMon, true, 1><<<grid, kP, 0, st>>>(s->d, a, chunk);
+    else kb_residual<kRes, kMon, false, 1><<<grid, kP, 0, st>>>(s->d, a, chunk);
+  }
 }
 
 void iteration_b(Batch* s, int it, float dt, int rec, cudaStream_t st) {
@@ -632,10 +669,16 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
     int dev = 0, sms = 0, bps = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kb_residual<true, false, true>, kP, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kb_residual<true, false, true, 1>, kP, 0) != cudaSuccess ||
         bps < 1)
       bps = 2;
     s->res_ctas = sms * bps > 0 ? sms * bps : 1;
+    bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kb_residual<true, false, true, 2>, kP / 2, 0) !=
+            cudaSuccess ||
+        bps < 1)
+      bps = 4;
+    s->res_ctas2 = sms * bps > 0 ? sms * bps : 1;
   }
   const int nval = d.V > d.n_patches ? d.V : d.n_patches;
   kb_validate<<<nblk(nval), 256>>>(d, s->n_out);

@@ -323,4 +323,80 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// det of a row-major 3x3 (cofactor expansion along the first column); for
+// inv_Dm it is 1 / det(Dm) = 1 / (6 V0) with the sign of the rest volume.
+__device__ __forceinline__ float det9(const float m[9]) {
+  return m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) + m[6] * (m[1] * m[5] - m[4] * m[2]);
+}
+
+// Resident CTAs per SM the tile projections are compiled for, by tets per
+// thread: with 2, 7 CTAs of 128 threads leave 73 registers a thread (the chain
+// needs 72 without spills); otherwise no minimum.
+__host__ __device__ constexpr int project_min_blocks(int tpt) { return tpt == 2 ? 7 : 1; }
+
+// Tile projection of kTPT Morton-consecutive tets of one thread (records
+// A, B, C, lid; multipliers L, stored to lam_out[k] as each tet is done), n of
+// them valid.  Vertex
+// positions come from the patch tile sp (global ids sg).  Consecutive tets of
+// a patch usually share a face, so the previous tet's four corner sums stay in
+// registers: a corner of the next tet that matches one is added there, and a
+// held corner the next tet does not touch is flushed with red.global.add.v4.
+// A chain of kTPT tets sharing s corners per step issues 4 + (kTPT - 1)(4 - s)
+// reductions instead of 4 kTPT.  cD, cH: time-scaled inverse Lame parameters;
+// the tet's compliances are 6 det(inv_Dm) cD and 6 det(inv_Dm) cH (1 / V0).
+template <bool kBlockMode, bool kPrecise, int kTPT>
+__device__ __forceinline__ void project_chain(const float4 (&A)[kTPT], const float4 (&B)[kTPT], const float (&C)[kTPT],
+                                              const uint32_t (&lid)[kTPT], float2 (&L)[kTPT], float2* lam_out,
+                                              int n, const float4* sp, const int* sg, float4* dx, float cD,
+                                              float cH, float relax_h, float relax_d) {
+  float4 acc[4];
+  int hid[4] = {-1, -1, -1, -1};
+#pragma unroll
+  for (int k = 0; k < kTPT; ++k) {
+    if (k >= n) break;
+    Tet tt;
+    tt.dm[0] = A[k].x; tt.dm[1] = A[k].y; tt.dm[2] = A[k].z;
+    tt.dm[3] = A[k].w; tt.dm[4] = B[k].x; tt.dm[5] = B[k].y;
+    tt.dm[6] = B[k].z; tt.dm[7] = B[k].w; tt.dm[8] = C[k];
+    int id[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      id[c] = (int)((lid[k] >> (8 * c)) & 0xffu);
+      tt.p[c] = sp[id[c]];
+    }
+    const float six_det = 6.f * det9(tt.dm);
+    float3 dp[4];
+    float cnt;
+    project_tet<kBlockMode, kPrecise>(tt, six_det * cD, six_det * cH, relax_h, relax_d, L[k], dp, cnt);
+    lam_out[k] = L[k];
+    float4 nacc[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) nacc[c] = make_float4(dp[c].x, dp[c].y, dp[c].z, cnt);
+    // Held corners: merge into the matching new corner, or flush.  A tet's
+    // corners are distinct vertices, so a held corner matches at most one.
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      bool used = false;
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (hid[q] == id[c]) {
+          nacc[c].x += acc[q].x;
+          nacc[c].y += acc[q].y;
+          nacc[c].z += acc[q].z;
+          nacc[c].w += acc[q].w;
+          used = true;
+        }
+      if (hid[q] >= 0 && !used) red_add_v4(dx + sg[hid[q]], acc[q].x, acc[q].y, acc[q].z, acc[q].w);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      acc[c] = nacc[c];
+      hid[c] = id[c];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (hid[q] >= 0) red_add_v4(dx + sg[hid[q]], acc[q].x, acc[q].y, acc[q].z, acc[q].w);
+}
+
 }  // namespace xpbd

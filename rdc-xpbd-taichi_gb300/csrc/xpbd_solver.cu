@@ -153,8 +153,16 @@ template <bool kCheb, bool kFirstIt, bool kResetDx>
 __global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.V) return;
+  // every load is issued before the first store: as far as the compiler
+  // knows the buffers may alias, so a load after a store would wait for it
   const float4 pc = d.p[cur][i];
   const float4 D = d.dx[i];
+  float4 yp = pc;
+  float om = 1.f;
+  if (kCheb) {
+    if (!kFirstIt) yp = d.p[cur ^ 1][i];
+    om = (float)d.st->omega;
+  }
   if (kResetDx) d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   float3 xp = make_float3(pc.x, pc.y, pc.z);
   if (D.w > 0.f) {
@@ -163,8 +171,6 @@ __global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma) 
     xp.z += D.z / D.w;
   }
   if (kCheb) {
-    const float om = (float)d.st->omega;
-    const float4 yp = kFirstIt ? pc : d.p[cur ^ 1][i];
     const float nx = gamma * (xp.x - pc.x) + pc.x;
     const float ny = gamma * (xp.y - pc.y) + pc.y;
     const float nz = gamma * (xp.z - pc.z) + pc.z;
@@ -230,10 +236,6 @@ __global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float cD, fl
   d.lam[t] = L;
 #pragma unroll
   for (int c = 0; c < 4; ++c) emit<kGather>(d, t, c, vid[c], dp[c], cnt);
-}
-
-__device__ __forceinline__ float det9(const float m[9]) {
-  return m[0] * (m[4] * m[8] - m[7] * m[5]) - m[3] * (m[1] * m[8] - m[7] * m[2]) + m[6] * (m[1] * m[5] - m[4] * m[2]);
 }
 
 // ---------------------------------------------------------------------------
@@ -706,14 +708,11 @@ __global__ void __launch_bounds__(kP) k_project_patch1(Dev d, int cur, float cD,
   }
 }
 
-// Tile variant, one CTA per patch, kTPT Morton-consecutive tets per thread.
-// Consecutive tets of a patch usually share a face, so the thread keeps the
-// previous tet's four corner sums in registers: a corner of the next tet that
-// matches one of them is added there, and a held corner the next tet does not
-// touch is flushed with red.global.add.v4.  A chain of kTPT tets sharing s
-// corners per step issues 4 + (kTPT - 1)(4 - s) reductions instead of 4 kTPT.
+// Tile variant, one CTA per patch, kTPT Morton-consecutive tets per thread;
+// corners shared along a thread's chain are summed in registers before the
+// global reduction (project_chain).
 template <bool kBlockMode, bool kFirst, bool kPrecise, int kP, int kTPT>
-__global__ void __launch_bounds__(kP / kTPT) k_project_patchN(Dev d, int cur, float cD, float cH, float relax_h,
+__global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) k_project_patchN(Dev d, int cur, float cD, float cH, float relax_h,
                                                              float relax_d) {
   constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
@@ -750,54 +749,9 @@ __global__ void __launch_bounds__(kP / kTPT) k_project_patchN(Dev d, int cur, fl
     sp[j] = ldg4(P + g);
   }
   __syncthreads();
-  float4 acc[4];
-  int hid[4] = {-1, -1, -1, -1};
-#pragma unroll
-  for (int k = 0; k < kTPT; ++k) {
-    if (l0 + k >= nt) break;
-    Tet tt;
-    tt.dm[0] = A[k].x; tt.dm[1] = A[k].y; tt.dm[2] = A[k].z;
-    tt.dm[3] = A[k].w; tt.dm[4] = B[k].x; tt.dm[5] = B[k].y;
-    tt.dm[6] = B[k].z; tt.dm[7] = B[k].w; tt.dm[8] = C[k];
-    int id[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      id[c] = (int)((lid[k] >> (8 * c)) & 0xffu);
-      tt.p[c] = sp[id[c]];
-    }
-    const float six_det = 6.f * det9(tt.dm);
-    float3 dp[4];
-    float cnt;
-    project_tet<kBlockMode, kPrecise>(tt, six_det * cD, six_det * cH, relax_h, relax_d, L[k], dp, cnt);
-    d.lam[t0 + l0 + k] = L[k];
-    float4 nacc[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) nacc[c] = make_float4(dp[c].x, dp[c].y, dp[c].z, cnt);
-    // Held corners: merge into the matching new corner, or flush.  A tet's
-    // corners are distinct vertices, so a held corner matches at most one.
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      bool used = false;
-#pragma unroll
-      for (int c = 0; c < 4; ++c)
-        if (hid[q] == id[c]) {
-          nacc[c].x += acc[q].x;
-          nacc[c].y += acc[q].y;
-          nacc[c].z += acc[q].z;
-          nacc[c].w += acc[q].w;
-          used = true;
-        }
-      if (hid[q] >= 0 && !used) red_add_v4(d.dx + sg[hid[q]], acc[q].x, acc[q].y, acc[q].z, acc[q].w);
-    }
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      acc[c] = nacc[c];
-      hid[c] = id[c];
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-    if (hid[q] >= 0) red_add_v4(d.dx + sg[hid[q]], acc[q].x, acc[q].y, acc[q].z, acc[q].w);
+  const int n = nt - l0 < kTPT ? nt - l0 : kTPT;
+  project_chain<kBlockMode, kPrecise, kTPT>(A, B, C, lid, L, d.lam + t0 + l0, n, sp, sg, d.dx, cD, cH, relax_h,
+                                            relax_d);
 }
 
 template <bool kRes, bool kMon, bool kPrecise, int kP>
@@ -1083,10 +1037,15 @@ int fail(int status, const std::string& msg) {
   return status;
 }
 
-#define XPBD_CUDA(call)                                                                             \
-  do {                                                                                              \
-    cudaError_t e_ = (call);                                                                        \
-    if (e_ != cudaSuccess) return fail(XPBD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+// On failure the runtime's per-thread last error is cleared as well, so that a
+// later cudaGetLastError check does not report this call again.
+#define XPBD_CUDA(call)                                                            \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      cudaGetLastError();                                                          \
+      return fail(XPBD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    }                                                                              \
   } while (0)
 
 struct GraphKey {
@@ -1115,6 +1074,13 @@ struct Solver {
   cudaStream_t cap = nullptr;
   cudaGraphExec_t exec = nullptr;
   GraphKey key;
+  // profiling with use_graph: the frame graph carries an event record node
+  // before and after every launch; the events belong to that graph
+  cudaGraphExec_t pexec = nullptr;
+  GraphKey pkey;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> gpairs[XPBD_K_COUNT];
+  bool greplay = false;    // a replay of pexec whose times are not yet added
+  bool capturing = false;  // a frame is being captured on cap
 };
 
 inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
@@ -1139,15 +1105,21 @@ struct Prof {
   Prof(Solver* s_, int cls_, cudaStream_t st_) : s(s_), cls(cls_), st(st_) {
     if (s->profiling) {
       a = take_event(s);
-      if (a) cudaEventRecord(a, st);
+      if (a) record(a);
     }
   }
   ~Prof() {
     if (!a) return;
     cudaEvent_t b = take_event(s);
     if (!b) return;
-    cudaEventRecord(b, st);
+    record(b);
     s->pending[cls].push_back({a, b});
+  }
+  // under stream capture an event record becomes a graph event record node
+  // only with cudaEventRecordExternal (otherwise it marks a capture dependency)
+  void record(cudaEvent_t e) const {
+    if (s->capturing) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+    else cudaEventRecord(e, st);
   }
 };
 
@@ -1387,10 +1359,69 @@ int enqueue_frame(Solver* s, double frame_dt, double dt, int substeps, cudaStrea
   return XPBD_OK;
 }
 
+// Adds the event times of the last profiled graph replay (waits for it).
+int accumulate_graph_profile(Solver* s) {
+  if (!s->greplay) return XPBD_OK;
+  s->greplay = false;
+  for (int k = 0; k < XPBD_K_COUNT; ++k)
+    for (auto& pr : s->gpairs[k]) {
+      float t = 0.f;
+      XPBD_CUDA(cudaEventSynchronize(pr.second));
+      XPBD_CUDA(cudaEventElapsedTime(&t, pr.first, pr.second));
+      s->prof_ms[k] += t;
+      s->prof_n[k] += 1;
+    }
+  return XPBD_OK;
+}
+
 void drop_graph(Solver* s) {
   if (s->exec) cudaGraphExecDestroy(s->exec);
   s->exec = nullptr;
   s->key = GraphKey();
+  accumulate_graph_profile(s);
+  if (s->pexec) cudaGraphExecDestroy(s->pexec);
+  s->pexec = nullptr;
+  s->pkey = GraphKey();
+  for (auto& v : s->gpairs) {
+    for (auto& pr : v) {
+      s->pool.push_back(pr.first);
+      s->pool.push_back(pr.second);
+    }
+    v.clear();
+  }
+}
+
+// Captures one frame into *exec.  With profiling on, the Prof brackets become
+// event record nodes and their event pairs move to gpairs.
+int capture_frame(Solver* s, double frame_dt, double dt, int substeps, cudaGraphExec_t* exec) {
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> direct[XPBD_K_COUNT];
+  for (int k = 0; k < XPBD_K_COUNT; ++k) direct[k].swap(s->pending[k]);
+  cudaError_t e = cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    for (int k = 0; k < XPBD_K_COUNT; ++k) s->pending[k].swap(direct[k]);
+    XPBD_CUDA(e);
+  }
+  s->capturing = true;
+  int r = enqueue_frame(s, frame_dt, dt, substeps, s->cap);
+  s->capturing = false;
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(s->cap, &g);
+  for (int k = 0; k < XPBD_K_COUNT; ++k) {
+    for (auto& pr : s->pending[k]) s->gpairs[k].push_back(pr);
+    s->pending[k].swap(direct[k]);
+  }
+  if (r != XPBD_OK) {
+    if (g) cudaGraphDestroy(g);
+    return r;
+  }
+  if (e != cudaSuccess) return fail(XPBD_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    *exec = nullptr;
+    return fail(XPBD_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+  }
+  return XPBD_OK;
 }
 
 }  // namespace
@@ -1664,29 +1695,33 @@ int xpbd_solve(void* handle, double frame_dt, double dt, int32_t substeps, void*
   if (substeps <= 0 || !(dt > 0.0) || !(frame_dt >= 0.0))
     return fail(XPBD_ERR_INVALID_ARGUMENT, "need substeps > 0, dt > 0, frame_dt >= 0");
   if (frame_dt / dt > 1e6) return fail(XPBD_ERR_INVALID_ARGUMENT, "frame_dt / dt too large");
-  if (!s->prm.use_graph || s->profiling) {
+  if (!s->prm.use_graph) {
     int r = enqueue_frame(s, frame_dt, dt, substeps, S(stream));
     if (r != XPBD_OK) return r;
     XPBD_CUDA(cudaGetLastError());
     return XPBD_OK;
   }
+  if (s->profiling) {
+    // the graph with timing nodes; the previous replay's times are added first
+    // (a host wait per frame, only while profiling)
+    if (!(s->pexec && s->pkey.frame_dt == frame_dt && s->pkey.dt == dt && s->pkey.substeps == substeps)) {
+      drop_graph(s);
+      int r = capture_frame(s, frame_dt, dt, substeps, &s->pexec);
+      if (r != XPBD_OK) return r;
+      s->pkey.frame_dt = frame_dt;
+      s->pkey.dt = dt;
+      s->pkey.substeps = substeps;
+    }
+    int r = accumulate_graph_profile(s);
+    if (r != XPBD_OK) return r;
+    XPBD_CUDA(cudaGraphLaunch(s->pexec, S(stream)));
+    s->greplay = true;
+    return XPBD_OK;
+  }
   if (!(s->exec && s->key.frame_dt == frame_dt && s->key.dt == dt && s->key.substeps == substeps)) {
     drop_graph(s);
-    XPBD_CUDA(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
-    int r = enqueue_frame(s, frame_dt, dt, substeps, s->cap);
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(s->cap, &g);
-    if (r != XPBD_OK) {
-      if (g) cudaGraphDestroy(g);
-      return r;
-    }
-    if (e != cudaSuccess) return fail(XPBD_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&s->exec, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) {
-      s->exec = nullptr;
-      return fail(XPBD_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
-    }
+    int r = capture_frame(s, frame_dt, dt, substeps, &s->exec);
+    if (r != XPBD_OK) return r;
     s->key.frame_dt = frame_dt;
     s->key.dt = dt;
     s->key.substeps = substeps;
@@ -1733,6 +1768,8 @@ int xpbd_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, in
   Solver* s = static_cast<Solver*>(handle);
   if (!s || n < 0 || n > XPBD_K_COUNT) return fail(XPBD_ERR_INVALID_ARGUMENT, "bad profile read");
   XPBD_CUDA(cudaStreamSynchronize(S(stream)));
+  int r = accumulate_graph_profile(s);
+  if (r != XPBD_OK) return r;
   for (int k = 0; k < XPBD_K_COUNT; ++k) {
     for (auto& pr : s->pending[k]) {
       float t = 0.f;

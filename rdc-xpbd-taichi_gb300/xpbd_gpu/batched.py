@@ -46,7 +46,7 @@ class XPBDBatchedSolver:
     def __init__(self, bodies, sdf, frame_dt=1e-2, dt=1e-2, substeps_num=20, constraints_iter=5,
                  hydrostatic_relaxation=1.2, deviatoric_relaxation=1.2, cheb_enable=True, cheb_warmup=5,
                  cheb_gamma=0.6666, block_neohookean_enable=True, monitor_convergence=False,
-                 gravity=(0.0, -9.8, 0.0), precise_hydro=None, use_graph=True):
+                 gravity=(0.0, -9.8, 0.0), precise_hydro=None, use_graph=True, tets_per_thread=2):
         if isinstance(sdf, (list, tuple)):
             self.sdfs = [s for s in sdf if s is not None]
         else:
@@ -72,6 +72,9 @@ class XPBDBatchedSolver:
         nus = [b.poisson_ratio for b in self.bodies]
         self.precise_hydro = (max(nus) >= 0.49) if precise_hydro is None else bool(precise_hydro)
         self.use_graph = bool(use_graph)
+        if tets_per_thread not in (1, 2):
+            raise ValueError("tets_per_thread must be 1 or 2")
+        self.tets_per_thread = int(tets_per_thread)
         self.time = 0.0
         self.current_frame = 0
         self._handle = None
@@ -236,6 +239,7 @@ class XPBDBatchedSolver:
         p.precise_hydro = 1 if self.precise_hydro else 0
         p.scatter = _native.SCATTER_PATCH
         p.use_graph = 1 if self.use_graph else 0
+        p.tets_per_thread = self.tets_per_thread
         p.rho_min, p.rho_max, p.rho_beta = self.rho_min, self.rho_max, self.rho_beta
         return p
 

@@ -231,8 +231,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         return out
 
     def set_profiling(self, enable):
-        """Bracket every kernel launch with CUDA events (frames then launch
-        directly instead of replaying the graph)."""
+        """Bracket every kernel launch with CUDA events (with use_graph the
+        frame graph carries them as event record nodes)."""
         _native.check(self._lib.xpbd_set_profiling(self._handle, 1 if enable else 0))
 
     def read_profile(self, reset=False):

@@ -108,3 +108,30 @@ def test_usd_export_accessors():
         elif isinstance(sdf, PlaneSdf):
             assert sdf.point[None].to_numpy().shape == (3,)
             np.testing.assert_allclose(np.linalg.norm(sdf.dir[None].to_numpy()), 1.0, rtol=1e-6)
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_profiling_counts_launches_and_keeps_results(use_graph):
+    """Event brackets per kernel class (event record nodes inside the frame
+    graph, or direct launches) count every launch of the profiled frames and
+    leave the results bitwise unchanged (deterministic gather variant)."""
+    from xpbd_gpu.neohookean_solver import frame_chunks
+    _, ref = _solver(scatter="gather", monitor_convergence=False, use_graph=use_graph)
+    _, s = _solver(scatter="gather", monitor_convergence=False, use_graph=use_graph)
+    K = s.constraints_iter
+    per_frame = len(frame_chunks(s.frame_dt, s.dt)) * s.substeps_num
+    s.set_profiling(True)
+    s.read_profile(reset=True)
+    for f in range(3):  # frames 0 and 2 profiled, frame 1 not
+        ref.solve()
+        s.solve()
+        s.set_profiling(f == 1)
+    prof = s.read_profile(reset=True)
+    n_sub = 2 * per_frame
+    assert prof["begin"]["launches"] == n_sub and prof["end"]["launches"] == n_sub
+    for k in ("project", "gather", "update"):
+        assert prof[k]["launches"] == n_sub * K, (k, prof)
+    for k, v in prof.items():
+        assert (v["ms"] > 0.0) == (v["launches"] > 0), (k, v)
+    np.testing.assert_array_equal(s.mesh.verts.x.to_numpy(), ref.mesh.verts.x.to_numpy())
+    assert s.read_profile()["project"]["launches"] == 0

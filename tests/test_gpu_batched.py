@@ -48,10 +48,11 @@ def _single(body, sdfs, kw):
                                 density=body.density, scatter="patch", **kw)
 
 
-def test_batch_matches_single_body_solvers():
+@pytest.mark.parametrize("tpt", [1, 2])
+def test_batch_matches_single_body_solvers(tpt):
     from xpbd_gpu.batched import XPBDBatchedSolver
     bodies, sdfs, kw = _scene()
-    batch = XPBDBatchedSolver(bodies, sdfs(), **kw)
+    batch = XPBDBatchedSolver(bodies, sdfs(), tets_per_thread=tpt, **kw)
     singles = [_single(b, sdfs, kw) for b in bodies]
     for k, s in enumerate(singles):
         np.testing.assert_allclose(batch.body_positions(k), s.mesh.verts.x.to_numpy(), rtol=0, atol=1e-6)
@@ -74,7 +75,8 @@ def test_batch_matches_single_body_solvers():
             assert abs(rho[k] - s.rho_hat) < 2e-3
 
 
-def test_batch_against_float64_oracle():
+@pytest.mark.parametrize("tpt", [1, 2])
+def test_batch_against_float64_oracle(tpt):
     """Against the float64 oracle the batch must be as accurate as an FP32 run of
     the reference algorithm: per body, max deviation <= max(1e-4 diag, 3 x the
     deviation of the float32 oracle).  (Body 1 rests on a fixed sphere with 103
@@ -83,7 +85,7 @@ def test_batch_against_float64_oracle():
     from oracle.xpbd_oracle import OracleSdf, OracleSolver
     from xpbd_gpu.batched import XPBDBatchedSolver
     bodies, sdfs, kw = _scene()
-    batch = XPBDBatchedSolver(bodies, sdfs(), **kw)
+    batch = XPBDBatchedSolver(bodies, sdfs(), tets_per_thread=tpt, **kw)
     pairs = []
     for b in bodies:
         pts = b.rest_pose.points if b.rotation is None else b.rest_pose.points @ b.rotation.T
