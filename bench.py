@@ -227,6 +227,144 @@ def run_c4(args):
     print(json.dumps(line), flush=True)
 
 
+def workload_c5(seed=0, n_bodies=64, h=1.0 / 16, sigma=2.0):
+    """64 Kuhn bodies with per-axis cell counts U{8..24} (cell edge 1/16 m, jitter 0.1 cell), each with a
+    hidden per-tet log E field (mean log-U[1e4, 1e6] + 0.5 g, g a unit-variance Gaussian field of sigma
+    cells) and nu U[0.35, 0.48]; density 1000; dropped from 0.3 m onto the plane y = 0 (bodies on an 8 x 8
+    grid of 2.5 m pitch, independent of each other); 30 frames x 5 substeps x 20 it."""
+    from xpbd_gpu.mesh import kuhn_grid
+    rng = np.random.default_rng(seed)
+    dims = rng.integers(8, 25, size=(n_bodies, 3))
+    mean = rng.uniform(np.log(1e4), np.log(1e6), n_bodies)
+    nus = rng.uniform(0.35, 0.48, n_bodies)
+    meshes, log_E = [], []
+    for k in range(n_bodies):
+        nx, ny, nz = (int(v) for v in dims[k])
+        origin = (2.5 * (k % 8), 0.3, 2.5 * (k // 8))
+        meshes.append(kuhn_grid(nx, ny, nz, h, origin=origin, jitter=0.1, seed=seed * 1000 + k))
+        g = smooth_field((nx, ny, nz), sigma, rng)
+        log_E.append(mean[k] + 0.5 * np.repeat(g.ravel(order="F"), 6))
+    specs = [("plane", dict(point=[0.0, 0.0, 0.0], dir=[0.0, 1.0, 0.0], fixed=True))]
+    kw = dict(frame_dt=1.0 / 60, dt=1.0 / 60, substeps_num=5, constraints_iter=20, cheb_enable=True,
+              cheb_warmup=5, cheb_gamma=0.6666, block_neohookean_enable=True)
+    desc = ("64 Kuhn bodies (cells U{8..24}^3, %d tets, %d verts), hidden per-tet log E (mean log-U[1e4,1e6], "
+            "sigma 0.5), nu U[0.35,0.48], plane, 30 frames x 5 substeps x 20 it, MSE of final positions" % (
+                sum(m.n_tets for m in meshes), sum(m.n_verts for m in meshes)))
+    return meshes, log_E, nus, specs, kw, desc
+
+
+def run_c5(args):
+    """Batched differentiable: Adam on every body's per-tet log E through the batched adjoint, against
+    the plain per-body form (one single-body adjoint per body) on a subset of the bodies."""
+    import torch
+    from xpbd_gpu.batched import Body
+    from xpbd_gpu.differentiable import BatchedDiffSim, DiffSim, xpbd_simulate, xpbd_simulate_batch
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda")
+    meshes, log_E_true, nus, specs, kw, desc = workload_c5()
+    frames, steps, lr = args.c5_frames, args.c5_adam_steps, args.c5_lr
+    nb = len(meshes)
+    T_all = sum(m.n_tets for m in meshes)
+    nu_tet = np.concatenate([np.full(m.n_tets, nus[k]) for k, m in enumerate(meshes)])
+    le_true = np.concatenate(log_E_true)
+    le0 = np.full(T_all, np.log(1e5))
+    bodies = [Body(m, tet_young_modulus=np.exp(log_E_true[k]), tet_poisson_ratio=nus[k], density=1000.0,
+                   poisson_ratio=float(nus[k])) for k, m in enumerate(meshes)]
+    sim = BatchedDiffSim(bodies, product_sdfs(specs), **kw)
+    x0 = torch.tensor(np.concatenate([m.points for m in meshes]), dtype=torch.float32, device=dev)
+    v0 = torch.zeros_like(x0)
+    nu_t = torch.tensor(nu_tet, dtype=torch.float64, device=dev)
+    with torch.no_grad():
+        x_target = xpbd_simulate_batch(sim, x0, v0, torch.tensor(le_true, device=dev), nu_t, frames).clone()
+    vcount = torch.tensor(np.concatenate([np.full(m.n_verts, 1.0 / m.n_verts) for m in meshes]), device=dev)
+
+    def per_body_rel_err(theta, lo, truth, start):
+        return float(np.linalg.norm(theta - truth) / max(np.linalg.norm(start - truth), 1e-30))
+
+    theta = torch.tensor(le0, dtype=torch.float64, device=dev, requires_grad=True)
+    opt = torch.optim.Adam([theta], lr=lr)
+    fwd_ms, bwd_ms, losses = [], [], []
+    for it in range(steps):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        opt.zero_grad()
+        e0.record()
+        xf = xpbd_simulate_batch(sim, x0, v0, theta, nu_t, frames)
+        loss = (((xf - x_target) ** 2).sum(1).double() * vcount).sum()  # sum of per-body MSEs
+        e1.record()
+        loss.backward()
+        e2.record()
+        opt.step()
+        e2.synchronize()
+        fwd_ms.append(e0.elapsed_time(e1))
+        bwd_ms.append(e1.elapsed_time(e2))
+        losses.append(float(loss))
+    sim.batch.check_status()
+    th = theta.detach().cpu().numpy()
+    offs = np.concatenate([[0], np.cumsum([m.n_tets for m in meshes])])
+    errs = [per_body_rel_err(th[offs[k]:offs[k + 1]], 0, le_true[offs[k]:offs[k + 1]], le0[offs[k]:offs[k + 1]])
+            for k in range(nb)]
+    rel_l2 = float(np.linalg.norm(th - le_true) / np.linalg.norm(le_true))
+
+    # plain per-body form on the first bodies: one single-body adjoint per body, same Adam
+    plain = []
+    nplain = min(args.c5_plain_bodies, nb)
+    for k in range(nplain):
+        m = meshes[k]
+        ps = DiffSim(m, product_sdfs(specs), np.full(m.n_tets, np.log(1e5)), np.full(m.n_tets, nus[k]),
+                     density=1000.0, poisson_ratio=float(nus[k]), **kw)
+        xk0 = torch.tensor(m.points, dtype=torch.float32, device=dev)
+        vk0 = torch.zeros_like(xk0)
+        nuk = torch.full((m.n_tets,), float(nus[k]), dtype=torch.float64, device=dev)
+        with torch.no_grad():
+            xt = xpbd_simulate(ps, xk0, vk0, torch.tensor(log_E_true[k], device=dev), nuk, frames).clone()
+        thk = torch.tensor(le0[offs[k]:offs[k + 1]], dtype=torch.float64, device=dev, requires_grad=True)
+        optk = torch.optim.Adam([thk], lr=lr)
+        ms = []
+        for it in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            optk.zero_grad()
+            a.record()
+            xf = xpbd_simulate(ps, xk0, vk0, thk, nuk, frames)
+            lk = ((xf - xt) ** 2).sum(1).double().mean()
+            lk.backward()
+            b.record()
+            optk.step()
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        ps.solver.check_status()
+        tk = thk.detach().cpu().numpy()
+        plain.append(dict(ms_per_adam_step=float(np.mean(ms[1:] if len(ms) > 1 else ms)),
+                          rel_err=per_body_rel_err(tk, 0, log_E_true[k], le0[offs[k]:offs[k + 1]]),
+                          batched_rel_err=errs[k],
+                          theta_rel_diff_vs_batched=float(np.linalg.norm(tk - th[offs[k]:offs[k + 1]]) /
+                                                          np.linalg.norm(th[offs[k]:offs[k + 1]]))))
+    sl = slice(1, None) if steps > 1 else slice(None)
+    step_ms = float(np.mean(np.add(fwd_ms, bwd_ms)[sl]))
+    units = T_all * frames * kw["substeps_num"] * kw["constraints_iter"]
+    plain_tets = sum(meshes[k].n_tets for k in range(nplain))
+    plain_ms = sum(p["ms_per_adam_step"] for p in plain)
+    plain_value = plain_tets * frames * kw["substeps_num"] * kw["constraints_iter"] / (plain_ms * 1e-3) if plain else None
+    line = {"metric": METRIC, "value": units / (step_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": steps,
+            "warmup": 1, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc,
+                       "step": "one Adam step on all 64 bodies: checkpointed batched forward of %d frames + "
+                               "batched adjoint (tet-iterations counted once, forward)" % frames,
+                       "form": "batched (one launch per phase over all bodies)"},
+            "forward_ms": float(np.mean(np.asarray(fwd_ms)[sl])), "backward_ms": float(np.mean(np.asarray(bwd_ms)[sl])),
+            "backward_over_forward": float(np.mean(np.asarray(bwd_ms)[sl]) / np.mean(np.asarray(fwd_ms)[sl])),
+            "adam": {"steps": steps, "lr": lr, "init": "log E = log 1e5 everywhere",
+                     "loss_first_last": [losses[0], losses[-1]],
+                     "recovered_rel_err_median": float(np.median(errs)),
+                     "recovered_rel_err_mean": float(np.mean(errs)),
+                     "recovered_rel_l2_of_log_E": rel_l2,
+                     "rel_err_definition": "|theta - theta*| / |theta_0 - theta*| per body"},
+            "plain": {"form": "one single-body DiffSim per body (ATOMIC scatter), same Adam",
+                      "bodies": nplain, "value": plain_value, "per_body": plain},
+            "batched_over_plain": (plain_value and units / (step_ms * 1e-3) / plain_value)}
+    print(json.dumps(line), flush=True)
+
+
 def relative_residuals(hist, substeps, iters, floor=1e-5):
     """Per body and substep r_hat_K / r_hat_0 from a (bodies, rows, 4) history; NaN where
     r_hat_0 is below `floor` (a free-falling body, residual at FP32 round-off)."""
@@ -657,7 +795,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5"])
+    ap.add_argument("--c5-frames", type=int, default=30)
+    ap.add_argument("--c5-adam-steps", type=int, default=200)
+    ap.add_argument("--c5-lr", type=float, default=0.05)
+    ap.add_argument("--c5-plain-bodies", type=int, default=4)
     ap.add_argument("--c4-frames", type=int, default=60)
     ap.add_argument("--c4-reps", type=int, default=2)
     ap.add_argument("--c4-check-frames", type=int, default=1)
@@ -680,6 +822,8 @@ def main():
         run_c3(args)
     elif args.workload == "c4" and args.impl != "reference":
         run_c4(args)
+    elif args.workload == "c5" and args.impl != "reference":
+        run_c5(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -350,6 +350,10 @@ typedef struct xpbd_batch {
   const int32_t* body_n_patches; /* [n_bodies] */
   const int32_t* body_n_tets; /* [n_bodies] real tets (r_hat = sum / n) */
   const int32_t* vert_perm;   /* [V] caller vertex of each solver vertex, -1 for padding */
+  /* optional per-tet materials: 1 / mu and 1 / lambda of every tet slot
+   * (padding slots unused); NULL = the body's body_inv_mu / body_inv_lambda */
+  const float* tet_inv_mu;    /* [T] */
+  const float* tet_inv_lambda; /* [T] */
 } xpbd_batch;
 
 /* Message of the last batch failure on the calling thread. */
@@ -377,6 +381,28 @@ int xpbd_batch_import_vec3(void* handle, int32_t field, const float* src, void* 
 int xpbd_batch_export_vec3(void* handle, int32_t field, float* dst, void* stream);
 int xpbd_batch_set_profiling(void* handle, int32_t enable);
 int xpbd_batch_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, int32_t reset, void* stream);
+
+/* Replace the batch's constants between frames (attribute changes of the
+ * solver objects a batch replaces, neohookean_solver.py:18-77); drops the
+ * cached frame graph when they differ.  Used by the launch autotuner to
+ * switch tets_per_thread in place. */
+int xpbd_batch_set_params(void* handle, const xpbd_params* params);
+
+/* Stream-ordered copy of every body's rho_hat (neohookean_solver.py:65) to /
+ * from a device array of n_bodies doubles (per-substep adjoint checkpoints). */
+int xpbd_batch_save_rho_hat(void* handle, double* dst_device, void* stream);
+int xpbd_batch_load_rho_hat(void* handle, const double* src_device, void* stream);
+
+/* Batched differentiation (no counterpart in the reference, which has no
+ * gradients): xpbd_substep_tape / xpbd_substep_adjoint for every body of the
+ * batch at once, block mode only.  Tape and adjoint buffers are sized by the
+ * padded batch (V = n_verts, T = n_tets of xpbd_batch); history rows [0, K)
+ * of every body receive the substep's omegas, so max_records >= K.  Per-tet
+ * material adjoints are written per tet slot (dL/d(1/mu), dL/d(1/lambda) of
+ * the tet's own material with tet_inv_mu, else of its body's). */
+int xpbd_batch_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* stream);
+int xpbd_batch_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xpbd_adjoint* adj,
+                               void* stream);
 
 #ifdef __cplusplus
 }

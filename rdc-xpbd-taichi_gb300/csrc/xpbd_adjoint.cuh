@@ -15,6 +15,18 @@
 // Conventions: omega is a stop-gradient (a control heuristic of the
 // residual ratio); the contact sets and the pivot branch are piecewise
 // constant; the derivative of the 2x2 solve is that of A^-1 b.
+//
+// The kernels are templates over the solver's device view D (the single-body
+// and the batched layouts).  Each layout provides, next to its own type so
+// that argument-dependent lookup finds them:
+//   int   adj_verts(const D&), adj_tets(const D&)   vertex and tet slots
+//   bool  adj_load_tet(const D&, int t, int vid[4], Tet&, float& inv_v0,
+//                      float& m_mu, float& m_la)   false for a padding slot;
+//         m_mu, m_la multiply the compliance factors (the tet's 1/mu and
+//         1/lambda with per-tet materials, else 1)
+//   float adj_omega(const D&, int i, int k)          omega of vertex i's body
+//                                                    at iteration k
+// and the members x, v, sdfs, n_sdf.
 #pragma once
 
 namespace xpbd {
@@ -44,9 +56,10 @@ __device__ __forceinline__ float3 cross3(const float3 a, const float3 b) {
 }
 
 // Velocities after gravity and predicted positions before the SDF list.
-__global__ void __launch_bounds__(256) k_tape_begin(Dev d, Tape tp, float dt, float gx, float gy, float gz) {
+template <class D>
+__global__ void __launch_bounds__(256) k_tape_begin(D d, Tape tp, float dt, float gx, float gy, float gz) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.V) return;
+  if (i >= adj_verts(d)) return;
   const float4 xi = d.x[i];
   float4 vi = d.v[i];
   if (xi.w > 0.f) {
@@ -60,9 +73,10 @@ __global__ void __launch_bounds__(256) k_tape_begin(Dev d, Tape tp, float dt, fl
 
 // Reverse of advance: live vertices x' = x~_K, v' = (x~_K - x) e / dt; pinned
 // vertices keep x and v.
-__global__ void __launch_bounds__(256) ka_end(Dev d, Adj a, float e_over_dt) {
+template <class D>
+__global__ void __launch_bounds__(256) ka_end(D d, Adj a, float e_over_dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.V) return;
+  if (i >= adj_verts(d)) return;
   const float4 gx = a.gx[i], gv = a.gv[i];
   if (d.x[i].w > 0.f) {
     a.abuf[0][i] = make_float4(gx.x + gv.x * e_over_dt, gx.y + gv.y * e_over_dt, gx.z + gv.z * e_over_dt, 0.f);
@@ -79,14 +93,14 @@ __global__ void __launch_bounds__(256) ka_end(Dev d, Adj a, float e_over_dt) {
 //   x~_{k+1} = y_prev + omega (xn - y_prev),  y_prev(k+1) = x~_k,
 // with y_prev(0) = x~_0.  Reads abuf[src] (adjoint of x~_{k+1}), writes
 // abuf[src^1] (direct part of the adjoint of x~_k), ybar and dxbar.
-template <bool kCheb>
-__global__ void __launch_bounds__(256) ka_cheb(Dev d, Adj a, int k, float gamma, int src) {
+template <class D, bool kCheb>
+__global__ void __launch_bounds__(256) ka_cheb(D d, Adj a, int k, float gamma, int src) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.V) return;
+  if (i >= adj_verts(d)) return;
   const float4 xb = a.abuf[src][i];
   float3 post, cur, yn;
   if (kCheb) {
-    const float om = (float)d.hist[4 * k + 1];
+    const float om = adj_omega(d, i, k);
     const float4 yb = a.ybar[i];
     post = make_float3(om * gamma * xb.x, om * gamma * xb.y, om * gamma * xb.z);
     const float c = om * (1.f - gamma);
@@ -111,28 +125,21 @@ __global__ void __launch_bounds__(256) ka_cheb(Dev d, Adj a, int k, float gamma,
 
 // Reverse of the block projection of iteration k for one tet; scatters the
 // position adjoints into abuf[dst] and updates the multiplier adjoint.
-template <bool kPrecise>
-__global__ void __launch_bounds__(128) ka_project(Dev d, Tape tp, Adj a, int k, float cD, float cH, int dst) {
+template <class D, bool kPrecise>
+__global__ void __launch_bounds__(128) ka_project(D d, Tape tp, Adj a, int k, float cD, float cH, int dst) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= d.T) return;
-  int4 id;
+  if (t >= adj_tets(d)) return;
+  int vid[4];
   Tet tt;
-  load_tet(d, t, id, tt);
-  const float4* X = tp.xs + (size_t)k * d.V;
-  tt.p[0] = __ldg(X + id.x);
-  tt.p[1] = __ldg(X + id.y);
-  tt.p[2] = __ldg(X + id.z);
-  tt.p[3] = __ldg(X + id.w);
-  const float2 L = tp.lams[(size_t)k * d.T + t];
+  float inv_v0, m_mu, m_la;
+  if (!adj_load_tet(d, t, vid, tt, inv_v0, m_mu, m_la)) return;
+  const float4* X = tp.xs + (size_t)k * adj_verts(d);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) tt.p[c] = __ldg(X + vid[c]);
+  const float2 L = tp.lams[(size_t)k * adj_tets(d) + t];
   const float w[4] = {tt.p[0].w, tt.p[1].w, tt.p[2].w, tt.p[3].w};
-  const int vid[4] = {id.x, id.y, id.z, id.w};
-  const float inv_v0 = 1.f / tt.V0;
-  float sD = cD * inv_v0, sH = cH * inv_v0;  // d aD / d(1/mu) (per-tet materials) or aD itself
-  float aD = sD, aH = sH;
-  if (d.tinv_mu) {
-    aD *= __ldg(d.tinv_mu + t);
-    aH *= __ldg(d.tinv_la + t);
-  }
+  const float sD = cD * inv_v0, sH = cH * inv_v0;  // d aD / d(1/mu), d aH / d(1/lambda)
+  const float aD = sD * m_mu, aH = sH * m_la;
   // ---- forward recompute ----
   float F[9];
   deformation_gradient(tt, F);
@@ -267,9 +274,10 @@ __device__ __forceinline__ float3 sdf_adjoint(const xpbd_sdf& s, const float3 q,
 }
 
 // Reverse of the SDF list (in reverse order) and of predict; adds into gx, gv.
-__global__ void __launch_bounds__(256) ka_begin(Dev d, Tape tp, Adj a, int src, float dt) {
+template <class D>
+__global__ void __launch_bounds__(256) ka_begin(D d, Tape tp, Adj a, int src, float dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.V) return;
+  if (i >= adj_verts(d)) return;
   float3 gb = f3(a.abuf[src][i]);
   const float4 pre = tp.xpre[i];
   if (pre.w > 0.f) {

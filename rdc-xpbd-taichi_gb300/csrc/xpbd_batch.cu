@@ -56,6 +56,8 @@ struct BDev {
   const int* vblock_body;
   const float* inv_mu;
   const float* inv_la;
+  const float* tinv_mu;  // per-tet 1 / mu (nullptr: the body's)
+  const float* tinv_la;  // per-tet 1 / lambda
   const int* body_patches;
   const int* body_tets;
   const int* perm;
@@ -119,9 +121,10 @@ __global__ void __launch_bounds__(256) kb_end(BDev d, int cur, float dt, float d
 }
 
 // Projection, one CTA of kP / kTPT threads per patch (the single-body tile
-// kernel with per-body compliance 1 / (mu_b dt^2), 1 / (lambda_b dt^2)); each
-// thread projects kTPT consecutive tets (project_chain).
-template <bool kBlockMode, bool kFirst, bool kPrecise, int kTPT>
+// kernel with per-body compliance 1 / (mu_b dt^2), 1 / (lambda_b dt^2), or
+// with kTetMat per-tet 1 / (mu_t dt^2), 1 / (lambda_t dt^2)); each thread
+// projects kTPT consecutive tets (project_chain).
+template <bool kBlockMode, bool kFirst, bool kPrecise, int kTPT, bool kTetMat>
 __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_project(BDev d, int cur, float inv_dt2, float relax_h, float relax_d) {
   constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
@@ -137,6 +140,7 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_projec
   float C[kTPT];
   uint32_t lid[kTPT];
   float2 L[kTPT];
+  float mD[kTPT], mH[kTPT];
 #pragma unroll
   for (int k = 0; k < kTPT; ++k) {
     A[k] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -144,12 +148,17 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_projec
     C[k] = 0.f;
     lid[k] = 0u;
     L[k] = make_float2(0.f, 0.f);
+    mD[k] = mH[k] = 0.f;
     if (l0 + k < nt) {
       A[k] = __ldg(d.dm_a + t0 + k);
       B[k] = __ldg(d.dm_b + t0 + k);
       C[k] = __ldg(d.dm_c + t0 + k);
       lid[k] = __ldg(d.lid + t0 + k);
       if (!kFirst) L[k] = d.lam[t0 + k];
+      if (kTetMat) {
+        mD[k] = __ldg(d.tinv_mu + t0 + k);
+        mH[k] = __ldg(d.tinv_la + t0 + k);
+      }
     }
   }
   const float4* P = d.p[cur];
@@ -161,9 +170,14 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_projec
   __syncthreads();
   const int n = nt - l0 < kTPT ? nt - l0 : kTPT;
   if (n <= 0) return;
-  const float cD = __ldg(d.inv_mu + b) * inv_dt2, cH = __ldg(d.inv_la + b) * inv_dt2;
-  project_chain<kBlockMode, kPrecise, kTPT>(A, B, C, lid, L, d.lam + t0, n, sp, sg, d.dx, cD, cH, relax_h,
-                                            relax_d);
+  if (kTetMat) {
+    project_chain<kBlockMode, kPrecise, kTPT, true>(A, B, C, lid, L, d.lam + t0, n, sp, sg, d.dx, inv_dt2, inv_dt2,
+                                                    relax_h, relax_d, mD, mH);
+  } else {
+    const float cD = __ldg(d.inv_mu + b) * inv_dt2, cH = __ldg(d.inv_la + b) * inv_dt2;
+    project_chain<kBlockMode, kPrecise, kTPT>(A, B, C, lid, L, d.lam + t0, n, sp, sg, d.dx, cD, cH, relax_h,
+                                              relax_d);
+  }
 }
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -249,7 +263,7 @@ __device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int b
 // Residual (neohookean_solver.py:298-329) and monitoring sums (:256-296).
 // Each CTA walks a contiguous run of `chunk` patches (patches are ordered by
 // body) and flushes its partial sums whenever the body changes.
-template <bool kRes, bool kMon, bool kPrecise, int kTPT>
+template <bool kRes, bool kMon, bool kPrecise, int kTPT, bool kTetMat>
 __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int chunk) {
   constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
@@ -270,6 +284,7 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
     float C[kTPT];
     uint32_t lid[kTPT];
     float2 L[kTPT];
+    float mD[kTPT], mH[kTPT];
 #pragma unroll
     for (int k = 0; k < kTPT; ++k) {
       if (l0 + k < nt) {
@@ -278,6 +293,10 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
         C[k] = __ldg(d.dm_c + t0 + k);
         lid[k] = __ldg(d.lid + t0 + k);
         L[k] = kRes ? d.lam[t0 + k] : make_float2(0.f, 0.f);
+        if (kTetMat && kRes) {
+          mD[k] = __ldg(d.tinv_mu + t0 + k);
+          mH[k] = __ldg(d.tinv_la + t0 + k);
+        }
       }
     }
     __syncthreads();  // the previous patch's readers are done with sp
@@ -287,8 +306,8 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
       sp[j] = make_float4(x.x, x.y, x.z, 0.f);
     }
     __syncthreads();
-    const float aDs = kRes ? __ldg(d.inv_mu + b) * a.inv_dt2 : 0.f;
-    const float aHs = kRes ? __ldg(d.inv_la + b) * a.inv_dt2 : 0.f;
+    const float aDs = kRes && !kTetMat ? __ldg(d.inv_mu + b) * a.inv_dt2 : 0.f;
+    const float aHs = kRes && !kTetMat ? __ldg(d.inv_la + b) * a.inv_dt2 : 0.f;
 #pragma unroll
     for (int k = 0; k < kTPT; ++k) {
       if (l0 + k >= nt) break;
@@ -306,7 +325,8 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
       invariants<kPrecise>(F, C_D, C_H);
       if (kRes) {
         const float six_det = 6.f * det9(tt.dm);
-        const float rD = C_D + six_det * aDs * L[k].x, rH = C_H + six_det * aHs * L[k].y;
+        const float cDk = kTetMat ? a.inv_dt2 * mD[k] : aDs, cHk = kTetMat ? a.inv_dt2 * mH[k] : aHs;
+        const float rD = C_D + six_det * cDk * L[k].x, rH = C_H + six_det * cHk * L[k].y;
         sr += sqrtf(rD * rD + rH * rH);
       }
       if (kMon) {
@@ -398,8 +418,51 @@ __global__ void kb_validate(BDev d, int n_out) {
   }
 }
 
+// Per-body rho_hat to / from a device array (adjoint checkpoints).
+__global__ void kb_rho_copy(BDev d, double* dst, const double* src) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= d.n_bodies) return;
+  if (dst) dst[b] = d.bs[b].rho_hat;
+  if (src) d.bs[b].rho_hat = src[b];
+}
+
+// Accessors of the batched layout for the adjoint kernels (xpbd_adjoint.cuh).
+__device__ __forceinline__ int adj_verts(const BDev& d) { return d.V; }
+__device__ __forceinline__ int adj_tets(const BDev& d) { return d.T; }
+__device__ __forceinline__ float adj_omega(const BDev& d, int i, int k) {
+  const int b = __ldg(d.vblock_body + (i >> 8));
+  return (float)d.hist[4 * ((size_t)b * d.max_records + k) + 1];
+}
+__device__ __forceinline__ bool adj_load_tet(const BDev& d, int t, int (&vid)[4], Tet& tt, float& inv_v0,
+                                             float& m_mu, float& m_la) {
+  const int p = t / kP;
+  if (t - p * kP >= __ldg(d.patch_ntets + p)) return false;  // padding slot
+  const uint32_t lid = __ldg(d.lid + t);
+  const int vb = __ldg(d.voff + p);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) vid[c] = __ldg(d.pverts + vb + (int)((lid >> (8 * c)) & 0xffu));
+  const float4 a = __ldg(d.dm_a + t);
+  const float4 b = __ldg(d.dm_b + t);
+  tt.dm[0] = a.x; tt.dm[1] = a.y; tt.dm[2] = a.z;
+  tt.dm[3] = a.w; tt.dm[4] = b.x; tt.dm[5] = b.y;
+  tt.dm[6] = b.z; tt.dm[7] = b.w; tt.dm[8] = __ldg(d.dm_c + t);
+  inv_v0 = 6.f * det9(tt.dm);
+  tt.V0 = 1.f / inv_v0;
+  if (d.tinv_mu) {
+    m_mu = __ldg(d.tinv_mu + t);
+    m_la = __ldg(d.tinv_la + t);
+  } else {
+    const int body = __ldg(d.patch_body + p);
+    m_mu = __ldg(d.inv_mu + body);
+    m_la = __ldg(d.inv_la + body);
+  }
+  return true;
+}
+
 }  // namespace batch
 }  // namespace xpbd
+
+#include "xpbd_adjoint.cuh"
 
 using namespace xpbd;
 using namespace xpbd::batch;
@@ -473,14 +536,22 @@ struct BProf {
 // tets per thread of the batched tile kernels: 1, or 2 (params 2 and 4)
 inline int batch_tpt(const xpbd_params& p) { return p.tets_per_thread >= 2 ? 2 : 1; }
 
-template <bool kBlock, bool kFirst, int kTPT>
-void project_bt(Batch* s, float inv_dt2, cudaStream_t st) {
+template <bool kBlock, bool kFirst, int kTPT, bool kTetMat>
+void project_btm(Batch* s, float inv_dt2, cudaStream_t st) {
   const xpbd_params& p = s->prm;
   const float rh = p.hydrostatic_relaxation, rd = p.deviatoric_relaxation;
   if (p.precise_hydro)
-    kb_project<kBlock, kFirst, true, kTPT><<<s->d.n_patches, kP / kTPT, 0, st>>>(s->d, s->cur, inv_dt2, rh, rd);
+    kb_project<kBlock, kFirst, true, kTPT, kTetMat><<<s->d.n_patches, kP / kTPT, 0, st>>>(s->d, s->cur, inv_dt2, rh,
+                                                                                          rd);
   else
-    kb_project<kBlock, kFirst, false, kTPT><<<s->d.n_patches, kP / kTPT, 0, st>>>(s->d, s->cur, inv_dt2, rh, rd);
+    kb_project<kBlock, kFirst, false, kTPT, kTetMat><<<s->d.n_patches, kP / kTPT, 0, st>>>(s->d, s->cur, inv_dt2,
+                                                                                           rh, rd);
+}
+
+template <bool kBlock, bool kFirst, int kTPT>
+void project_bt(Batch* s, float inv_dt2, cudaStream_t st) {
+  if (s->d.tinv_mu) project_btm<kBlock, kFirst, kTPT, true>(s, inv_dt2, st);
+  else project_btm<kBlock, kFirst, kTPT, false>(s, inv_dt2, st);
 }
 
 template <bool kBlock, bool kFirst>
@@ -489,20 +560,26 @@ void project_b(Batch* s, float inv_dt2, cudaStream_t st) {
   else project_bt<kBlock, kFirst, 1>(s, inv_dt2, st);
 }
 
-template <bool kRes, bool kMon>
-void residual_b(Batch* s, const BSweep& a, cudaStream_t st) {
+template <bool kRes, bool kMon, bool kTetMat>
+void residual_bm(Batch* s, const BSweep& a, cudaStream_t st) {
   const bool two = batch_tpt(s->prm) == 2;
   const int ctas = two ? s->res_ctas2 : s->res_ctas;
   const int chunk = (s->d.n_patches + ctas - 1) / ctas;
   const int grid = (s->d.n_patches + chunk - 1) / chunk;
   const bool pr = s->prm.precise_hydro != 0;
   if (two) {
-    if (pr) kb_residual<kRes, kMon, true, 2><<<grid, kP / 2, 0, st>>>(s->d, a, chunk);
-    else kb_residual<kRes, kMon, false, 2><<<grid, kP / 2, 0, st>>>(s->d, a, chunk);
+    if (pr) kb_residual<kRes, kMon, true, 2, kTetMat><<<grid, kP / 2, 0, st>>>(s->d, a, chunk);
+    else kb_residual<kRes, kMon, false, 2, kTetMat><<<grid, kP / 2, 0, st>>>(s->d, a, chunk);
   } else {
-    if (pr) kb_residual<kRes, kMon, true, 1><<<grid, kP, 0, st>>>(s->d, a, chunk);
-    else kb_residual<kRes, kMon, false, 1><<<grid, kP, 0, st>>>(s->d, a, chunk);
+    if (pr) kb_residual<kRes, kMon, true, 1, kTetMat><<<grid, kP, 0, st>>>(s->d, a, chunk);
+    else kb_residual<kRes, kMon, false, 1, kTetMat><<<grid, kP, 0, st>>>(s->d, a, chunk);
   }
+}
+
+template <bool kRes, bool kMon>
+void residual_b(Batch* s, const BSweep& a, cudaStream_t st) {
+  if (s->d.tinv_mu && kRes) residual_bm<kRes, kMon, true>(s, a, st);
+  else residual_bm<kRes, kMon, false>(s, a, st);
 }
 
 void iteration_b(Batch* s, int it, float dt, int rec, cudaStream_t st) {
@@ -603,6 +680,8 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
       !body->patch_ntets || !body->vblock_body || !body->body_inv_mu || !body->body_inv_lambda ||
       !body->body_n_patches || !body->body_n_tets || !body->vert_perm)
     return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL batch buffer");
+  if ((body->tet_inv_mu == nullptr) != (body->tet_inv_lambda == nullptr))
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "per-tet materials need both tet_inv_mu and tet_inv_lambda");
   if (max_records < 0) return bfail(XPBD_ERR_INVALID_ARGUMENT, "max_records < 0");
   Batch* s = new (std::nothrow) Batch();
   if (!s) return bfail(XPBD_ERR_INVALID_ARGUMENT, "out of host memory");
@@ -632,6 +711,8 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
   d.vblock_body = body->vblock_body;
   d.inv_mu = body->body_inv_mu;
   d.inv_la = body->body_inv_lambda;
+  d.tinv_mu = body->tet_inv_mu;
+  d.tinv_la = body->tet_inv_mu ? body->tet_inv_lambda : nullptr;
   d.body_patches = body->body_n_patches;
   d.body_tets = body->body_n_tets;
   d.perm = body->vert_perm;
@@ -669,12 +750,12 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
     int dev = 0, sms = 0, bps = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kb_residual<true, false, true, 1>, kP, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kb_residual<true, false, true, 1, false>, kP, 0) != cudaSuccess ||
         bps < 1)
       bps = 2;
     s->res_ctas = sms * bps > 0 ? sms * bps : 1;
     bps = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kb_residual<true, false, true, 2>, kP / 2, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kb_residual<true, false, true, 2, false>, kP / 2, 0) !=
             cudaSuccess ||
         bps < 1)
       bps = 4;
@@ -837,6 +918,107 @@ int xpbd_batch_read_profile(void* h, double* ms, int64_t* launches, int32_t n, i
       s->prof_ms[k] = 0.0;
       s->prof_n[k] = 0;
     }
+  return XPBD_OK;
+}
+
+
+int xpbd_batch_set_params(void* h, const xpbd_params* params) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !params) return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or params");
+  if (params->constraints_iter < 0 || params->cheb_warmup < 0)
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "constraints_iter and cheb_warmup must be >= 0");
+  if (std::memcmp(&s->prm, params, sizeof(xpbd_params)) != 0) drop_b(s);
+  s->prm = *params;
+  return XPBD_OK;
+}
+
+int xpbd_batch_save_rho_hat(void* h, double* dst_device, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !dst_device) return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or destination");
+  kb_rho_copy<<<nblk(s->d.n_bodies), 256, 0, BS(stream)>>>(s->d, dst_device, nullptr);
+  B_CUDA(cudaGetLastError());
+  return XPBD_OK;
+}
+
+int xpbd_batch_load_rho_hat(void* h, const double* src_device, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !src_device) return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or source");
+  kb_rho_copy<<<nblk(s->d.n_bodies), 256, 0, BS(stream)>>>(s->d, nullptr, src_device);
+  B_CUDA(cudaGetLastError());
+  return XPBD_OK;
+}
+
+static int check_batch_diff(Batch* s) {
+  if (!s->prm.block_mode) return bfail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint supports block mode only");
+  if (s->prm.constraints_iter > s->d.max_records)
+    return bfail(XPBD_ERR_HISTORY_FULL, "history shorter than constraints_iter");
+  return XPBD_OK;
+}
+
+int xpbd_batch_substep_tape(void* h, float dt, const xpbd_tape* tape, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !tape || !tape->xs || !tape->lams || !tape->xpre || !tape->v1)
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or tape buffer");
+  int r = check_batch_diff(s);
+  if (r) return r;
+  cudaStream_t st = BS(stream);
+  const int K = s->prm.constraints_iter, V = s->d.V, T = s->d.T;
+  Tape tp{reinterpret_cast<float4*>(tape->xs), reinterpret_cast<float2*>(tape->lams),
+          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1)};
+  const float* g = s->prm.gravity;
+  k_tape_begin<BDev><<<nblk(V), 256, 0, st>>>(s->d, tp, dt, g[0], g[1], g[2]);
+  s->cur = 0;
+  kb_begin<<<nblk(V), 256, 0, st>>>(s->d, dt, g[0], g[1], g[2]);
+  for (int it = 0; it < K; ++it) {
+    B_CUDA(cudaMemcpyAsync(tp.xs + (size_t)it * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
+    if (it == 0) B_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
+    else
+      B_CUDA(cudaMemcpyAsync(tp.lams + (size_t)it * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
+    iteration_b(s, it, dt, it, st);
+  }
+  B_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
+  kb_end<<<nblk(V), 256, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
+  B_CUDA(cudaGetLastError());
+  return XPBD_OK;
+}
+
+int xpbd_batch_substep_adjoint(void* h, float dt, const xpbd_tape* tape, const xpbd_adjoint* adj, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !tape || !adj || !adj->gx || !adj->gv || !adj->g_inv_mu || !adj->g_inv_lambda || !adj->work0 ||
+      !adj->work1 || !adj->ybar || !adj->dxbar || !adj->lambar || !adj->cnt)
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle, tape or adjoint buffer");
+  int r = check_batch_diff(s);
+  if (r) return r;
+  cudaStream_t st = BS(stream);
+  const int K = s->prm.constraints_iter, V = s->d.V, T = s->d.T;
+  Tape tp{reinterpret_cast<float4*>(tape->xs), reinterpret_cast<float2*>(tape->lams),
+          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1)};
+  Adj a;
+  a.gx = reinterpret_cast<float4*>(adj->gx);
+  a.gv = reinterpret_cast<float4*>(adj->gv);
+  a.g_mu = adj->g_inv_mu;
+  a.g_la = adj->g_inv_lambda;
+  a.abuf[0] = reinterpret_cast<float4*>(adj->work0);
+  a.abuf[1] = reinterpret_cast<float4*>(adj->work1);
+  a.ybar = reinterpret_cast<float4*>(adj->ybar);
+  a.dxbar = reinterpret_cast<float4*>(adj->dxbar);
+  a.lambar = reinterpret_cast<float2*>(adj->lambar);
+  a.cnt = adj->cnt;
+  B_CUDA(cudaMemsetAsync(a.lambar, 0, sizeof(float2) * T, st));
+  const float e_over_dt = expf(-dt * s->prm.damping) / dt;
+  ka_end<BDev><<<nblk(V), 256, 0, st>>>(s->d, a, e_over_dt);
+  const float c = (float)(1.0 / ((double)dt * (double)dt));
+  int src = 0;
+  const int g = (T + 127) / 128;
+  for (int k = K - 1; k >= 0; --k) {
+    if (s->prm.cheb_enable) ka_cheb<BDev, true><<<nblk(V), 256, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
+    else ka_cheb<BDev, false><<<nblk(V), 256, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
+    if (s->prm.precise_hydro) ka_project<BDev, true><<<g, 128, 0, st>>>(s->d, tp, a, k, c, c, src ^ 1);
+    else ka_project<BDev, false><<<g, 128, 0, st>>>(s->d, tp, a, k, c, c, src ^ 1);
+    src ^= 1;
+  }
+  ka_begin<BDev><<<nblk(V), 256, 0, st>>>(s->d, tp, a, src, dt);
+  B_CUDA(cudaGetLastError());
   return XPBD_OK;
 }
 

@@ -344,11 +344,14 @@ __host__ __device__ constexpr int project_min_blocks(int tpt) { return tpt == 2 
 // A chain of kTPT tets sharing s corners per step issues 4 + (kTPT - 1)(4 - s)
 // reductions instead of 4 kTPT.  cD, cH: time-scaled inverse Lame parameters;
 // the tet's compliances are 6 det(inv_Dm) cD and 6 det(inv_Dm) cH (1 / V0).
-template <bool kBlockMode, bool kPrecise, int kTPT>
+// kTetMat: per-tet materials, the compliances are further multiplied by the
+// tet's 1 / mu and 1 / lambda (mD[k], mH[k]).
+template <bool kBlockMode, bool kPrecise, int kTPT, bool kTetMat = false>
 __device__ __forceinline__ void project_chain(const float4 (&A)[kTPT], const float4 (&B)[kTPT], const float (&C)[kTPT],
                                               const uint32_t (&lid)[kTPT], float2 (&L)[kTPT], float2* lam_out,
                                               int n, const float4* sp, const int* sg, float4* dx, float cD,
-                                              float cH, float relax_h, float relax_d) {
+                                              float cH, float relax_h, float relax_d, const float* mD = nullptr,
+                                              const float* mH = nullptr) {
   float4 acc[4];
   int hid[4] = {-1, -1, -1, -1};
 #pragma unroll
@@ -367,7 +370,11 @@ __device__ __forceinline__ void project_chain(const float4 (&A)[kTPT], const flo
     const float six_det = 6.f * det9(tt.dm);
     float3 dp[4];
     float cnt;
-    project_tet<kBlockMode, kPrecise>(tt, six_det * cD, six_det * cH, relax_h, relax_d, L[k], dp, cnt);
+    if (kTetMat)
+      project_tet<kBlockMode, kPrecise>(tt, six_det * (cD * mD[k]), six_det * (cH * mH[k]), relax_h, relax_d, L[k],
+                                        dp, cnt);
+    else
+      project_tet<kBlockMode, kPrecise>(tt, six_det * cD, six_det * cH, relax_h, relax_d, L[k], dp, cnt);
     lam_out[k] = L[k];
     float4 nacc[4];
 #pragma unroll

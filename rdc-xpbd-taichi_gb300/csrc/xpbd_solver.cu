@@ -1020,6 +1020,28 @@ __global__ void __launch_bounds__(kBlock) k_residual_noalloc(Dev d, float cD, fl
 
 }  // namespace xpbd
 
+namespace xpbd {
+
+// Accessors of the single-body layout for the adjoint kernels.
+__device__ __forceinline__ int adj_verts(const Dev& d) { return d.V; }
+__device__ __forceinline__ int adj_tets(const Dev& d) { return d.T; }
+__device__ __forceinline__ float adj_omega(const Dev& d, int, int k) { return (float)d.hist[4 * k + 1]; }
+__device__ __forceinline__ bool adj_load_tet(const Dev& d, int t, int (&vid)[4], Tet& tt, float& inv_v0, float& m_mu,
+                                             float& m_la) {
+  int4 id;
+  load_tet(d, t, id, tt);
+  vid[0] = id.x;
+  vid[1] = id.y;
+  vid[2] = id.z;
+  vid[3] = id.w;
+  inv_v0 = 1.f / tt.V0;
+  m_mu = d.tinv_mu ? __ldg(d.tinv_mu + t) : 1.f;
+  m_la = d.tinv_mu ? __ldg(d.tinv_la + t) : 1.f;
+  return true;
+}
+
+}  // namespace xpbd
+
 #include "xpbd_adjoint.cuh"
 
 // ===========================================================================
@@ -1869,7 +1891,7 @@ int xpbd_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* strea
   Tape tp{reinterpret_cast<float4*>(tape->xs), reinterpret_cast<float2*>(tape->lams),
           reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1)};
   const float* g = s->prm.gravity;
-  k_tape_begin<<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, dt, g[0], g[1], g[2]);
+  k_tape_begin<Dev><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, dt, g[0], g[1], g[2]);
   s->cur = 0;
   launch_begin(s, true, true, dt, st);
   for (int it = 0; it < K; ++it) {
@@ -1909,19 +1931,19 @@ int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xp
   a.cnt = adj->cnt;
   XPBD_CUDA(cudaMemsetAsync(a.lambar, 0, sizeof(float2) * T, st));
   const float e_over_dt = expf(-dt * s->prm.damping) / dt;
-  ka_end<<<blocks_for(V), kBlock, 0, st>>>(s->d, a, e_over_dt);
+  ka_end<Dev><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, e_over_dt);
   float cD, cH;
   compliance_factors(s, dt, cD, cH);
   int src = 0;
   for (int k = K - 1; k >= 0; --k) {
-    if (s->prm.cheb_enable) ka_cheb<true><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
-    else ka_cheb<false><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
+    if (s->prm.cheb_enable) ka_cheb<Dev, true><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
+    else ka_cheb<Dev, false><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
     const int g = (T + 127) / 128;
-    if (s->prm.precise_hydro) ka_project<true><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
-    else ka_project<false><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
+    if (s->prm.precise_hydro) ka_project<Dev, true><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
+    else ka_project<Dev, false><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
     src ^= 1;
   }
-  ka_begin<<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, src, dt);
+  ka_begin<Dev><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, src, dt);
   XPBD_CUDA(cudaGetLastError());
   return XPBD_OK;
 }

@@ -80,7 +80,8 @@ class XpbdBatch(ctypes.Structure):
                 ("dm_a", _P), ("dm_b", _P), ("dm_c", _P), ("lam", _P), ("tet_lid", _P),
                 ("patch_voff", _P), ("patch_verts", _P), ("patch_body", _P), ("patch_ntets", _P),
                 ("vblock_body", _P), ("body_inv_mu", _P), ("body_inv_lambda", _P),
-                ("body_n_patches", _P), ("body_n_tets", _P), ("vert_perm", _P)]
+                ("body_n_patches", _P), ("body_n_tets", _P), ("vert_perm", _P),
+                ("tet_inv_mu", _P), ("tet_inv_lambda", _P)]
 
 
 class XpbdTape(ctypes.Structure):
@@ -143,6 +144,12 @@ _SIGNATURES = {
     "xpbd_batch_set_profiling": (ctypes.c_int, [_P, ctypes.c_int32]),
     "xpbd_batch_read_profile": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
                                                ctypes.c_int32, ctypes.c_int32, _P]),
+    "xpbd_batch_set_params": (ctypes.c_int, [_P, ctypes.POINTER(XpbdParams)]),
+    "xpbd_batch_save_rho_hat": (ctypes.c_int, [_P, _P, _P]),
+    "xpbd_batch_load_rho_hat": (ctypes.c_int, [_P, _P, _P]),
+    "xpbd_batch_substep_tape": (ctypes.c_int, [_P, ctypes.c_float, ctypes.POINTER(XpbdTape), _P]),
+    "xpbd_batch_substep_adjoint": (ctypes.c_int, [_P, ctypes.c_float, ctypes.POINTER(XpbdTape),
+                                                  ctypes.POINTER(XpbdAdjoint), _P]),
     "xpbd_build_patch_csr": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
     "xpbd_build_patches": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P,
                                           ctypes.POINTER(ctypes.c_int32)]),

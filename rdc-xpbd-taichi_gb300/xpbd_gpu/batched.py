@@ -26,7 +26,9 @@ PATCH = 256
 
 @dataclass
 class Body:
-    """One body of a batch.  ``rotation`` (3x3) is applied before ``scale`` and ``offset``."""
+    """One body of a batch.  ``rotation`` (3x3) is applied before ``scale`` and ``offset``.
+    ``tet_young_modulus`` / ``tet_poisson_ratio`` (file tet order) give per-tet
+    materials; a batch uses them for every body once any body has them."""
 
     rest_pose: object
     young_modulus: float = 200000.0
@@ -36,6 +38,8 @@ class Body:
     rotation: np.ndarray = None
     total_mass: float = 1.0
     density: float = None
+    tet_young_modulus: np.ndarray = None
+    tet_poisson_ratio: np.ndarray = None
 
 
 def _pad(n, m=PATCH):
@@ -46,7 +50,8 @@ class XPBDBatchedSolver:
     def __init__(self, bodies, sdf, frame_dt=1e-2, dt=1e-2, substeps_num=20, constraints_iter=5,
                  hydrostatic_relaxation=1.2, deviatoric_relaxation=1.2, cheb_enable=True, cheb_warmup=5,
                  cheb_gamma=0.6666, block_neohookean_enable=True, monitor_convergence=False,
-                 gravity=(0.0, -9.8, 0.0), precise_hydro=None, use_graph=True, tets_per_thread=2):
+                 gravity=(0.0, -9.8, 0.0), precise_hydro=None, use_graph=True, tets_per_thread=2,
+                 autotune_cache=True):
         if isinstance(sdf, (list, tuple)):
             self.sdfs = [s for s in sdf if s is not None]
         else:
@@ -72,13 +77,19 @@ class XPBDBatchedSolver:
         nus = [b.poisson_ratio for b in self.bodies]
         self.precise_hydro = (max(nus) >= 0.49) if precise_hydro is None else bool(precise_hydro)
         self.use_graph = bool(use_graph)
-        if tets_per_thread not in (1, 2):
-            raise ValueError("tets_per_thread must be 1 or 2")
-        self.tets_per_thread = int(tets_per_thread)
+        if tets_per_thread not in (1, 2, "auto"):
+            raise ValueError("tets_per_thread must be 1, 2 or 'auto'")
+        self.tets_per_thread = 2 if tets_per_thread == "auto" else int(tets_per_thread)
+        self.per_tet_materials = any(b.tet_young_modulus is not None for b in self.bodies)
         self.time = 0.0
         self.current_frame = 0
         self._handle = None
         self._build()
+        self.autotune_result = None
+        if tets_per_thread == "auto":
+            from xpbd_gpu import autotune
+            self.autotune_result = autotune.tune_batch(self, cache=autotune_cache)
+            self.set_tets_per_thread(self.autotune_result["tets_per_thread"])
 
     # -- setup ------------------------------------------------------------------
     def _prepare_body(self, b):
@@ -126,9 +137,20 @@ class XPBDBatchedSolver:
             raise ValueError("a 256-tet patch of this body touches more than 256 vertices")
         lame_mu = calc_second_lame(b.young_modulus, b.poisson_ratio)
         lame_la = calc_first_lame(b.young_modulus, b.poisson_ratio)
+        if b.tet_young_modulus is not None:
+            tE = np.asarray(b.tet_young_modulus, dtype=np.float64).reshape(-1)
+            if tE.shape != (T,):
+                raise ValueError("tet_young_modulus must have one entry per tet")
+            tnu = b.poisson_ratio if b.tet_poisson_ratio is None else b.tet_poisson_ratio
+            tnu = np.broadcast_to(np.asarray(tnu, dtype=np.float64), tE.shape)
+        else:
+            tE = np.full(T, float(b.young_modulus))
+            tnu = np.full(T, float(b.poisson_ratio))
+        # valence (constraints per vertex in block mode), solver vertex order
+        cnt = np.bincount(tets_s.reshape(-1), minlength=V).astype(np.float32)
         return dict(x=x, V0=V0, inv_Dm=inv_Dm, m=m, inv_m=inv_m, vperm=vperm, tperm=tperm, T=T, V=V, npat=npat,
-                    voff=voff, pverts=pverts[:voff[-1]], lid=lid, mu=lame_mu, la=lame_la,
-                    indices=tets[:, np.array([[0, 2, 1], [0, 3, 2], [0, 1, 3], [1, 2, 3]])].reshape(-1))
+                    voff=voff, pverts=pverts[:voff[-1]], lid=lid, mu=lame_mu, la=lame_la, tet_E=tE, tet_nu=tnu,
+                    cnt=cnt, indices=tets[:, np.array([[0, 2, 1], [0, 3, 2], [0, 1, 3], [1, 2, 3]])].reshape(-1))
 
     def _build(self):
         torch = _torch()
@@ -191,6 +213,21 @@ class XPBDBatchedSolver:
         self._body_patches = T_(np.array([p["npat"] for p in preps]), torch.int32)
         self._body_tets = T_(np.array([p["T"] for p in preps]), torch.int32)
         self._perm = T_(perm, torch.int32)
+        # tet slot of every caller tet (body order, then file order) and vertex valence
+        slot = np.concatenate([toffs[k] + np.argsort(p["tperm"]) for k, p in enumerate(preps)]).astype(np.int64)
+        self._tet_slot = torch.from_numpy(slot).to(dev)
+        cnt = np.zeros(Vt, dtype=np.float32)
+        for k, p in enumerate(preps):
+            cnt[voffs[k]:voffs[k] + p["V"]] = p["cnt"]
+        self._cnt = T_(cnt)
+        self._vert_slot = torch.from_numpy(
+            np.concatenate([voffs[k] + np.argsort(p["vperm"]) for k, p in enumerate(preps)]).astype(np.int64)).to(dev)
+        self._tinv_mu = self._tinv_la = None
+        if self.per_tet_materials:
+            self._tinv_mu = torch.ones(Tt, dtype=torch.float32, device=dev)
+            self._tinv_la = torch.ones(Tt, dtype=torch.float32, device=dev)
+            self.set_tet_materials(np.log(np.concatenate([p["tet_E"] for p in preps])),
+                                   np.concatenate([p["tet_nu"] for p in preps]))
         self.n_bodies, self.n_verts_padded, self.n_tets_padded, self.n_patches = nb, Vt, Tt, NP
         self.n_verts = int(outoffs[-1])
         self.n_tets = int(sum(p["T"] for p in preps))
@@ -213,6 +250,8 @@ class XPBDBatchedSolver:
         b.body_inv_mu, b.body_inv_lambda = self._inv_mu.data_ptr(), self._inv_la.data_ptr()
         b.body_n_patches, b.body_n_tets = self._body_patches.data_ptr(), self._body_tets.data_ptr()
         b.vert_perm = self._perm.data_ptr()
+        if self._tinv_mu is not None:
+            b.tet_inv_mu, b.tet_inv_lambda = self._tinv_mu.data_ptr(), self._tinv_la.data_ptr()
         self._max_records = max(1, len(frame_chunks(self.frame_dt, self.dt)) * self.substeps_num
                                 * self.constraints_iter)
         table = (_native.XpbdSdf * len(self.sdfs))()
@@ -222,6 +261,19 @@ class XPBDBatchedSolver:
         _native.check(self._lib.xpbd_batch_create(self._params(), b, table, len(self.sdfs), self._max_records,
                                                   _native.ctypes.byref(h)), batch=True)
         self._handle = h.value
+
+    def set_tet_materials(self, log_E, nu):
+        """Per-tet log Young's modulus and Poisson ratio of every body (numpy or
+        torch; all bodies' tets in body order, each body in file order; nu may be
+        a scalar).  Uploads 1/mu and 1/lambda into the tet slots."""
+        torch = _torch()
+        if self._tinv_mu is None:
+            raise RuntimeError("the batch was built without per-tet materials")
+        le = torch.as_tensor(log_E, dtype=torch.float64, device=self._device).reshape(-1)
+        nu_t = torch.as_tensor(nu, dtype=torch.float64, device=self._device).reshape(-1).expand(le.shape[0])
+        E = torch.exp(le)
+        self._tinv_mu[self._tet_slot] = (2.0 * (1.0 + nu_t) / E).to(torch.float32)
+        self._tinv_la[self._tet_slot] = ((1.0 + nu_t) * (1.0 - 2.0 * nu_t) / (E * nu_t)).to(torch.float32)
 
     def _params(self):
         p = _native.XpbdParams()
@@ -304,6 +356,48 @@ class XPBDBatchedSolver:
 
     def check_status(self):
         _native.check(self._lib.xpbd_batch_check_status(self._handle, self._stream()), batch=True)
+
+    # -- in-place tuning support ---------------------------------------------------
+    def set_tets_per_thread(self, tpt):
+        if tpt not in (1, 2):
+            raise ValueError("tets_per_thread must be 1 or 2")
+        self.tets_per_thread = int(tpt)
+        _native.check(self._lib.xpbd_batch_set_params(self._handle, self._params()), batch=True)
+
+    def snapshot(self):
+        """Device copies of the whole mutable state (positions, velocities,
+        predicted positions, Jacobi accumulator, multipliers, rho_hat)."""
+        torch = _torch()
+        rho = torch.empty(self.n_bodies, dtype=torch.float64, device=self._device)
+        _native.check(self._lib.xpbd_batch_save_rho_hat(self._handle, rho.data_ptr(), self._stream()), batch=True)
+        return dict(x=self._x4.clone(), v=self._v4.clone(), p0=self._p4[0].clone(), p1=self._p4[1].clone(),
+                    dx=self._dx4.clone(), lam=self._lam.clone(), rho=rho)
+
+    def restore(self, snap):
+        self._x4.copy_(snap["x"])
+        self._v4.copy_(snap["v"])
+        self._p4[0].copy_(snap["p0"])
+        self._p4[1].copy_(snap["p1"])
+        self._dx4.copy_(snap["dx"])
+        self._lam.copy_(snap["lam"])
+        _native.check(self._lib.xpbd_batch_load_rho_hat(self._handle, snap["rho"].data_ptr(), self._stream()),
+                      batch=True)
+
+    def time_substeps(self, sub_dt, warmup, reps):
+        """ms per substep over `reps` replays of a one-substep frame graph."""
+        torch = _torch()
+        lib, h, st = self._lib, self._handle, self._stream()
+        for _ in range(max(1, warmup)):
+            _native.check(lib.xpbd_batch_solve(h, float(sub_dt), float(sub_dt), 1, st), batch=True)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            _native.check(lib.xpbd_batch_solve(h, float(sub_dt), float(sub_dt), 1, st), batch=True)
+        b.record()
+        b.synchronize()
+        self.check_status()
+        return a.elapsed_time(b) / reps
 
     def set_profiling(self, enable):
         _native.check(self._lib.xpbd_batch_set_profiling(self._handle, 1 if enable else 0), batch=True)

@@ -150,3 +150,143 @@ def xpbd_simulate(sim, x0, v0, log_E, nu, frames):
     """Final positions (V, 3) after `frames` frames from (x0, v0) with per-tet
     log E and nu; differentiable w.r.t. all four tensors."""
     return _Simulate.apply(x0, v0, log_E, nu, sim, frames)
+
+
+def _lame_inverse_grads(gmu, gla, log_E, nu):
+    """d/d(1/mu), d/d(1/lambda) -> d/dlog E, d/dnu (float64 tensors, per tet)."""
+    torch = _torch()
+    E = torch.exp(log_E.detach().to(torch.float64))
+    n = nu.detach().to(torch.float64).expand_as(E)
+    inv_mu = 2.0 * (1.0 + n) / E
+    inv_la = (1.0 + n) * (1.0 - 2.0 * n) / (E * n)
+    g_logE = -(gmu * inv_mu + gla * inv_la)
+    g_nu = gmu * 2.0 / E + gla * (-1.0 - 2.0 * n * n) / (n * n * E)
+    return g_logE, g_nu
+
+
+class BatchedDiffSim:
+    """A batch of bodies (``XPBDBatchedSolver``) with per-tet materials and the
+    buffers of its adjoint.  Forward and adjoint of a substep are each one
+    launch per phase over the tets or vertices of all bodies; every body keeps
+    its own Chebyshev state, so the gradients of each body equal those of the
+    same body simulated alone."""
+
+    def __init__(self, bodies, sdf, **kw):
+        from xpbd_gpu.batched import Body, XPBDBatchedSolver
+        kw.setdefault("block_neohookean_enable", True)
+        if not kw["block_neohookean_enable"]:
+            raise ValueError("the adjoint supports the block projection only")
+        bodies = [b if b.tet_young_modulus is not None else
+                  Body(**dict(b.__dict__, tet_young_modulus=np.full(_n_tets(b.rest_pose), b.young_modulus)))
+                  for b in bodies]
+        self.batch = XPBDBatchedSolver(bodies, sdf, **kw)
+        s = self.batch
+        torch = _torch()
+        dev = s._device
+        V, T, K = s.n_verts_padded, s.n_tets_padded, s.constraints_iter
+        self.V, self.T, self.K = V, T, K
+        self.n_verts, self.n_tets = s.n_verts, s.n_tets
+        f4 = lambda n: torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        self._xs = torch.zeros(((K + 1) * V, 4), dtype=torch.float32, device=dev)
+        self._lams = torch.zeros((max(K, 1) * T, 2), dtype=torch.float32, device=dev)
+        self._xpre, self._v1 = f4(V), f4(V)
+        self._gx, self._gv = f4(V), f4(V)
+        self._w0, self._w1, self._yb, self._dxb = f4(V), f4(V), f4(V), f4(V)
+        self._lamb = torch.zeros((T, 2), dtype=torch.float32, device=dev)
+        self._gmu = torch.zeros(T, dtype=torch.float64, device=dev)
+        self._gla = torch.zeros(T, dtype=torch.float64, device=dev)
+        self.tape = _native.XpbdTape(self._xs.data_ptr(), self._lams.data_ptr(), self._xpre.data_ptr(),
+                                     self._v1.data_ptr())
+        self.adj = _native.XpbdAdjoint(self._gx.data_ptr(), self._gv.data_ptr(), self._gmu.data_ptr(),
+                                       self._gla.data_ptr(), self._w0.data_ptr(), self._w1.data_ptr(),
+                                       self._yb.data_ptr(), self._dxb.data_ptr(), self._lamb.data_ptr(),
+                                       s._cnt.data_ptr())
+        self.initial_rho_hat = torch.empty(s.n_bodies, dtype=torch.float64, device=dev)
+        self.rho_copy_to(self.initial_rho_hat)
+
+    def rho_copy_to(self, dst):
+        s = self.batch
+        _native.check(s._lib.xpbd_batch_save_rho_hat(s._handle, dst.data_ptr(), s._stream()), batch=True)
+
+    def rho_load_from(self, src):
+        s = self.batch
+        _native.check(s._lib.xpbd_batch_load_rho_hat(s._handle, src.data_ptr(), s._stream()), batch=True)
+
+    def substep_dts(self, frames):
+        s = self.batch
+        out = []
+        for _ in range(frames):
+            for d in frame_chunks(s.frame_dt, s.dt):
+                out.extend([d / s.substeps_num] * s.substeps_num)
+        return out
+
+    def set_state(self, x, v):
+        """x, v: (n_verts, 3) of all bodies in body order, each in file order."""
+        s = self.batch
+        s._x4[s._vert_slot, :3] = x.to(s._x4)
+        s._v4[s._vert_slot, :3] = v.to(s._v4)
+
+    def positions(self):
+        s = self.batch
+        return s._x4[s._vert_slot, :3].clone()
+
+
+def _n_tets(rest_pose):
+    from xpbd_gpu.xpbd_base import load_rest_pose
+    return load_rest_pose(rest_pose).n_tets
+
+
+class _SimulateBatch(_torch().autograd.Function):
+    @staticmethod
+    def forward(ctx, x0, v0, log_E, nu, sim, frames):
+        torch = _torch()
+        s = sim.batch
+        lib, stream = s._lib, s._stream()
+        s.set_tet_materials(log_E.detach(), nu.detach())
+        sim.set_state(x0.detach(), v0.detach())
+        sim.rho_load_from(sim.initial_rho_hat)
+        dts = sim.substep_dts(frames)
+        ckpts = []
+        rho = torch.empty((len(dts), s.n_bodies), dtype=torch.float64, device=s._device)
+        for k, dt in enumerate(dts):
+            sim.rho_copy_to(rho[k])
+            ckpts.append((s._x4.clone(), s._v4.clone(), rho[k]))
+            _native.check(lib.xpbd_batch_substep(s._handle, float(dt), 0, stream), batch=True)
+        ctx.sim, ctx.dts, ctx.ckpts = sim, dts, ckpts
+        ctx.save_for_backward(log_E, nu)
+        return sim.positions()
+
+    @staticmethod
+    def backward(ctx, g_out):
+        torch = _torch()
+        sim, dts, ckpts = ctx.sim, ctx.dts, ctx.ckpts
+        log_E, nu = ctx.saved_tensors
+        s = sim.batch
+        lib, stream = s._lib, s._stream()
+        sim._gx.zero_()
+        sim._gv.zero_()
+        sim._gx[s._vert_slot, :3] = g_out.to(torch.float32)
+        sim._gmu.zero_()
+        sim._gla.zero_()
+        for dt, (x4, v4, rho) in zip(reversed(dts), reversed(ckpts)):
+            s._x4.copy_(x4)
+            s._v4.copy_(v4)
+            sim.rho_load_from(rho)
+            _native.check(lib.xpbd_batch_substep_tape(s._handle, float(dt), sim.tape, stream), batch=True)
+            _native.check(lib.xpbd_batch_substep_adjoint(s._handle, float(dt), sim.tape, sim.adj, stream),
+                          batch=True)
+        gx = sim._gx[s._vert_slot, :3].clone()
+        gv = sim._gv[s._vert_slot, :3].clone()
+        gmu = sim._gmu[s._tet_slot]
+        gla = sim._gla[s._tet_slot]
+        g_logE, g_nu = _lame_inverse_grads(gmu, gla, log_E, nu)
+        if nu.numel() == 1:
+            g_nu = g_nu.sum().reshape(nu.shape)
+        return (gx.to(g_out.dtype), gv.to(g_out.dtype), g_logE.to(log_E.dtype), g_nu.to(nu.dtype), None, None)
+
+
+def xpbd_simulate_batch(sim, x0, v0, log_E, nu, frames):
+    """Final positions (n_verts, 3) of every body after `frames` frames from
+    (x0, v0) with per-tet log E and nu (all bodies' vertices and tets in body
+    order); differentiable w.r.t. all four tensors."""
+    return _SimulateBatch.apply(x0, v0, log_E, nu, sim, frames)

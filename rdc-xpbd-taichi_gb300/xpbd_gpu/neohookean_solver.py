@@ -19,7 +19,10 @@ Extensions (keyword-only): ``total_mass`` / ``density`` (the reference fixes
 1 kg, xpbd_base.py:36), ``gravity``, ``scatter`` ('atomic' = vector
 red.global.add, 'gather' = deterministic vertex->tet CSR), ``precise_hydro``
 (cancellation-free det F - 1; default on for poisson_ratio >= 0.49),
-``use_graph`` and ``reorder`` (Morton order on the device).
+``use_graph`` and ``reorder`` (Morton order on the device).  With
+``scatter="auto"`` the scatter variant, patch size, tets per thread and
+tile pipeline are measured on this mesh and GPU (``xpbd_gpu.autotune``) and
+the choice is kept in ``autotune_result``.
 """
 import numpy as np
 
@@ -56,8 +59,17 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
                  cheb_enable=True, cheb_warmup=5, cheb_gamma=0.6666, block_neohookean_enable=False,
                  monitor_convergence=False, *, total_mass=1.0, density=None, gravity=(0.0, -9.8, 0.0),
                  scatter="patch", precise_hydro=None, use_graph=True, reorder=True, sweep_order=1,
-                 patch_pipeline=0, patch_reduce=0, tets_per_thread=2, tet_young_modulus=None,
-                 tet_poisson_ratio=None):
+                 patch_pipeline=0, patch_reduce=0, tets_per_thread=2, patch_tets=256, tet_young_modulus=None,
+                 tet_poisson_ratio=None, autotune_cache=True):
+        self.autotune_result = None
+        if scatter == "auto":
+            from xpbd_gpu import autotune
+            args = {k: v for k, v in locals().items() if k not in ("self", "autotune", "__class__")}
+            args.pop("autotune_cache")
+            self.autotune_result = autotune.tune_single(type(self), args, cache=autotune_cache)
+            r = self.autotune_result
+            scatter, patch_tets = r["scatter"], r["patch_tets"]
+            tets_per_thread, patch_pipeline = r["tets_per_thread"], r["patch_pipeline"]
         self.constraints_iter = constraints_iter
         self.hydrostatic_relaxation = hydrostatic_relaxation
         self.deviatoric_relaxation = deviatoric_relaxation
@@ -90,6 +102,7 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         self.patch_pipeline = int(patch_pipeline)
         self.patch_reduce = int(patch_reduce)
         self.tets_per_thread = int(tets_per_thread)
+        self.patch_tets = int(patch_tets)
         # per-tet materials (file tet order); they need a per-tet scatter variant
         self._tet_E = None if tet_young_modulus is None else np.asarray(tet_young_modulus, dtype=np.float64)
         self._tet_nu = None

@@ -305,14 +305,15 @@ class XPBDSolverBase:
         self._corner = torch.zeros((4 * T, 4), dtype=torch.float32, device=self._device)
 
     def _ensure_patch_buffers(self):
-        """Patches of P Morton-consecutive tets with <= 256 vertices each
-        (P = 256, else 128, else 64); returns False if no P fits."""
+        """Patches of P Morton-consecutive tets with <= 256 vertices each (P =
+        the largest of 256, 128, 64 not above ``patch_tets`` whose patches all
+        fit); returns False if none fits."""
         if self._tet_lid is not None:
             return True
         torch = _torch()
         V, T = self.n_verts, self.n_tets
         tt = np.ascontiguousarray(self._tets_solver)
-        for P in (256, 128, 64):
+        for P in (p for p in (256, 128, 64) if p <= getattr(self, "patch_tets", 256)):
             npat = (T + P - 1) // P
             voff = np.empty(npat + 1, dtype=np.int32)
             pverts = np.empty(4 * T, dtype=np.int32)
