@@ -384,7 +384,8 @@ def run_c3(args):
     torch.cuda.set_device(0)
     bodies, specs, kw, desc = workload_c3()
     units = sum(b.rest_pose.n_tets for b in bodies) * kw["substeps_num"] * kw["constraints_iter"]
-    batch = XPBDBatchedSolver(bodies, product_sdfs(specs), tets_per_thread=min(args.tets_per_thread, 2), **kw)
+    btpt = "auto" if args.batch_tpt == "auto" else int(args.batch_tpt)
+    batch = XPBDBatchedSolver(bodies, product_sdfs(specs), tets_per_thread=btpt, **kw)
     plain = []
     for b in bodies:
         mesh = TetMesh(b.rest_pose.points @ b.rotation.T, b.rest_pose.tets)
@@ -433,6 +434,7 @@ def run_c3(args):
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak = float(json.load(open(peaks_path))["hbm_gbs"]) if os.path.exists(peaks_path) else 6800.0
     iter_bytes = 136.0 * T + 128.0 * V
+    conv = convergence_probe(batch, S, min(args.c3_conv_iters, batch._max_records))
     line = {
         "metric": METRIC, "value": units / (ms_batch * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak",
@@ -459,9 +461,47 @@ def run_c3(args):
                                "frac": iter_bytes * S * K / (ms_batch * 1e-3) / 1e9 / peak},
         "kernel_profile": {k: {"ms_per_launch": v["ms"] / max(1, v["launches"]), "launches": v["launches"]}
                            for k, v in prof.items() if v["launches"]},
+        "iterations_to_1e-3": conv,
         "clocks": clk_b,
     }
+    if batch.autotune_result is not None:
+        line["config"]["autotune"] = {"tets_per_thread": batch.tets_per_thread,
+                                      "cached": batch.autotune_result["cached"],
+                                      "ms_per_substep": {"tpt%d" % r["tets_per_thread"]: r["ms"]
+                                                         for r in batch.autotune_result["table"]}}
     print(json.dumps(line), flush=True)
+
+
+def convergence_probe(batch, substeps, k_max, target=1e-3, floor=1e-5):
+    """Iterations every body needs per substep to reach r_hat_k / r_hat_0 <= target: one frame re-run
+    substep by substep with k_max iterations, from the batch's current state (restored afterwards).
+    Both forms run the identical per-body algorithm, so the counts hold for the plain form too."""
+    from xpbd_gpu import _native
+    snap = batch.snapshot()
+    K0 = batch.constraints_iter
+    batch.constraints_iter = k_max
+    _native.check(batch._lib.xpbd_batch_set_params(batch._handle, batch._params()), batch=True)
+    need = []
+    sub_dt = float(batch.dt) / substeps
+    for _ in range(substeps):
+        _native.check(batch._lib.xpbd_batch_substep(batch._handle, sub_dt, 0, batch._stream()), batch=True)
+        r = batch.read_history(k_max)[:, :, 0]
+        for b in range(r.shape[0]):
+            if r[b, 0] <= floor:
+                continue  # free fall: residual at FP32 round-off
+            hit = np.nonzero(r[b] / r[b, 0] <= target)[0]
+            need.append(int(hit[0]) + 1 if len(hit) else -1)
+    batch.constraints_iter = K0
+    _native.check(batch._lib.xpbd_batch_set_params(batch._handle, batch._params()), batch=True)
+    batch.restore(snap)
+    need = np.asarray(need)
+    ok = need[need > 0]
+    return {"target": target, "max_iterations": k_max, "substeps_counted": int(len(need)),
+            "fraction_reached": float(len(ok) / max(1, len(need))),
+            "iterations_median": float(np.median(ok)) if len(ok) else None,
+            "iterations_p90": float(np.percentile(ok, 90)) if len(ok) else None,
+            "fraction_within_configured_iterations": float(np.mean((need > 0) & (need <= K0))) if len(need) else None,
+            "note": "bodies' substeps with r_hat_0 <= %g (free fall) excluded" % floor}
 
 
 def product_sdfs(specs):
@@ -486,9 +526,10 @@ def tet_iterations_per_frame(mesh, kw):
 # CPU baseline: the oracle on a bounded sample
 # ---------------------------------------------------------------------------
 
-def cpu_oracle(mesh, specs, kw, substeps, threads=None):
-    """The threaded FP32 C restatement of the reference substep on the workload's mesh,
-    stepping `substeps` substeps of the workload's substep length per call."""
+def cpu_oracle(mesh, specs, kw, substeps, threads=None, dtype=np.float32):
+    """The threaded C restatement of the reference substep on the workload's mesh (FP32, or FP64
+    for the float64 reference run), stepping `substeps` substeps of the workload's substep length
+    per call."""
     from oracle.xpbd_oracle import OracleSdf
     from oracle.xpbd_oracle_c import COracle
     sub_dt = kw["dt"] / kw["substeps_num"]
@@ -496,7 +537,35 @@ def cpu_oracle(mesh, specs, kw, substeps, threads=None):
     okw.update(substeps_num=substeps, frame_dt=sub_dt * substeps, dt=sub_dt * substeps)
     total = kw.get("density", 1.0) * float(np.abs(_volume(mesh)).sum()) if "density" in kw else 1.0
     return COracle(mesh.points, mesh.tets, [OracleSdf(k, **p) for k, p in specs], threads=threads,
-                   total_mass=total, **okw)
+                   total_mass=total, dtype=dtype, **okw)
+
+
+def fp64_error(solver_factory, mesh, specs, kw, frames):
+    """Error of a fresh GPU run against the float64 run of the reference algorithm (the C
+    restatement in FP64 on every host core) over `frames` frames: max and RMS vertex deviation
+    as fractions of the bounding-box diagonal, and the relative difference of the per-iteration
+    residual curves of the last frame."""
+    threads = os.cpu_count() or 1
+    solver = solver_factory()
+    S, K = kw["substeps_num"], kw["constraints_iter"]
+    ref = cpu_oracle(mesh, specs, kw, S, threads, dtype=np.float64)
+    diag = float(np.linalg.norm(mesh.points.max(0) - mesh.points.min(0)))
+    hist = np.zeros(S * K)
+    worst, t_ref = 0.0, 0.0
+    for _ in range(frames):
+        solver.solve()
+        t0 = time.perf_counter()
+        ref.solve(1, hist)
+        t_ref += time.perf_counter() - t0
+        d = np.abs(solver.mesh.verts.x.to_numpy().astype(np.float64) - ref.x)
+        worst = max(worst, float(d.max()))
+    rms = float(np.sqrt((d ** 2).sum(1).mean()))
+    r_gpu = solver.read_history()[:S * K, 0]
+    scale = max(float(np.abs(hist).max()), 1e-30)
+    return {"frames": frames, "max_dev_over_bbox_diag": worst / diag, "rms_dev_over_bbox_diag": rms / diag,
+            "tolerance": 1e-4, "residual_curve_max_rel_diff": float(np.max(np.abs(r_gpu - hist) /
+                                                                           (np.abs(hist) + 2e-4 * scale))),
+            "reference": "C restatement in FP64, %d threads, %.1f s per frame" % (threads, t_ref / frames)}
 
 
 def _volume(mesh):
@@ -629,12 +698,17 @@ def run_gb300(args):
     from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver, frame_chunks
 
     mesh, specs, kw, desc = workload(args.workload)
+    t_build = time.perf_counter()
     solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
                                   patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce,
                                   tets_per_thread=args.tets_per_thread, **kw)
+    t_build = time.perf_counter() - t_build
+    # the configuration that runs (the autotuner's pick with --scatter auto)
+    scatter, tpt, pipe = solver.scatter, solver.tets_per_thread, solver.patch_pipeline
+    patch_tets = solver._patch_tets if scatter == "patch" else 0
     frame_units = tet_iterations_per_frame(mesh, kw)
     n_chunks = len(frame_chunks(kw["frame_dt"], kw["dt"]))
-    per_substep = 2 + kw["constraints_iter"] * (3 + (1 if args.scatter == "gather" else 0))
+    per_substep = 2 + kw["constraints_iter"] * (3 + (1 if scatter == "gather" else 0))
     launches_per_frame = n_chunks * kw["substeps_num"] * per_substep
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
@@ -716,19 +790,23 @@ def run_gb300(args):
     proj_bytes = 72.0 * T + 32.0 * V
     proj_ms = prof["project"]["ms"] / max(1, n_proj)
     achieved = proj_bytes / (proj_ms * 1e-3) / 1e9
-    kernel_name = {"patch": ("k_project_patchN (tile, 256-tet patches, %d consecutive tets per thread, "
-                             "shared corners merged before red.global.add.v4)" % args.tets_per_thread
-                             if args.tets_per_thread > 1 and not args.patch_reduce and not args.patch_pipeline
-                             else "k_project_patch1 (tile, 256-tet patches, red.global.add.v4 per corner)"),
-                   "atomic": "k_project (one thread per tet, red.global.add.v4 per corner)",
-                   "gather": "k_project (per-corner buffer + deterministic vertex gather)"}[args.scatter]
+    if scatter == "patch" and pipe == 1 and patch_tets == 256:
+        kernel_name = "k_project_tile (persistent CTAs, cp.async.bulk tet records, 256-tet patches)"
+    elif scatter == "patch" and tpt > 1 and not args.patch_reduce:
+        kernel_name = ("k_project_patchN (tile, %d-tet patches, %d consecutive tets per thread, shared corners "
+                       "merged before red.global.add.v4)" % (patch_tets, tpt))
+    elif scatter == "patch":
+        kernel_name = "k_project_patch1 (tile, %d-tet patches, red.global.add.v4 per corner)" % patch_tets
+    else:
+        kernel_name = {"atomic": "k_project (one thread per tet, red.global.add.v4 per corner)",
+                       "gather": "k_project (per-corner buffer + deterministic vertex gather)"}[scatter]
     # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this
     # workload, from the ncu captures summarised in profiles/k_project_*_c2_64cube.md
     # (k_project_patchN for 2 tets per thread, k_project_patch1 for 1)
-    traffic = {("patch", 2): 88.98e6, ("patch", 1): 89.4e6}.get((args.scatter, args.tets_per_thread))
-    if args.scatter == "atomic":
+    traffic = {("patch", 2): 88.98e6, ("patch", 1): 89.4e6}.get((scatter, tpt))
+    if scatter == "atomic":
         traffic = 115.2e6
-    if args.patch_pipeline != 0 or args.patch_reduce != 0 or args.workload != "c2":
+    if pipe != 0 or args.patch_reduce != 0 or args.workload != "c2" or (scatter == "patch" and patch_tets != 256):
         traffic = None
     iter_bytes = 136.0 * T + 128.0 * V
     line = {
@@ -736,8 +814,9 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc, "step": "one frame (%d tet-iterations)" % frame_units,
-                   "scatter": args.scatter, "sweep_order": args.sweep_order,
-                   "patch_pipeline": args.patch_pipeline, "tets_per_thread": args.tets_per_thread, "l2": "flushed between steps (%d MiB write)" % (L2_FLUSH_BYTES >> 20),
+                   "scatter": scatter, "patch_tets": patch_tets, "sweep_order": args.sweep_order,
+                   "patch_pipeline": pipe, "tets_per_thread": tpt,
+                   "l2": "flushed between steps (%d MiB write)" % (L2_FLUSH_BYTES >> 20),
                    "parallelism": "replicas" if world > 1 else "single GPU", "graph": "one CUDA graph per frame"},
         "frames_per_s": 1e3 / ms_per_step * world,
         "gpu_launches": launches_per_frame * args.steps,
@@ -758,8 +837,21 @@ def run_gb300(args):
                 "h2d_bytes_per_step": 2 * V * 12, "d2h_bytes_per_step": V * 12, "ms_per_step": e2e_step},
         "clocks": clk.summary(),
     }
+    if solver.autotune_result is not None:
+        r = solver.autotune_result
+        line["config"]["autotune"] = {
+            "cached": r["cached"], "construction_s": t_build,
+            "ms_per_substep": {"%s/P%s/tpt%s/pipe%s" % (c["scatter"], c["patch_tets"], c["tets_per_thread"],
+                                                         c["patch_pipeline"]): c["ms"] for c in r["table"]}}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(mesh, specs, kw, substeps=args.cpu_substeps)
+    if args.fp64_frames > 0:
+        del solver
+        line["fp64_error"] = fp64_error(
+            lambda: XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=scatter, sweep_order=args.sweep_order,
+                                         patch_pipeline=pipe, patch_reduce=args.patch_reduce, tets_per_thread=tpt,
+                                         patch_tets=patch_tets or 256, **kw),
+            mesh, specs, kw, args.fp64_frames)
     print(json.dumps(line), flush=True)
 
 
@@ -778,8 +870,26 @@ def run_profile(args):
         batch.check_status()
         print("profile mode: %d frame(s) of %s (batched)" % (args.profile_frames, desc))
         return
+    if args.workload == "c5":  # batched forward + adjoint of `profile_frames` frames
+        from xpbd_gpu.batched import Body
+        from xpbd_gpu.differentiable import BatchedDiffSim, xpbd_simulate_batch
+        meshes, log_E, nus, specs, kw, desc = workload_c5()
+        bodies = [Body(m, tet_young_modulus=np.exp(log_E[k]), tet_poisson_ratio=nus[k], density=1000.0,
+                       poisson_ratio=float(nus[k])) for k, m in enumerate(meshes)]
+        sim = BatchedDiffSim(bodies, product_sdfs(specs), **kw)
+        dev = torch.device("cuda")
+        x0 = torch.tensor(np.concatenate([m.points for m in meshes]), dtype=torch.float32, device=dev)
+        le = torch.tensor(np.concatenate(log_E), dtype=torch.float64, device=dev, requires_grad=True)
+        nu = torch.tensor(np.concatenate([np.full(m.n_tets, nus[k]) for k, m in enumerate(meshes)]), device=dev)
+        xf = xpbd_simulate_batch(sim, x0, torch.zeros_like(x0), le, nu, args.profile_frames)
+        (xf ** 2).sum().backward()
+        torch.cuda.synchronize()
+        sim.batch.check_status()
+        print("profile mode: forward + adjoint of %d frame(s) of %s" % (args.profile_frames, desc))
+        return
     mesh, specs, kw, desc = workload(args.workload)
-    solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
+    scatter = "patch" if args.scatter == "auto" else args.scatter
+    solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=scatter, sweep_order=args.sweep_order,
                                   patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce,
                                   tets_per_thread=args.tets_per_thread, use_graph=False, **kw)
     for _ in range(args.profile_frames):
@@ -804,15 +914,18 @@ def main():
     ap.add_argument("--c4-reps", type=int, default=2)
     ap.add_argument("--c4-check-frames", type=int, default=1)
     ap.add_argument("--c4-check-start", type=int, default=20)
-    ap.add_argument("--scatter", default="patch", choices=["atomic", "gather", "patch"])
+    ap.add_argument("--scatter", default="auto", choices=["auto", "atomic", "gather", "patch"])
     ap.add_argument("--sweep-order", type=int, default=1, choices=[0, 1])
     ap.add_argument("--patch-pipeline", type=int, default=0, choices=[0, 1])
     ap.add_argument("--patch-reduce", type=int, default=0, choices=[0, 1])
     ap.add_argument("--tets-per-thread", type=int, default=2, choices=[1, 2, 4])
+    ap.add_argument("--batch-tpt", default="auto", choices=["auto", "1", "2"])
+    ap.add_argument("--c3-conv-iters", type=int, default=150)
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-substeps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-frames", type=int, default=1)
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     ap.add_argument("--profile-frames", type=int, default=1)
     args = ap.parse_args()

@@ -1,8 +1,10 @@
 """Build and run oracle/xpbd_oracle_c.c -- TEST INFRASTRUCTURE ONLY.
 
-The threaded FP32 C restatement of the reference substep, used as the timed
-CPU baseline and as a second checker.  Built with gcc into
-oracle/_build/liboracle_xpbd.so (no -march=native, no fast-math).
+The threaded C restatement of the reference substep: FP32 (the reference's
+arithmetic type) as the timed CPU baseline and a second checker, and FP64 as
+the float64 reference run of meshes too large for the NumPy oracle.  Built
+with gcc into oracle/_build/liboracle_xpbd.so and liboracle_xpbd64.so (no
+-march=native, no fast-math).
 """
 import ctypes
 import os
@@ -13,6 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "xpbd_oracle_c.c")
 LIB = os.path.join(HERE, "_build", "liboracle_xpbd.so")
+LIB64 = os.path.join(HERE, "_build", "liboracle_xpbd64.so")
 
 
 class OcSdf(ctypes.Structure):
@@ -28,48 +31,60 @@ class OcParams(ctypes.Structure):
                 ("rho_min", ctypes.c_double), ("rho_max", ctypes.c_double), ("rho_beta", ctypes.c_double)]
 
 
-def build(force=False):
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
-        return LIB
-    os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    tmp = LIB + ".tmp"
-    cmd = ["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread", "-o", tmp, SRC, "-lm"]
+def _build_one(lib, defines, force):
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= os.path.getmtime(SRC):
+        return lib
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
+    tmp = lib + ".tmp"
+    cmd = ["gcc", "-O3", "-std=c11", "-fPIC", "-shared", "-pthread"] + defines + ["-o", tmp, SRC, "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("gcc failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
-_lib = None
+def build(force=False):
+    """Build the FP32 and the FP64 library; returns the FP32 path."""
+    _build_one(LIB64, ["-DOC_DOUBLE"], force)
+    return _build_one(LIB, [], force)
 
 
-def load():
-    global _lib
-    if _lib is None:
-        lib = ctypes.CDLL(build())
+_libs = {}
+
+
+def load(double=False):
+    key = bool(double)
+    if key not in _libs:
+        build()
+        lib = ctypes.CDLL(LIB64 if key else LIB)
         lib.oc_run.restype = ctypes.c_int
         lib.oc_run.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6 + [
             ctypes.POINTER(OcSdf), ctypes.c_int, ctypes.POINTER(OcParams), ctypes.c_double, ctypes.c_double,
             ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p]
-        _lib = lib
-    return _lib
+        _libs[key] = lib
+    return _libs[key]
 
 
 class COracle:
     """Same constructor as oracle.xpbd_oracle.OracleSolver (setup computed by it in
-    float64), stepping frames with the C restatement in FP32."""
+    float64), stepping frames with the C restatement in `dtype` (np.float32, the
+    reference's arithmetic, or np.float64)."""
 
-    def __init__(self, points, tets, sdf, threads=None, **kw):
+    def __init__(self, points, tets, sdf, threads=None, dtype=np.float32, **kw):
         from oracle.xpbd_oracle import OracleSolver
         o = OracleSolver(points, tets, sdf, dtype=np.float64, **kw)
         self._o = o
-        self.x = o.x.astype(np.float32).copy()
-        self.v = o.v.astype(np.float32).copy()
+        self.dtype = np.dtype(dtype)
+        if self.dtype not in (np.float32, np.float64):
+            raise ValueError("dtype must be float32 or float64")
+        dt_ = self.dtype
+        self.x = o.x.astype(dt_).copy()
+        self.v = o.v.astype(dt_).copy()
         self.tets = np.ascontiguousarray(o.tets, dtype=np.int32)
-        self.inv_Dm = np.ascontiguousarray(o.inv_Dm.reshape(-1, 9), dtype=np.float32)
-        self.V0 = np.ascontiguousarray(o.V0, dtype=np.float32)
-        self.inv_m = np.ascontiguousarray(o.inv_m, dtype=np.float32)
+        self.inv_Dm = np.ascontiguousarray(o.inv_Dm.reshape(-1, 9), dtype=dt_)
+        self.V0 = np.ascontiguousarray(o.V0, dtype=dt_)
+        self.inv_m = np.ascontiguousarray(o.inv_m, dtype=dt_)
         self.rho_hat = ctypes.c_double(0.999)
         self.threads = threads or os.cpu_count() or 1
         self.sdfs = (OcSdf * len(o.sdfs))()
@@ -100,7 +115,7 @@ class COracle:
         buf = None
         if r_hat_hist is not None:
             buf = r_hat_hist.ctypes.data
-        rc = load().oc_run(len(self.x), len(self.tets), self.x.ctypes.data, self.v.ctypes.data,
+        rc = load(self.dtype == np.float64).oc_run(len(self.x), len(self.tets), self.x.ctypes.data, self.v.ctypes.data,
                            self.tets.ctypes.data, self.inv_Dm.ctypes.data, self.V0.ctypes.data,
                            self.inv_m.ctypes.data, self.sdfs, len(self.sdfs), ctypes.byref(self.p),
                            self.frame_dt, self.dt, self.substeps, frames, ctypes.byref(self.rho_hat),

@@ -23,7 +23,8 @@
 //   bool  adj_load_tet(const D&, int t, int vid[4], Tet&, float& inv_v0,
 //                      float& m_mu, float& m_la)   false for a padding slot;
 //         m_mu, m_la multiply the compliance factors (the tet's 1/mu and
-//         1/lambda with per-tet materials, else 1)
+//         1/lambda with per-tet materials, else 1); only ka_project needs it
+//         (a layout with its own tet kernel calls tet_adjoint directly)
 //   float adj_omega(const D&, int i, int k)          omega of vertex i's body
 //                                                    at iteration k
 // and the members x, v, sdfs, n_sdf.
@@ -51,6 +52,9 @@ struct Adj {
 };
 
 __device__ __forceinline__ float3 f3(const float4 a) { return make_float3(a.x, a.y, a.z); }
+// abuf[k] for a run-time k without indexing the kernel-parameter array (which
+// would copy the whole Adj parameter block to local memory)
+__device__ __forceinline__ float4* adj_buf(const Adj& a, int k) { return k ? a.abuf[1] : a.abuf[0]; }
 __device__ __forceinline__ float3 cross3(const float3 a, const float3 b) {
   return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
@@ -97,7 +101,7 @@ template <class D, bool kCheb>
 __global__ void __launch_bounds__(256) ka_cheb(D d, Adj a, int k, float gamma, int src) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= adj_verts(d)) return;
-  const float4 xb = a.abuf[src][i];
+  const float4 xb = adj_buf(a, src)[i];
   float3 post, cur, yn;
   if (kCheb) {
     const float om = adj_omega(d, i, k);
@@ -116,30 +120,24 @@ __global__ void __launch_bounds__(256) ka_cheb(D d, Adj a, int k, float gamma, i
     cur = post;
     yn = make_float3(0.f, 0.f, 0.f);
   }
-  a.abuf[src ^ 1][i] = make_float4(cur.x, cur.y, cur.z, 0.f);
+  adj_buf(a, src ^ 1)[i] = make_float4(cur.x, cur.y, cur.z, 0.f);
   a.ybar[i] = make_float4(yn.x, yn.y, yn.z, 0.f);
   const float c = a.cnt[i];
   const float ic = c > 0.f ? 1.f / c : 0.f;
   a.dxbar[i] = make_float4(post.x * ic, post.y * ic, post.z * ic, 0.f);
 }
 
-// Reverse of the block projection of iteration k for one tet; scatters the
-// position adjoints into abuf[dst] and updates the multiplier adjoint.
-template <class D, bool kPrecise>
-__global__ void __launch_bounds__(128) ka_project(D d, Tape tp, Adj a, int k, float cD, float cH, int dst) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= adj_tets(d)) return;
-  int vid[4];
-  Tet tt;
-  float inv_v0, m_mu, m_la;
-  if (!adj_load_tet(d, t, vid, tt, inv_v0, m_mu, m_la)) return;
-  const float4* X = tp.xs + (size_t)k * adj_verts(d);
-#pragma unroll
-  for (int c = 0; c < 4; ++c) tt.p[c] = __ldg(X + vid[c]);
-  const float2 L = tp.lams[(size_t)k * adj_tets(d) + t];
+// Reverse of the block projection of one tet.  In: the tet's positions
+// entering the iteration (tt.p, w = inv_m) and inv_Dm, its multipliers L
+// entering it, compliances aD, aH, the adjoint of its multipliers after the
+// iteration (lb_next) and the adjoints of its corners' Jacobi accumulators
+// (dpb).  Out: the adjoints of the four corner positions (gout), of the
+// multipliers entering the iteration (lb_out) and of aD, aH (aDb, aHb).
+template <bool kPrecise>
+__device__ __forceinline__ void tet_adjoint(const Tet& tt, const float2 L, const float aD, const float aH,
+                                            const float2 lb_next, const float3 (&dpb)[4], float3 (&gout)[4],
+                                            float2& lb_out, float& aDb, float& aHb) {
   const float w[4] = {tt.p[0].w, tt.p[1].w, tt.p[2].w, tt.p[3].w};
-  const float sD = cD * inv_v0, sH = cH * inv_v0;  // d aD / d(1/mu), d aH / d(1/lambda)
-  const float aD = sD * m_mu, aH = sH * m_la;
   // ---- forward recompute ----
   float F[9];
   deformation_gradient(tt, F);
@@ -166,12 +164,9 @@ __global__ void __launch_bounds__(128) ka_project(D d, Tape tp, Adj a, int k, fl
   const float dD = (A22 * b1 - A12 * b2) * idet;
   const float dH = (A11 * b2 - A12 * b1) * idet;
   // ---- reverse ----
-  const float2 lb_next = a.lambar[t];
   float dDb = lb_next.x, dHb = lb_next.y;
-  float3 dpb[4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    dpb[c] = f3(a.dxbar[vid[c]]);
     dDb += w[c] * dot3(gD[c], dpb[c]);
     dHb += w[c] * dot3(gH[c], dpb[c]);
   }
@@ -179,8 +174,9 @@ __global__ void __launch_bounds__(128) ka_project(D d, Tape tp, Adj a, int k, fl
   const float bb2 = (A11 * dHb - A12 * dDb) * idet;
   const float A11b = -bb1 * dD, A22b = -bb2 * dH, A12b = -(bb1 * dH + bb2 * dD);
   const float CDb = -bb1, CHb = -bb2;
-  const float aDb = -L.x * bb1 + A11b, aHb = -L.y * bb2 + A22b;
-  a.lambar[t] = make_float2(lb_next.x - aD * bb1, lb_next.y - aH * bb2);
+  aDb = -L.x * bb1 + A11b;
+  aHb = -L.y * bb2 + A22b;
+  lb_out = make_float2(lb_next.x - aD * bb1, lb_next.y - aH * bb2);
   // adjoints of the corner gradients
   float3 gDb[4], gHb[4];
 #pragma unroll
@@ -192,6 +188,16 @@ __global__ void __launch_bounds__(128) ka_project(D d, Tape tp, Adj a, int k, fl
                          wh * dpb[c].z + a2 * gH[c].z + a3 * gD[c].z);
   }
   // g_{c+1}[r] = sum_q G[r][q] dm[c][q], g_0 = -sum  =>  G_bar[r][q] = sum_c (gb_{c+1} - gb_0)[r] dm[c][q]
+  float ed[3][3], eh[3][3];  // [c][r]
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    ed[c][0] = gDb[c + 1].x - gDb[0].x;
+    ed[c][1] = gDb[c + 1].y - gDb[0].y;
+    ed[c][2] = gDb[c + 1].z - gDb[0].z;
+    eh[c][0] = gHb[c + 1].x - gHb[0].x;
+    eh[c][1] = gHb[c + 1].y - gHb[0].y;
+    eh[c][2] = gHb[c + 1].z - gHb[0].z;
+  }
   float GDb[9], Hb[9];
 #pragma unroll
   for (int r = 0; r < 3; ++r)
@@ -200,10 +206,8 @@ __global__ void __launch_bounds__(128) ka_project(D d, Tape tp, Adj a, int k, fl
       float sd = 0.f, sh = 0.f;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const float ed = (r == 0 ? gDb[c + 1].x - gDb[0].x : r == 1 ? gDb[c + 1].y - gDb[0].y : gDb[c + 1].z - gDb[0].z);
-        const float eh = (r == 0 ? gHb[c + 1].x - gHb[0].x : r == 1 ? gHb[c + 1].y - gHb[0].y : gHb[c + 1].z - gHb[0].z);
-        sd += ed * tt.dm[c * 3 + q];
-        sh += eh * tt.dm[c * 3 + q];
+        sd += ed[c][r] * tt.dm[c * 3 + q];
+        sh += eh[c][r] * tt.dm[c * 3 + q];
       }
       GDb[r * 3 + q] = sd;
       Hb[r * 3 + q] = sh;
@@ -224,17 +228,41 @@ __global__ void __launch_bounds__(128) ka_project(D d, Tape tp, Adj a, int k, fl
     Fb[2] += c2.x + c2b.x; Fb[5] += c2.y + c2b.y; Fb[8] += c2.z + c2b.z;
   }
   // F = E Dm (E[r][c] = e_c[r])  =>  E_bar[r][c] = sum_q F_bar[r][q] dm[c][q]
-  float3 eb[3];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
-    eb[c] = make_float3(Fb[0] * tt.dm[c * 3] + Fb[1] * tt.dm[c * 3 + 1] + Fb[2] * tt.dm[c * 3 + 2],
-                        Fb[3] * tt.dm[c * 3] + Fb[4] * tt.dm[c * 3 + 1] + Fb[5] * tt.dm[c * 3 + 2],
-                        Fb[6] * tt.dm[c * 3] + Fb[7] * tt.dm[c * 3 + 1] + Fb[8] * tt.dm[c * 3 + 2]);
-  float4* G = a.abuf[dst];
-  red_add_v4(G + vid[0], -(eb[0].x + eb[1].x + eb[2].x), -(eb[0].y + eb[1].y + eb[2].y),
-             -(eb[0].z + eb[1].z + eb[2].z), 0.f);
+    gout[c + 1] = make_float3(Fb[0] * tt.dm[c * 3] + Fb[1] * tt.dm[c * 3 + 1] + Fb[2] * tt.dm[c * 3 + 2],
+                              Fb[3] * tt.dm[c * 3] + Fb[4] * tt.dm[c * 3 + 1] + Fb[5] * tt.dm[c * 3 + 2],
+                              Fb[6] * tt.dm[c * 3] + Fb[7] * tt.dm[c * 3 + 1] + Fb[8] * tt.dm[c * 3 + 2]);
+  gout[0] = make_float3(-(gout[1].x + gout[2].x + gout[3].x), -(gout[1].y + gout[2].y + gout[3].y),
+                        -(gout[1].z + gout[2].z + gout[3].z));
+}
+
+// Reverse of the block projection of iteration k, one thread per tet; scatters
+// the position adjoints into abuf[dst] and updates the multiplier adjoint.
+template <class D, bool kPrecise>
+__global__ void __launch_bounds__(128) ka_project(D d, Tape tp, Adj a, int k, float cD, float cH, int dst) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= adj_tets(d)) return;
+  int vid[4];
+  Tet tt;
+  float inv_v0, m_mu, m_la;
+  if (!adj_load_tet(d, t, vid, tt, inv_v0, m_mu, m_la)) return;
+  const float4* X = tp.xs + (size_t)k * adj_verts(d);
 #pragma unroll
-  for (int c = 0; c < 3; ++c) red_add_v4(G + vid[c + 1], eb[c].x, eb[c].y, eb[c].z, 0.f);
+  for (int c = 0; c < 4; ++c) tt.p[c] = __ldg(X + vid[c]);
+  const float2 L = tp.lams[(size_t)k * adj_tets(d) + t];
+  const float sD = cD * inv_v0, sH = cH * inv_v0;  // d aD / d(1/mu), d aH / d(1/lambda)
+  const float aD = sD * m_mu, aH = sH * m_la;
+  float3 dpb[4], gout[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) dpb[c] = f3(a.dxbar[vid[c]]);
+  float2 lb;
+  float aDb, aHb;
+  tet_adjoint<kPrecise>(tt, L, aD, aH, a.lambar[t], dpb, gout, lb, aDb, aHb);
+  a.lambar[t] = lb;
+  float4* G = adj_buf(a, dst);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) red_add_v4(G + vid[c], gout[c].x, gout[c].y, gout[c].z, 0.f);
   // materials: aD = (1/mu) sD, aH = (1/lambda) sH
   a.g_mu[t] += (double)(aDb * sD);
   a.g_la[t] += (double)(aHb * sH);
@@ -278,7 +306,7 @@ template <class D>
 __global__ void __launch_bounds__(256) ka_begin(D d, Tape tp, Adj a, int src, float dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= adj_verts(d)) return;
-  float3 gb = f3(a.abuf[src][i]);
+  float3 gb = f3(adj_buf(a, src)[i]);
   const float4 pre = tp.xpre[i];
   if (pre.w > 0.f) {
     const float3 vel = f3(tp.v1[i]);

@@ -426,28 +426,63 @@ __global__ void kb_rho_copy(BDev d, double* dst, const double* src) {
   if (src) d.bs[b].rho_hat = src[b];
 }
 
-// Accessors of the batched layout for the adjoint kernels (xpbd_adjoint.cuh).
+// Accessors of the batched layout for the vertex adjoint kernels
+// (xpbd_adjoint.cuh); the tet adjoint is the tile kernel kba_project below.
 __device__ __forceinline__ int adj_verts(const BDev& d) { return d.V; }
 __device__ __forceinline__ int adj_tets(const BDev& d) { return d.T; }
 __device__ __forceinline__ float adj_omega(const BDev& d, int i, int k) {
   const int b = __ldg(d.vblock_body + (i >> 8));
   return (float)d.hist[4 * ((size_t)b * d.max_records + k) + 1];
 }
-__device__ __forceinline__ bool adj_load_tet(const BDev& d, int t, int (&vid)[4], Tet& tt, float& inv_v0,
-                                             float& m_mu, float& m_la) {
-  const int p = t / kP;
-  if (t - p * kP >= __ldg(d.patch_ntets + p)) return false;  // padding slot
-  const uint32_t lid = __ldg(d.lid + t);
+}  // namespace batch
+}  // namespace xpbd
+
+#include "xpbd_adjoint.cuh"
+
+namespace xpbd {
+namespace batch {
+
+// Reverse of the batched block projection of iteration k, one CTA per 256-tet
+// patch: the patch's positions entering the iteration (from the tape) and its
+// vertices' accumulator adjoints are staged in shared memory once, then each
+// thread reverses one tet (tet_adjoint) and scatters its corner adjoints into
+// abuf[dst] with red.global.add.v4.  c = 1 / dt^2; the tet's compliances are
+// c / V0 times its (or its body's) 1 / mu and 1 / lambda.
+template <bool kPrecise>
+__global__ void __launch_bounds__(kP) kba_project(BDev d, Tape tp, Adj a, int k, float c, int dst) {
+  __shared__ float4 sp[256];
+  __shared__ float4 sb[256];
+  __shared__ int sg[256];
+  const int p = blockIdx.x;
   const int vb = __ldg(d.voff + p);
+  const int nv = __ldg(d.voff + p + 1) - vb;
+  const int nt = __ldg(d.patch_ntets + p);
+  const float4* X = tp.xs + (size_t)k * d.V;
+  for (int j = threadIdx.x; j < nv; j += kP) {
+    const int g = __ldg(d.pverts + vb + j);
+    sg[j] = g;
+    sp[j] = __ldg(X + g);
+    sb[j] = a.dxbar[g];
+  }
+  __syncthreads();
+  if ((int)threadIdx.x >= nt) return;
+  const int t = p * kP + threadIdx.x;
+  const uint32_t lid = __ldg(d.lid + t);
+  const float4 A = __ldg(d.dm_a + t);
+  const float4 B = __ldg(d.dm_b + t);
+  Tet tt;
+  tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+  tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+  tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
+  int l[4];
+  float3 dpb[4];
 #pragma unroll
-  for (int c = 0; c < 4; ++c) vid[c] = __ldg(d.pverts + vb + (int)((lid >> (8 * c)) & 0xffu));
-  const float4 a = __ldg(d.dm_a + t);
-  const float4 b = __ldg(d.dm_b + t);
-  tt.dm[0] = a.x; tt.dm[1] = a.y; tt.dm[2] = a.z;
-  tt.dm[3] = a.w; tt.dm[4] = b.x; tt.dm[5] = b.y;
-  tt.dm[6] = b.z; tt.dm[7] = b.w; tt.dm[8] = __ldg(d.dm_c + t);
-  inv_v0 = 6.f * det9(tt.dm);
-  tt.V0 = 1.f / inv_v0;
+  for (int q = 0; q < 4; ++q) {
+    l[q] = (int)((lid >> (8 * q)) & 0xffu);
+    tt.p[q] = sp[l[q]];
+    dpb[q] = f3(sb[l[q]]);
+  }
+  float m_mu, m_la;
   if (d.tinv_mu) {
     m_mu = __ldg(d.tinv_mu + t);
     m_la = __ldg(d.tinv_la + t);
@@ -456,13 +491,24 @@ __device__ __forceinline__ bool adj_load_tet(const BDev& d, int t, int (&vid)[4]
     m_mu = __ldg(d.inv_mu + body);
     m_la = __ldg(d.inv_la + body);
   }
-  return true;
+  const float inv_v0 = 6.f * det9(tt.dm);
+  const float s0 = c * inv_v0;  // d aD / d(1/mu) = d aH / d(1/lambda)
+  const float aD = s0 * m_mu, aH = s0 * m_la;
+  const float2 L = tp.lams[(size_t)k * d.T + t];
+  float3 gout[4];
+  float2 lb;
+  float aDb, aHb;
+  tet_adjoint<kPrecise>(tt, L, aD, aH, a.lambar[t], dpb, gout, lb, aDb, aHb);
+  a.lambar[t] = lb;
+  float4* G = adj_buf(a, dst);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) red_add_v4(G + sg[l[q]], gout[q].x, gout[q].y, gout[q].z, 0.f);
+  a.g_mu[t] += (double)(aDb * s0);
+  a.g_la[t] += (double)(aHb * s0);
 }
 
 }  // namespace batch
 }  // namespace xpbd
-
-#include "xpbd_adjoint.cuh"
 
 using namespace xpbd;
 using namespace xpbd::batch;
@@ -1009,12 +1055,11 @@ int xpbd_batch_substep_adjoint(void* h, float dt, const xpbd_tape* tape, const x
   ka_end<BDev><<<nblk(V), 256, 0, st>>>(s->d, a, e_over_dt);
   const float c = (float)(1.0 / ((double)dt * (double)dt));
   int src = 0;
-  const int g = (T + 127) / 128;
   for (int k = K - 1; k >= 0; --k) {
     if (s->prm.cheb_enable) ka_cheb<BDev, true><<<nblk(V), 256, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
     else ka_cheb<BDev, false><<<nblk(V), 256, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
-    if (s->prm.precise_hydro) ka_project<BDev, true><<<g, 128, 0, st>>>(s->d, tp, a, k, c, c, src ^ 1);
-    else ka_project<BDev, false><<<g, 128, 0, st>>>(s->d, tp, a, k, c, c, src ^ 1);
+    if (s->prm.precise_hydro) kba_project<true><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
+    else kba_project<false><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
     src ^= 1;
   }
   ka_begin<BDev><<<nblk(V), 256, 0, st>>>(s->d, tp, a, src, dt);
