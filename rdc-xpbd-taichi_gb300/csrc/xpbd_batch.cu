@@ -447,9 +447,11 @@ namespace batch {
 // vertices' accumulator adjoints are staged in shared memory once, then each
 // thread reverses one tet (tet_adjoint) and scatters its corner adjoints into
 // abuf[dst] with red.global.add.v4.  c = 1 / dt^2; the tet's compliances are
-// c / V0 times its (or its body's) 1 / mu and 1 / lambda.
+// c / V0 times its (or its body's) 1 / mu and 1 / lambda.  Compiled for 3
+// resident CTAs per SM (80 registers; the tet adjoint alone wants 96, which
+// allows only 2 CTAs and leaves the staging latency exposed).
 template <bool kPrecise>
-__global__ void __launch_bounds__(kP) kba_project(BDev d, Tape tp, Adj a, int k, float c, int dst) {
+__global__ void __launch_bounds__(kP, 3) kba_project(BDev d, Tape tp, Adj a, int k, float c, int dst) {
   __shared__ float4 sp[256];
   __shared__ float4 sb[256];
   __shared__ int sg[256];
@@ -457,6 +459,29 @@ __global__ void __launch_bounds__(kP) kba_project(BDev d, Tape tp, Adj a, int k,
   const int vb = __ldg(d.voff + p);
   const int nv = __ldg(d.voff + p + 1) - vb;
   const int nt = __ldg(d.patch_ntets + p);
+  const bool live = (int)threadIdx.x < nt;
+  const int t = p * kP + threadIdx.x;
+  // the tet's own records first: their latency overlaps the tile staging
+  uint32_t lid = 0u;
+  float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;
+  float C = 0.f, m_mu = 0.f, m_la = 0.f;
+  float2 L = make_float2(0.f, 0.f), lb_next = L;
+  if (live) {
+    lid = __ldg(d.lid + t);
+    A = __ldg(d.dm_a + t);
+    B = __ldg(d.dm_b + t);
+    C = __ldg(d.dm_c + t);
+    if (d.tinv_mu) {
+      m_mu = __ldg(d.tinv_mu + t);
+      m_la = __ldg(d.tinv_la + t);
+    } else {
+      const int body = __ldg(d.patch_body + p);
+      m_mu = __ldg(d.inv_mu + body);
+      m_la = __ldg(d.inv_la + body);
+    }
+    L = tp.lams[(size_t)k * d.T + t];
+    lb_next = a.lambar[t];
+  }
   const float4* X = tp.xs + (size_t)k * d.V;
   for (int j = threadIdx.x; j < nv; j += kP) {
     const int g = __ldg(d.pverts + vb + j);
@@ -465,15 +490,11 @@ __global__ void __launch_bounds__(kP) kba_project(BDev d, Tape tp, Adj a, int k,
     sb[j] = a.dxbar[g];
   }
   __syncthreads();
-  if ((int)threadIdx.x >= nt) return;
-  const int t = p * kP + threadIdx.x;
-  const uint32_t lid = __ldg(d.lid + t);
-  const float4 A = __ldg(d.dm_a + t);
-  const float4 B = __ldg(d.dm_b + t);
+  if (!live) return;
   Tet tt;
   tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
   tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
-  tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = __ldg(d.dm_c + t);
+  tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = C;
   int l[4];
   float3 dpb[4];
 #pragma unroll
@@ -482,23 +503,13 @@ __global__ void __launch_bounds__(kP) kba_project(BDev d, Tape tp, Adj a, int k,
     tt.p[q] = sp[l[q]];
     dpb[q] = f3(sb[l[q]]);
   }
-  float m_mu, m_la;
-  if (d.tinv_mu) {
-    m_mu = __ldg(d.tinv_mu + t);
-    m_la = __ldg(d.tinv_la + t);
-  } else {
-    const int body = __ldg(d.patch_body + p);
-    m_mu = __ldg(d.inv_mu + body);
-    m_la = __ldg(d.inv_la + body);
-  }
   const float inv_v0 = 6.f * det9(tt.dm);
   const float s0 = c * inv_v0;  // d aD / d(1/mu) = d aH / d(1/lambda)
   const float aD = s0 * m_mu, aH = s0 * m_la;
-  const float2 L = tp.lams[(size_t)k * d.T + t];
   float3 gout[4];
   float2 lb;
   float aDb, aHb;
-  tet_adjoint<kPrecise>(tt, L, aD, aH, a.lambar[t], dpb, gout, lb, aDb, aHb);
+  tet_adjoint<kPrecise>(tt, L, aD, aH, lb_next, dpb, gout, lb, aDb, aHb);
   a.lambar[t] = lb;
   float4* G = adj_buf(a, dst);
 #pragma unroll
