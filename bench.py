@@ -673,6 +673,24 @@ def dist_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+def max_over_ranks(value, device=None):
+    """MAX of a float over all ranks of the process group (the replicas' timing
+    reduction); the value itself without a group or with one rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_step, steps, world, max_total_ms):
+    """Whole-job throughput of `world` independent replicas that each processed
+    `units_per_step` x `steps` units, timed by the slowest rank."""
+    return units_per_step * steps * world / (max_total_ms * 1e-3)
+
+
 def run_reference(args):
     """The reference arm: the reference's algorithm on the host cores.  The reference's
     own Taichi CPU backend cannot be installed on this machine (no Taichi wheel for
@@ -754,14 +772,9 @@ def run_gb300(args):
         torch.cuda.synchronize()
     barrier()
     ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = float(sum(ms))
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(sum(ms)), device="cuda")
     ms_per_step = total_ms / args.steps
-    value = frame_units * args.steps * world / (total_ms * 1e-3)
+    value = replica_throughput(frame_units, args.steps, world, total_ms)
     solver.check_status()
 
     # per-kernel durations: the same frames, each launch bracketed by events (event record
