@@ -614,7 +614,8 @@ def cpu_baseline(mesh, specs, kw, substeps=5):
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,clocks.mem,"
+              "temperature.gpu")
 
     def __init__(self, index):
         self.index = index
@@ -645,7 +646,7 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, smax, reasons = [], [], set()
+        sm, smax, mem, temp, reasons = [], [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
@@ -659,10 +660,20 @@ class ClockSampler:
             for nm, val in zip(names, f[5:9]):
                 if val.lower().startswith("active"):
                     reasons.add(nm)
+            for lst, k in ((mem, 9), (temp, 10)):
+                try:
+                    lst.append(float(f[k]))
+                except (ValueError, IndexError):
+                    pass
         if not sm:
             return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+               "samples": len(sm)}
+        if mem:
+            out["mem_mhz"] = float(np.median(mem))
+        if temp:
+            out["temp_c"] = float(max(temp))
+        return out
 
 
 # ---------------------------------------------------------------------------
