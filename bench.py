@@ -385,13 +385,15 @@ def run_c3(args):
     bodies, specs, kw, desc = workload_c3()
     units = sum(b.rest_pose.n_tets for b in bodies) * kw["substeps_num"] * kw["constraints_iter"]
     btpt = "auto" if args.batch_tpt == "auto" else int(args.batch_tpt)
-    batch = XPBDBatchedSolver(bodies, product_sdfs(specs), tets_per_thread=btpt, **kw)
+    batch = XPBDBatchedSolver(bodies, product_sdfs(specs), tets_per_thread=btpt, pair_tets=bool(args.pair_tets),
+                              **kw)
     plain = []
     for b in bodies:
         mesh = TetMesh(b.rest_pose.points @ b.rotation.T, b.rest_pose.tets)
         plain.append(XPBDNeoHookeanSolver(mesh, product_sdfs(specs), young_modulus=b.young_modulus,
                                           poisson_ratio=b.poisson_ratio, offset=b.offset, density=b.density,
-                                          scatter="patch", tets_per_thread=args.tets_per_thread, **kw))
+                                          scatter="patch", tets_per_thread=args.tets_per_thread,
+                                          pair_tets=bool(args.pair_tets), **kw))
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
@@ -749,7 +751,7 @@ def run_gb300(args):
     t_build = time.perf_counter()
     solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
                                   patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce,
-                                  tets_per_thread=args.tets_per_thread, **kw)
+                                  tets_per_thread=args.tets_per_thread, pair_tets=bool(args.pair_tets), **kw)
     t_build = time.perf_counter() - t_build
     # the configuration that runs (the autotuner's pick with --scatter auto)
     scatter, tpt, pipe = solver.scatter, solver.tets_per_thread, solver.patch_pipeline
@@ -858,7 +860,7 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": desc, "step": "one frame (%d tet-iterations)" % frame_units,
                    "scatter": scatter, "patch_tets": patch_tets, "sweep_order": args.sweep_order,
-                   "patch_pipeline": pipe, "tets_per_thread": tpt,
+                   "patch_pipeline": pipe, "tets_per_thread": tpt, "tet_pairs": solver.n_tet_pairs,
                    "l2": "flushed between steps (%d MiB write)" % (L2_FLUSH_BYTES >> 20),
                    "parallelism": "replicas" if world > 1 else "single GPU", "graph": "one CUDA graph per frame"},
         "frames_per_s": 1e3 / ms_per_step * world,
@@ -893,7 +895,7 @@ def run_gb300(args):
         line["fp64_error"] = fp64_error(
             lambda: XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=scatter, sweep_order=args.sweep_order,
                                          patch_pipeline=pipe, patch_reduce=args.patch_reduce, tets_per_thread=tpt,
-                                         patch_tets=patch_tets or 256, **kw),
+                                         patch_tets=patch_tets or 256, pair_tets=bool(args.pair_tets), **kw),
             mesh, specs, kw, args.fp64_frames, warm_start=args.fp64_warm_start, warm_frames=args.fp64_warm_frames)
     print(json.dumps(line), flush=True)
 
@@ -906,7 +908,7 @@ def run_profile(args):
         from xpbd_gpu.batched import XPBDBatchedSolver
         bodies, specs, kw, desc = workload_c3()
         batch = XPBDBatchedSolver(bodies, product_sdfs(specs), tets_per_thread=min(args.tets_per_thread, 2),
-                                  use_graph=False, **kw)
+                                  use_graph=False, pair_tets=bool(args.pair_tets), **kw)
         for _ in range(args.profile_frames):
             batch.solve()
         torch.cuda.synchronize()
@@ -934,7 +936,8 @@ def run_profile(args):
     scatter = "patch" if args.scatter == "auto" else args.scatter
     solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=scatter, sweep_order=args.sweep_order,
                                   patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce,
-                                  tets_per_thread=args.tets_per_thread, use_graph=False, **kw)
+                                  tets_per_thread=args.tets_per_thread, use_graph=False,
+                                  pair_tets=bool(args.pair_tets), **kw)
     for _ in range(args.profile_frames):
         solver.solve()
     torch.cuda.synchronize()
@@ -963,6 +966,8 @@ def main():
     ap.add_argument("--patch-reduce", type=int, default=0, choices=[0, 1])
     ap.add_argument("--tets-per-thread", type=int, default=2, choices=[1, 2, 4])
     ap.add_argument("--batch-tpt", default="auto", choices=["auto", "1", "2"])
+    ap.add_argument("--pair-tets", type=int, default=1, choices=[0, 1],
+                    help="order face-adjacent tets in corner-aligned pairs (xpbd_pair_tets)")
     ap.add_argument("--c3-conv-iters", type=int, default=150)
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)

@@ -133,6 +133,11 @@ typedef struct xpbd_body {
    * 4 * (tet - p*P) + corner, ascending. */
   const uint16_t* pv_start;   /* [patch_voff[n_patches]] */
   const uint16_t* pv_slots;   /* [4 * n_patches * patch_tets] */
+  /* 1: the tets were laid out by xpbd_pair_tets (two-tet units at positions
+   * (2k, 2k+1), face pairs with aligned corners); the two-tets-per-thread
+   * kernels then merge a face pair's shared corners without comparisons and
+   * flush the other units' corners unmerged */
+  int32_t tet_pairs;
 } xpbd_body;
 
 /* Vertex fields addressable by xpbd_import_vec3 / xpbd_export_vec3. */
@@ -309,6 +314,24 @@ int xpbd_build_patches(const int32_t* tets, int32_t n_tets, int32_t n_verts, int
 int xpbd_build_patch_csr(const int32_t* patch_voff, const uint32_t* tet_lid, int32_t n_tets, int32_t patch_tets,
                          uint16_t* pv_start, uint16_t* pv_slots);
 
+/* Pairs of face-adjacent tets for the two-tets-per-thread tile kernels (the
+ * reference's patcher has no counterpart; it only orders the mesh,
+ * xpbd_base.py:42).  tets: [T][4] in the solver's order.  Writes order[T]
+ * (position i of the new order holds old tet order[i]) and corner_perm[T]
+ * (corner c of the new tet is old corner (corner_perm >> 2c) & 3), and the
+ * number of face pairs in *n_pairs.  A tet pairs with its nearest face
+ * neighbour within 48 positions of the old order (which should be a
+ * space-filling order, e.g. xpbd_morton_order's), so the new order keeps its
+ * locality.  The new order is made of two-tet units at positions (2k, 2k+1)
+ * sorted by their first tet: the face pairs, and the other tets two by two in
+ * their old order with unchanged corners (an odd count leaves one last tet).
+ * A face pair (a, b) with shared face {u, v, w} becomes a = (u, v, w, a*) and
+ * b = (v, u, w, b*), each an even permutation of its old corner order, so
+ * every tet keeps its signed rest volume; the kernels then merge the three
+ * shared corners in registers without comparing vertex ids. */
+int xpbd_pair_tets(const int32_t* tets, int32_t n_tets, int32_t n_verts, int32_t* order, uint8_t* corner_perm,
+                   int32_t* n_pairs);
+
 /* Vertex -> (tet*4+corner) CSR for the gather variant, slots ascending. */
 int xpbd_build_vertex_csr(const int32_t* tets, int32_t n_tets, int32_t n_verts,
                           int32_t* offsets /* [V+1] */, int32_t* slots /* [4T] */);
@@ -354,6 +377,7 @@ typedef struct xpbd_batch {
    * (padding slots unused); NULL = the body's body_inv_mu / body_inv_lambda */
   const float* tet_inv_mu;    /* [T] */
   const float* tet_inv_lambda; /* [T] */
+  int32_t tet_pairs;          /* 1: every body's tets laid out by xpbd_pair_tets (see xpbd_body) */
 } xpbd_batch;
 
 /* Message of the last batch failure on the calling thread. */

@@ -58,6 +58,7 @@ struct BDev {
   const float* inv_la;
   const float* tinv_mu;  // per-tet 1 / mu (nullptr: the body's)
   const float* tinv_la;  // per-tet 1 / lambda
+  int paired;            // tets laid out by xpbd_pair_tets
   const int* body_patches;
   const int* body_tets;
   const int* perm;
@@ -172,11 +173,11 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_projec
   if (n <= 0) return;
   if (kTetMat) {
     project_chain<kBlockMode, kPrecise, kTPT, true>(A, B, C, lid, L, d.lam + t0, n, sp, sg, d.dx, inv_dt2, inv_dt2,
-                                                    relax_h, relax_d, mD, mH);
+                                                    relax_h, relax_d, d.paired != 0, mD, mH);
   } else {
     const float cD = __ldg(d.inv_mu + b) * inv_dt2, cH = __ldg(d.inv_la + b) * inv_dt2;
     project_chain<kBlockMode, kPrecise, kTPT>(A, B, C, lid, L, d.lam + t0, n, sp, sg, d.dx, cD, cH, relax_h,
-                                              relax_d);
+                                              relax_d, d.paired != 0);
   }
 }
 
@@ -770,6 +771,7 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
   d.inv_la = body->body_inv_lambda;
   d.tinv_mu = body->tet_inv_mu;
   d.tinv_la = body->tet_inv_mu ? body->tet_inv_lambda : nullptr;
+  d.paired = body->tet_pairs != 0;
   d.body_patches = body->body_n_patches;
   d.body_tets = body->body_n_tets;
   d.perm = body->vert_perm;

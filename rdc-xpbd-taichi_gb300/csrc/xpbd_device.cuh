@@ -334,6 +334,13 @@ __device__ __forceinline__ float det9(const float m[9]) {
 // needs 72 without spills); otherwise no minimum.
 __host__ __device__ constexpr int project_min_blocks(int tpt) { return tpt == 2 ? 7 : 1; }
 
+__device__ __forceinline__ void add4(float4& a, const float4 b) {
+  a.x += b.x;
+  a.y += b.y;
+  a.z += b.z;
+  a.w += b.w;
+}
+
 // Tile projection of kTPT Morton-consecutive tets of one thread (records
 // A, B, C, lid; multipliers L, stored to lam_out[k] as each tet is done), n of
 // them valid.  Vertex
@@ -342,7 +349,9 @@ __host__ __device__ constexpr int project_min_blocks(int tpt) { return tpt == 2 
 // registers: a corner of the next tet that matches one is added there, and a
 // held corner the next tet does not touch is flushed with red.global.add.v4.
 // A chain of kTPT tets sharing s corners per step issues 4 + (kTPT - 1)(4 - s)
-// reductions instead of 4 kTPT.  cD, cH: time-scaled inverse Lame parameters;
+// reductions instead of 4 kTPT.  A face pair laid out by xpbd_pair_tets (the
+// second tet's corners 0, 1, 2 are the first's 1, 0, 2, recognised from the
+// packed patch-local ids) merges its three shared corners without comparisons.  cD, cH: time-scaled inverse Lame parameters;
 // the tet's compliances are 6 det(inv_Dm) cD and 6 det(inv_Dm) cH (1 / V0).
 // kTetMat: per-tet materials, the compliances are further multiplied by the
 // tet's 1 / mu and 1 / lambda (mD[k], mH[k]).
@@ -350,8 +359,8 @@ template <bool kBlockMode, bool kPrecise, int kTPT, bool kTetMat = false>
 __device__ __forceinline__ void project_chain(const float4 (&A)[kTPT], const float4 (&B)[kTPT], const float (&C)[kTPT],
                                               const uint32_t (&lid)[kTPT], float2 (&L)[kTPT], float2* lam_out,
                                               int n, const float4* sp, const int* sg, float4* dx, float cD,
-                                              float cH, float relax_h, float relax_d, const float* mD = nullptr,
-                                              const float* mH = nullptr) {
+                                              float cH, float relax_h, float relax_d, bool paired,
+                                              const float* mD = nullptr, const float* mH = nullptr) {
   float4 acc[4];
   int hid[4] = {-1, -1, -1, -1};
 #pragma unroll
@@ -379,21 +388,34 @@ __device__ __forceinline__ void project_chain(const float4 (&A)[kTPT], const flo
     float4 nacc[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) nacc[c] = make_float4(dp[c].x, dp[c].y, dp[c].z, cnt);
-    // Held corners: merge into the matching new corner, or flush.  A tet's
-    // corners are distinct vertices, so a held corner matches at most one.
+    if (paired && (k & 1)) {
+      // Two-tet unit of xpbd_pair_tets (paired is uniform over the grid).  A
+      // face pair has aligned corners: corners 0, 1, 2 of this tet are corners
+      // 1, 0, 2 of the held one, and corner 3 is flushed.  Any other unit
+      // flushes all four held corners unmerged.
+      if ((lid[k] & 0xffffffu) == (__byte_perm(lid[k - 1], 0u, 0x3201u) & 0xffffffu)) {
+        add4(nacc[0], acc[1]);
+        add4(nacc[1], acc[0]);
+        add4(nacc[2], acc[2]);
+        red_add_v4(dx + sg[hid[3]], acc[3].x, acc[3].y, acc[3].z, acc[3].w);
+      } else {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      bool used = false;
+        for (int q = 0; q < 4; ++q) red_add_v4(dx + sg[hid[q]], acc[q].x, acc[q].y, acc[q].z, acc[q].w);
+      }
+    } else {
+      // Held corners: merge into the matching new corner, or flush.  A tet's
+      // corners are distinct vertices, so a held corner matches at most one.
 #pragma unroll
-      for (int c = 0; c < 4; ++c)
-        if (hid[q] == id[c]) {
-          nacc[c].x += acc[q].x;
-          nacc[c].y += acc[q].y;
-          nacc[c].z += acc[q].z;
-          nacc[c].w += acc[q].w;
-          used = true;
-        }
-      if (hid[q] >= 0 && !used) red_add_v4(dx + sg[hid[q]], acc[q].x, acc[q].y, acc[q].z, acc[q].w);
+      for (int q = 0; q < 4; ++q) {
+        bool used = false;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          if (hid[q] == id[c]) {
+            add4(nacc[c], acc[q]);
+            used = true;
+          }
+        if (hid[q] >= 0 && !used) red_add_v4(dx + sg[hid[q]], acc[q].x, acc[q].y, acc[q].z, acc[q].w);
+      }
     }
 #pragma unroll
     for (int c = 0; c < 4; ++c) {

@@ -49,6 +49,18 @@ void order_by(const std::vector<uint64_t>& code, int32_t* perm) {
   std::copy(idx.begin(), idx.end(), perm);
 }
 
+// Parity of a permutation of (0, 1, 2, 3): true if even.
+inline bool even4(const int q[4]) {
+  int inv = 0;
+  for (int i = 0; i < 4; ++i)
+    for (int j = i + 1; j < 4; ++j) inv += q[i] > q[j];
+  return (inv & 1) == 0;
+}
+
+inline uint8_t pack4(const int q[4]) {
+  return (uint8_t)(q[0] | (q[1] << 2) | (q[2] << 4) | (q[3] << 6));
+}
+
 }  // namespace
 
 extern "C" {
@@ -188,6 +200,132 @@ int xpbd_build_vertex_csr(const int32_t* tets, int32_t n_tets, int32_t n_verts, 
   for (int32_t v = 0; v < n_verts; ++v) offsets[v + 1] += offsets[v];
   std::vector<int32_t> fill(offsets, offsets + n_verts);
   for (int64_t k = 0; k < 4ll * n_tets; ++k) slots[fill[tets[k]]++] = (int32_t)k;
+  return XPBD_OK;
+}
+
+int xpbd_pair_tets(const int32_t* tets, int32_t n_tets, int32_t n_verts, int32_t* order, uint8_t* corner_perm,
+                   int32_t* n_pairs) {
+  if (n_tets < 0 || n_verts <= 0 || !order || !corner_perm || !n_pairs || (n_tets > 0 && !tets))
+    return XPBD_ERR_INVALID_ARGUMENT;
+  for (int64_t k = 0; k < 4ll * n_tets; ++k)
+    if (tets[k] < 0 || tets[k] >= n_verts) return XPBD_ERR_BAD_MESH;
+  *n_pairs = 0;
+  const uint8_t identity = (uint8_t)(0 | (1 << 2) | (2 << 4) | (3 << 6));
+  if (n_verts >= (1 << 21)) {  // face keys pack three 21-bit ids: no pairing
+    for (int32_t t = 0; t < n_tets; ++t) {
+      order[t] = t;
+      corner_perm[t] = identity;
+    }
+    return XPBD_OK;
+  }
+  // faces: sorted vertex triple of the face opposite corner j of tet t
+  struct Face {
+    uint64_t key;
+    int32_t t;
+    int32_t j;
+  };
+  std::vector<Face> faces((size_t)4 * n_tets);
+  for (int32_t t = 0; t < n_tets; ++t)
+    for (int j = 0; j < 4; ++j) {
+      int32_t v[3], m = 0;
+      for (int c = 0; c < 4; ++c)
+        if (c != j) v[m++] = tets[4 * (int64_t)t + c];
+      std::sort(v, v + 3);
+      faces[4 * (size_t)t + j] = {((uint64_t)v[0] << 42) | ((uint64_t)v[1] << 21) | (uint64_t)v[2], t, j};
+    }
+  std::sort(faces.begin(), faces.end(), [](const Face& a, const Face& b) {
+    return a.key < b.key || (a.key == b.key && a.t < b.t);
+  });
+  std::vector<int32_t> nb((size_t)4 * n_tets, -1);  // tet across the face opposite corner j
+  for (size_t k = 0; k + 1 < faces.size(); ++k)
+    if (faces[k].key == faces[k + 1].key && faces[k].t != faces[k + 1].t) {
+      nb[4 * (size_t)faces[k].t + faces[k].j] = faces[k + 1].t;
+      nb[4 * (size_t)faces[k + 1].t + faces[k + 1].j] = faces[k].t;
+    }
+  // corner orders of a pair (a, b) sharing the face opposite a's corner ja:
+  // a' = (u, v, w, a*), b' = (v, u, w, b*), both even; false if b' is odd
+  auto orders = [&](int32_t a, int ja, int32_t b, int qa[4], int qb[4]) {
+    int m = 0;
+    for (int c = 0; c < 4; ++c)
+      if (c != ja) qa[m++] = c;
+    qa[3] = ja;
+    if (!even4(qa)) std::swap(qa[0], qa[1]);
+    const int32_t* A = tets + 4 * (int64_t)a;
+    const int32_t* B = tets + 4 * (int64_t)b;
+    const int32_t want[3] = {A[qa[1]], A[qa[0]], A[qa[2]]};
+    bool used[4] = {false, false, false, false};
+    for (int k = 0; k < 3; ++k) {
+      qb[k] = -1;
+      for (int c = 0; c < 4; ++c)
+        if (B[c] == want[k]) qb[k] = c;
+      if (qb[k] < 0) return false;
+      used[qb[k]] = true;
+    }
+    for (int c = 0; c < 4; ++c)
+      if (!used[c]) qb[3] = c;
+    return even4(qb);
+  };
+  // Greedy in the given (Morton) order; a partner is a face neighbour within
+  // kWindow positions, the nearest one, so that pairs keep the order's locality.
+  constexpr int64_t kWindow = 48;
+  std::vector<int32_t> partner(n_tets, -1);
+  std::vector<uint8_t> perm(n_tets, identity);
+  for (int32_t t = 0; t < n_tets; ++t) {
+    if (partner[t] >= 0) continue;
+    int32_t best = -1;
+    int64_t best_d = 0;
+    int qa[4], qb[4], ba[4] = {0, 1, 2, 3}, bb[4] = {0, 1, 2, 3};
+    for (int j = 0; j < 4; ++j) {
+      const int32_t u = nb[4 * (size_t)t + j];
+      if (u < 0 || partner[u] >= 0) continue;
+      const int64_t d = u > t ? (int64_t)u - t : (int64_t)t - u;
+      if (d > kWindow || (best >= 0 && d >= best_d)) continue;
+      if (!orders(t, j, u, qa, qb)) continue;
+      best = u;
+      best_d = d;
+      std::copy(qa, qa + 4, ba);
+      std::copy(qb, qb + 4, bb);
+    }
+    if (best < 0) continue;
+    partner[t] = best;
+    partner[best] = t;
+    perm[t] = pack4(ba);
+    perm[best] = pack4(bb);
+  }
+  // Units of two slots: face pairs, and the remaining tets two by two in
+  // order (their corners unchanged); units in the order of their first tet.
+  struct Unit {
+    int32_t a, b;  // b < 0: a lone last tet
+  };
+  std::vector<Unit> units;
+  units.reserve(n_tets / 2 + 1);
+  int32_t pending = -1, np = 0;
+  for (int32_t t = 0; t < n_tets; ++t) {
+    const int32_t u = partner[t];
+    if (u >= 0) {
+      if (u > t) {
+        units.push_back({t, u});
+        ++np;
+      }
+    } else if (pending < 0) {
+      pending = t;
+    } else {
+      units.push_back({pending, t});
+      pending = -1;
+    }
+  }
+  std::stable_sort(units.begin(), units.end(), [](const Unit& x, const Unit& y) { return x.a < y.a; });
+  if (pending >= 0) units.push_back({pending, -1});
+  int32_t k = 0;
+  for (const Unit& un : units) {
+    order[k] = un.a;
+    corner_perm[k++] = perm[un.a];
+    if (un.b >= 0) {
+      order[k] = un.b;
+      corner_perm[k++] = perm[un.b];
+    }
+  }
+  *n_pairs = np;
   return XPBD_OK;
 }
 

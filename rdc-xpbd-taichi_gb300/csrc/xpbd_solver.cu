@@ -62,6 +62,7 @@ struct Dev {
   const int* v2t_slot;
   float4* corner;
   const int* perm;  // solver vertex i <- caller vertex perm[i] (nullptr = identity)
+  int paired;       // tets laid out by xpbd_pair_tets
   // tile variant: patch p = tets [p*P, (p+1)*P), vertices verts[voff[p]..voff[p+1])
   int n_patches, P, n_pverts;
   const uint32_t* lid;
@@ -751,7 +752,7 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) k_project
   __syncthreads();
   const int n = nt - l0 < kTPT ? nt - l0 : kTPT;
   project_chain<kBlockMode, kPrecise, kTPT>(A, B, C, lid, L, d.lam + t0 + l0, n, sp, sg, d.dx, cD, cH, relax_h,
-                                            relax_d);
+                                            relax_d, d.paired != 0);
 }
 
 template <bool kRes, bool kMon, bool kPrecise, int kP>
@@ -1538,6 +1539,7 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
   d.v2t_slot = body->v2t_slots;
   d.corner = reinterpret_cast<float4*>(body->corner_dx);
   d.perm = body->vert_perm;
+  d.paired = body->tet_pairs != 0;
   if (has_patch) {
     d.n_patches = body->n_patches;
     d.P = body->patch_tets;

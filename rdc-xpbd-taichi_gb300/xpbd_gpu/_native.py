@@ -70,7 +70,7 @@ class XpbdBody(ctypes.Structure):
                 ("vert_perm", _P),
                 ("n_patches", ctypes.c_int32), ("patch_tets", ctypes.c_int32),
                 ("tet_lid", _P), ("patch_voff", _P), ("patch_verts", _P),
-                ("pv_start", _P), ("pv_slots", _P)]
+                ("pv_start", _P), ("pv_slots", _P), ("tet_pairs", ctypes.c_int32)]
 
 
 class XpbdBatch(ctypes.Structure):
@@ -81,7 +81,7 @@ class XpbdBatch(ctypes.Structure):
                 ("patch_voff", _P), ("patch_verts", _P), ("patch_body", _P), ("patch_ntets", _P),
                 ("vblock_body", _P), ("body_inv_mu", _P), ("body_inv_lambda", _P),
                 ("body_n_patches", _P), ("body_n_tets", _P), ("vert_perm", _P),
-                ("tet_inv_mu", _P), ("tet_inv_lambda", _P)]
+                ("tet_inv_mu", _P), ("tet_inv_lambda", _P), ("tet_pairs", ctypes.c_int32)]
 
 
 class XpbdTape(ctypes.Structure):
@@ -129,6 +129,7 @@ _SIGNATURES = {
                                          ctypes.c_int32, ctypes.c_int32, _P]),
     "xpbd_morton_order": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int32, _P, _P]),
     "xpbd_build_vertex_csr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P]),
+    "xpbd_pair_tets": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, _P, _P, ctypes.POINTER(ctypes.c_int32)]),
     "xpbd_batch_last_error": (ctypes.c_char_p, []),
     "xpbd_batch_create": (ctypes.c_int, [ctypes.POINTER(XpbdParams), ctypes.POINTER(XpbdBatch),
                                          ctypes.POINTER(XpbdSdf), ctypes.c_int32, ctypes.c_int32,
@@ -244,3 +245,19 @@ def check(status, batch=False):
     if status == 4:  # XPBD_ERR_NO_SDF mirrors xpbd_base.py:66-67
         raise ValueError(msg)
     raise XpbdError(status, msg)
+
+
+def pair_tets(lib, tets, n_verts):
+    """Face pairs of `tets` ([T, 4] int, solver order) for the two-tets-per-thread
+    kernels: returns (order [T], corner permutation [T, 4], number of pairs);
+    new tet i is old tet order[i] with corners old[perm[i]]."""
+    import numpy as np
+    tt = np.ascontiguousarray(tets, dtype=np.int32)
+    T = len(tt)
+    order = np.empty(T, dtype=np.int32)
+    packed = np.empty(T, dtype=np.uint8)
+    n = ctypes.c_int32()
+    check(lib.xpbd_pair_tets(tt.ctypes.data, T, int(n_verts), order.ctypes.data, packed.ctypes.data,
+                             ctypes.byref(n)))
+    perm = np.stack([(packed >> (2 * c)) & 3 for c in range(4)], axis=1).astype(np.int64)
+    return order, perm, n.value

@@ -19,7 +19,7 @@ import numpy as np
 
 from xpbd_gpu import _native
 from xpbd_gpu.neohookean_solver import calc_first_lame, calc_second_lame, frame_chunks
-from xpbd_gpu.xpbd_base import _require_cuda, _torch, calc_tet_volume, load_rest_pose
+from xpbd_gpu.xpbd_base import _require_cuda, _torch, calc_tet_volume, inv_dm_of, load_rest_pose
 
 PATCH = 256
 
@@ -51,7 +51,7 @@ class XPBDBatchedSolver:
                  hydrostatic_relaxation=1.2, deviatoric_relaxation=1.2, cheb_enable=True, cheb_warmup=5,
                  cheb_gamma=0.6666, block_neohookean_enable=True, monitor_convergence=False,
                  gravity=(0.0, -9.8, 0.0), precise_hydro=None, use_graph=True, tets_per_thread=2,
-                 autotune_cache=True):
+                 autotune_cache=True, pair_tets=True):
         if isinstance(sdf, (list, tuple)):
             self.sdfs = [s for s in sdf if s is not None]
         else:
@@ -81,6 +81,7 @@ class XPBDBatchedSolver:
             raise ValueError("tets_per_thread must be 1, 2 or 'auto'")
         self.tets_per_thread = 2 if tets_per_thread == "auto" else int(tets_per_thread)
         self.per_tet_materials = any(b.tet_young_modulus is not None for b in self.bodies)
+        self.pair_tets = bool(pair_tets)
         self.time = 0.0
         self.current_frame = 0
         self._handle = None
@@ -126,6 +127,12 @@ class XPBDBatchedSolver:
         inv_vperm = np.empty(V, dtype=np.int64)
         inv_vperm[vperm] = np.arange(V)
         tets_s = np.ascontiguousarray(inv_vperm[tets[tperm]], dtype=np.int32)
+        dm_solver = inv_Dm[tperm]
+        if self.pair_tets:  # face pairs with aligned corners (xpbd_pair_tets)
+            order, cperm, _ = _native.pair_tets(self._lib, tets_s, V)
+            tperm = tperm[order]
+            tets_s = np.ascontiguousarray(np.take_along_axis(tets_s[order], cperm, axis=1), dtype=np.int32)
+            dm_solver = inv_dm_of(x, np.take_along_axis(tets[tperm], cperm, axis=1))
         npat = -(-T // PATCH)
         voff = np.empty(npat + 1, dtype=np.int32)
         pverts = np.empty(4 * T, dtype=np.int32)
@@ -148,7 +155,8 @@ class XPBDBatchedSolver:
             tnu = np.full(T, float(b.poisson_ratio))
         # valence (constraints per vertex in block mode), solver vertex order
         cnt = np.bincount(tets_s.reshape(-1), minlength=V).astype(np.float32)
-        return dict(x=x, V0=V0, inv_Dm=inv_Dm, m=m, inv_m=inv_m, vperm=vperm, tperm=tperm, T=T, V=V, npat=npat,
+        return dict(x=x, V0=V0, inv_Dm=inv_Dm, dm_solver=dm_solver, m=m, inv_m=inv_m, vperm=vperm, tperm=tperm,
+                    T=T, V=V, npat=npat,
                     voff=voff, pverts=pverts[:voff[-1]], lid=lid, mu=lame_mu, la=lame_la, tet_E=tE, tet_nu=tnu,
                     cnt=cnt, indices=tets[:, np.array([[0, 2, 1], [0, 3, 2], [0, 1, 3], [1, 2, 3]])].reshape(-1))
 
@@ -177,7 +185,7 @@ class XPBDBatchedSolver:
             x4[vo:vo + p["V"], 3] = p["inv_m"][p["vperm"]]
             perm[vo:vo + p["V"]] = oo + p["vperm"]
             vblock_body[vo // PATCH:(vo + Vp[k]) // PATCH] = k
-            D[to:to + p["T"]] = p["inv_Dm"][p["tperm"]].reshape(-1, 9)
+            D[to:to + p["T"]] = p["dm_solver"].reshape(-1, 9)
             lid[to:to + Tp[k]] = p["lid"]
             p0 = to // PATCH
             patch_body[p0:p0 + p["npat"]] = k
@@ -252,6 +260,7 @@ class XPBDBatchedSolver:
         b.vert_perm = self._perm.data_ptr()
         if self._tinv_mu is not None:
             b.tet_inv_mu, b.tet_inv_lambda = self._tinv_mu.data_ptr(), self._tinv_la.data_ptr()
+        b.tet_pairs = 1 if self.pair_tets else 0
         self._max_records = max(1, len(frame_chunks(self.frame_dt, self.dt)) * self.substeps_num
                                 * self.constraints_iter)
         table = (_native.XpbdSdf * len(self.sdfs))()

@@ -19,7 +19,10 @@ Extensions (keyword-only): ``total_mass`` / ``density`` (the reference fixes
 1 kg, xpbd_base.py:36), ``gravity``, ``scatter`` ('atomic' = vector
 red.global.add, 'gather' = deterministic vertex->tet CSR), ``precise_hydro``
 (cancellation-free det F - 1; default on for poisson_ratio >= 0.49),
-``use_graph`` and ``reorder`` (Morton order on the device).  With
+``use_graph``, ``reorder`` (Morton order on the device) and ``pair_tets``
+(face-adjacent tets ordered in pairs with aligned corners, so the
+two-tets-per-thread kernels merge their shared corners without comparing
+vertex ids; on by default).  With
 ``scatter="auto"`` the scatter variant, patch size, tets per thread and
 tile pipeline are measured on this mesh and GPU (``xpbd_gpu.autotune``) and
 the choice is kept in ``autotune_result``.
@@ -60,7 +63,7 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
                  monitor_convergence=False, *, total_mass=1.0, density=None, gravity=(0.0, -9.8, 0.0),
                  scatter="patch", precise_hydro=None, use_graph=True, reorder=True, sweep_order=1,
                  patch_pipeline=0, patch_reduce=0, tets_per_thread=2, patch_tets=256, tet_young_modulus=None,
-                 tet_poisson_ratio=None, autotune_cache=True):
+                 tet_poisson_ratio=None, autotune_cache=True, pair_tets=True):
         self.autotune_result = None
         if scatter == "auto":
             from xpbd_gpu import autotune
@@ -116,7 +119,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         self.use_graph = bool(use_graph)
         self.block_size = block_size
         super().__init__(rest_pose, sdf, scale, offset, frame_dt, dt, substeps_num, reorder_all, block_size,
-                         total_mass=total_mass, density=density, gravity=gravity, reorder=reorder)
+                         total_mass=total_mass, density=density, gravity=gravity, reorder=reorder,
+                         pair_tets=pair_tets)
 
     # -- construction (neohookean_solver.py:79-95) ------------------------------
     def initialize_specific(self, scale, offset):

@@ -29,6 +29,14 @@ def calc_tet_volume(p0, p1, p2, p3):
     return np.einsum("...i,...i->...", np.cross(p1 - p0, p2 - p0), p3 - p0) / 6.0
 
 
+def inv_dm_of(x, tets):
+    """inverse([x1 - x0, x2 - x0, x3 - x0]) of every tet (neohookean_solver.py:97-107), float64."""
+    P = np.asarray(x, dtype=np.float64)[tets]
+    Ds = np.stack([P[:, 1] - P[:, 0], P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]], axis=-1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.linalg.inv(Ds)
+
+
 def _torch():
     import torch
     return torch
@@ -159,7 +167,7 @@ class XPBDSolverBase:
 
     def __init__(self, rest_pose, sdf, scale=1.0, offset=(0.0, 0.0, 0.0), frame_dt=1e-2, dt=1e-2,
                  substeps_num=20, reorder_all=False, block_size=128, total_mass=1.0, density=None,
-                 gravity=(0.0, -9.8, 0.0), reorder=True):
+                 gravity=(0.0, -9.8, 0.0), reorder=True, pair_tets=True):
         # Collision list first: the reference raises ValueError for an empty list (:60-67)
         if isinstance(sdf, (list, tuple)):
             self.sdfs = [s for s in sdf if s is not None]
@@ -200,6 +208,7 @@ class XPBDSolverBase:
         self.indices = HostField(tets[:, FACE_TABLE].reshape(-1).astype(np.uint32))
 
         self._reorder = bool(reorder)
+        self.pair_tets = bool(pair_tets)
         self.initialize_specific(scale, offset)
 
     # -- setup ----------------------------------------------------------------
@@ -250,6 +259,7 @@ class XPBDSolverBase:
         return m, inv_m
 
     def _upload(self, x, V0, inv_Dm, m, inv_m):
+        self._inv_dm_file = inv_Dm
         torch = _torch()
         dev = self._device
         V, T = self.n_verts, self.n_tets
@@ -258,6 +268,14 @@ class XPBDSolverBase:
         inv_vperm[vperm] = np.arange(V)
         self._vperm, self._tperm = vperm, tperm
         tets_new = inv_vperm[self._tets_host[tperm]].astype(np.int32)
+        self.n_tet_pairs = 0
+        dm_solver = inv_Dm[tperm]
+        if self.pair_tets:
+            order, cperm, self.n_tet_pairs = _native.pair_tets(self._lib, tets_new, V)
+            tperm = tperm[order]
+            self._tperm = tperm
+            tets_new = np.ascontiguousarray(np.take_along_axis(tets_new[order], cperm, axis=1), dtype=np.int32)
+            dm_solver = inv_dm_of(x, np.take_along_axis(self._tets_host[tperm], cperm, axis=1))
         self._tets_solver = tets_new
         x4 = np.zeros((V, 4), dtype=np.float32)
         x4[:, :3] = x[vperm]
@@ -266,7 +284,7 @@ class XPBDSolverBase:
         # so that every patch's slice can be bulk-copied whole
         Tp = -(-T // 256) * 256
         D = np.zeros((Tp, 9), dtype=np.float32)
-        D[:T] = inv_Dm[tperm].reshape(T, 9)
+        D[:T] = dm_solver.reshape(T, 9)
         dm_a = np.ascontiguousarray(D[:, 0:4])
         dm_b = np.ascontiguousarray(D[:, 4:8])
         dm_c = np.ascontiguousarray(D[:, 8])
@@ -362,6 +380,7 @@ class XPBDSolverBase:
             b.v2t_slots = self._v2t_slots.data_ptr()
             b.corner_dx = self._corner.data_ptr()
         b.vert_perm = self._perm.data_ptr()
+        b.tet_pairs = 1 if self.pair_tets else 0
         return b
 
     def _sdf_table(self):
@@ -396,12 +415,9 @@ class XPBDSolverBase:
         return out
 
     def _inv_dm_array(self):
-        T = self.n_tets
-        D = np.concatenate([self._dm_a[:T].cpu().numpy(), self._dm_b[:T].cpu().numpy(),
-                            self._dm_c[:T].cpu().numpy()[:, None]], axis=1).reshape(-1, 3, 3)
-        out = np.empty_like(D)
-        out[self._tperm] = D
-        return out
+        """inv_Dm in the caller's tet and corner order (the device copy of a
+        face-paired tet is that of its reordered corners)."""
+        return self._inv_dm_file.astype(np.float32)
 
     def _export_vec3_device(self, field_id):
         out = _torch().empty((self.n_verts, 3), dtype=_torch().float32, device=self._device)

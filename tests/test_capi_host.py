@@ -147,3 +147,50 @@ def test_build_patches_layout(native_lib):
                 for sl in seg:
                     t, q = p * P + int(sl) // 4, int(sl) % 4
                     assert (int(lid[t]) >> (8 * q)) & 0xFF == k
+
+
+def _signed_volumes(pts, tets):
+    P = pts[tets]
+    return np.einsum("ij,ij->i", np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]), P[:, 3] - P[:, 0]) / 6.0
+
+
+def test_pair_tets_on_a_kuhn_grid(native_lib):
+    """Every tet of a Kuhn grid (6 tets around each cell diagonal) finds a face
+    partner; pairs are laid out as (u, v, w, a*), (v, u, w, b*) with even corner
+    permutations, so every signed volume is unchanged."""
+    from xpbd_gpu import _native
+    from xpbd_gpu.mesh import kuhn_grid
+    m = kuhn_grid(5, 4, 3, 0.1, jitter=0.1, seed=3)
+    tets = np.asarray(m.tets, dtype=np.int64)
+    order, perm, n_pairs = _native.pair_tets(native_lib, tets, m.n_verts)
+    T = len(tets)
+    assert n_pairs == T // 2
+    assert sorted(order.tolist()) == list(range(T))
+    assert all(sorted(p.tolist()) == [0, 1, 2, 3] for p in perm)
+    new = np.take_along_axis(tets[order], perm, axis=1)
+    np.testing.assert_allclose(_signed_volumes(m.points, new), _signed_volumes(m.points, tets)[order], rtol=1e-12)
+    a, b = new[0::2], new[1::2]
+    np.testing.assert_array_equal(b[:, 0], a[:, 1])
+    np.testing.assert_array_equal(b[:, 1], a[:, 0])
+    np.testing.assert_array_equal(b[:, 2], a[:, 2])
+    assert not np.any(b[:, 3] == a[:, 3])
+
+
+def test_pair_tets_leaves_unpairable_tets_last(native_lib):
+    """Two tets sharing only an edge cannot pair, nor can a tet inverted
+    against its face neighbour (odd orientation).  Unpaired tets keep their
+    corners and are grouped two by two; every tet keeps its signed volume."""
+    from xpbd_gpu import _native
+    tets = np.array([[0, 1, 2, 3], [0, 1, 4, 5], [1, 2, 3, 6], [7, 8, 9, 10], [2, 3, 1, 12]], dtype=np.int64)
+    pts = np.random.default_rng(0).normal(size=(13, 3))
+    order, perm, n_pairs = _native.pair_tets(native_lib, tets, 13)
+    assert sorted(order.tolist()) == [0, 1, 2, 3, 4]
+    paired = set(order[:0].tolist())
+    for i in range(5):
+        if perm[i].tolist() != [0, 1, 2, 3]:
+            paired.add(int(order[i]))
+    assert len(paired) <= 2 * n_pairs
+    new = np.take_along_axis(tets[order], perm, axis=1)
+    np.testing.assert_allclose(_signed_volumes(pts, new), _signed_volumes(pts, tets)[order], rtol=1e-12)
+    with pytest.raises(Exception):
+        _native.pair_tets(native_lib, np.array([[0, 1, 2, 13]]), 13)

@@ -128,3 +128,49 @@ def test_batch_graph_and_direct_launch_agree():
     xa, xb = a.positions(), b.positions()
     diag = float(np.linalg.norm(xa.max(0) - xa.min(0)))
     assert np.abs(xa - xb).max() <= 1e-5 * diag
+
+
+@pytest.mark.parametrize("block,cheb", [(False, True), (True, False), (False, False)])
+def test_batch_split_and_plain_jacobi_match_single_bodies(block, cheb):
+    """The reference's method matrix (split NH / block NH, with and without the
+    Chebyshev acceleration, neohookean_solver.py:484-488) in the batched form:
+    every body follows its single-body solver."""
+    from xpbd_gpu.batched import XPBDBatchedSolver
+    bodies, sdfs, kw = _scene()
+    kw = dict(kw, block_neohookean_enable=block, cheb_enable=cheb)
+    batch = XPBDBatchedSolver(bodies, sdfs(), **kw)
+    singles = [_single(b, sdfs, kw) for b in bodies]
+    for f in range(5):
+        batch.solve()
+        X = batch.positions()
+        for k, s in enumerate(singles):
+            s.solve()
+            x = s.mesh.verts.x.to_numpy()
+            diag = float(np.linalg.norm(x.max(0) - x.min(0)))
+            assert np.abs(X[batch.body_vert_slices[k]] - x).max() <= POS_TOL * diag, "frame %d body %d" % (f, k)
+    batch.check_status()
+
+
+def test_batch_monitoring_records_match_single_bodies():
+    """monitor_convergence in the batch: per body and iteration, the mean
+    |det F - 1| and |tr F^T F - 3| (neohookean_solver.py:256-296, :509-532) of
+    the single-body solver."""
+    from xpbd_gpu.batched import XPBDBatchedSolver
+    bodies, sdfs, kw = _scene()
+    kw = dict(kw, monitor_convergence=True)
+    batch = XPBDBatchedSolver(bodies, sdfs(), **kw)
+    singles = [_single(b, sdfs, kw) for b in bodies]
+    for _ in range(3):
+        batch.solve()
+        for s in singles:
+            s.solve()
+    # the batch records the whole frame; a monitored single-body frame runs
+    # substep by substep, each writing history rows [0, K)
+    K, S = kw["constraints_iter"], kw["substeps_num"]
+    hb = batch.read_history()[:, (S - 1) * K:S * K]
+    for k, s in enumerate(singles):
+        hs = s.read_history(K)
+        np.testing.assert_allclose(hb[k, :, 2], hs[:, 2], rtol=5e-3, atol=1e-6)
+        np.testing.assert_allclose(hb[k, :, 3], hs[:, 3], rtol=5e-3, atol=1e-6)
+        recs = s.convergence_history[-K:]
+        np.testing.assert_allclose([r["hydro_error"] for r in recs], hs[:, 2], rtol=0, atol=0)
