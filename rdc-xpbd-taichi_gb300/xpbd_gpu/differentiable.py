@@ -9,6 +9,13 @@ runs hand-written adjoint kernels (``xpbd_substep_adjoint``).  The state is
 checkpointed once per substep (positions, velocities, rho_hat) and every
 substep's Jacobi iterations are recomputed on a tape before its reverse pass.
 
+Each simulation length gets a plan (``_Plan``): static checkpoint buffers
+and its two passes -- the forward (per substep: checkpoint, substep) and the
+backward (per substep in reverse: restore, tape, adjoint) -- each captured
+once as a CUDA graph and replayed, so an optimisation loop launches two
+graphs per step.  A simulation object holds one simulation in flight: its
+backward must run before its next forward.
+
 Differentiation conventions: the Chebyshev factor omega is a stop-gradient
 (it is a control heuristic of the residual ratio, neohookean_solver.py:
 495-546); active contact sets and the 2x2 pivot branch are piecewise
@@ -21,10 +28,77 @@ from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver, frame_chunks
 from xpbd_gpu.xpbd_base import _torch
 
 
+class _Plan:
+    """Checkpoints and passes of one simulation length of `sim` (a DiffSim or a
+    BatchedDiffSim): captured as two CUDA graphs with `use_graphs`, else run
+    directly."""
+
+    def __init__(self, sim, frames, use_graphs):
+        torch = _torch()
+        self.dts = sim.substep_dts(frames)
+        n = len(self.dts)
+        x4, v4 = sim._state()
+        self.ck_x = torch.empty((n,) + tuple(x4.shape), dtype=x4.dtype, device=x4.device)
+        self.ck_v = torch.empty((n,) + tuple(v4.shape), dtype=v4.dtype, device=v4.device)
+        self.ck_rho = torch.empty((n, sim.n_rho), dtype=torch.float64, device=x4.device)
+        self.generation = 0
+        self._graphs = None
+        if use_graphs:
+            gf, gb = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gf):
+                self._forward(sim)
+            with torch.cuda.graph(gb):
+                self._backward(sim)
+            self._graphs = (gf, gb)
+
+    def _forward(self, sim):
+        x4, v4 = sim._state()
+        for k, dt in enumerate(self.dts):
+            self.ck_x[k].copy_(x4)
+            self.ck_v[k].copy_(v4)
+            sim.rho_copy_to(self.ck_rho[k])
+            sim._substep(dt)
+
+    def _backward(self, sim):
+        x4, v4 = sim._state()
+        for k in reversed(range(len(self.dts))):
+            x4.copy_(self.ck_x[k])
+            v4.copy_(self.ck_v[k])
+            sim.rho_load_from(self.ck_rho[k])
+            sim._tape(self.dts[k])
+            sim._adjoint(self.dts[k])
+
+    def forward(self, sim):
+        self.generation += 1
+        if self._graphs:
+            self._graphs[0].replay()
+        else:
+            self._forward(sim)
+        return self.generation
+
+    def backward(self, sim, generation):
+        if generation != self.generation:
+            raise RuntimeError("a later forward of this simulation object overwrote the checkpoints; run "
+                               "each backward before the next forward")
+        if self._graphs:
+            self._graphs[1].replay()
+        else:
+            self._backward(sim)
+
+
+def _plan(sim, frames):
+    plans = sim.__dict__.setdefault("_plans", {})
+    if frames not in plans:
+        plans[frames] = _Plan(sim, frames, sim.use_graphs)
+    return plans[frames]
+
+
 class DiffSim:
     """A single body with per-tet materials and the buffers of its adjoint."""
 
-    def __init__(self, rest_pose, sdf, log_E, nu, scatter="atomic", **kw):
+    n_rho = 1
+
+    def __init__(self, rest_pose, sdf, log_E, nu, scatter="atomic", use_graphs=True, **kw):
         kw.setdefault("block_neohookean_enable", True)
         if not kw["block_neohookean_enable"]:
             raise ValueError("the adjoint supports the block projection only")
@@ -57,6 +131,23 @@ class DiffSim:
                                        self._yb.data_ptr(), self._dxb.data_ptr(), self._lamb.data_ptr(),
                                        self._cnt.data_ptr())
         self.initial_rho_hat = s.rho_hat
+        self.use_graphs = bool(use_graphs)
+
+    # -- the steps of a plan ---------------------------------------------------
+    def _state(self):
+        return self.solver._x4, self.solver._v4
+
+    def _substep(self, dt):
+        s = self.solver
+        _native.check(s._lib.xpbd_substep(s._handle, float(dt), 0, s._stream()))
+
+    def _tape(self, dt):
+        s = self.solver
+        _native.check(s._lib.xpbd_substep_tape(s._handle, float(dt), self.tape, s._stream()))
+
+    def _adjoint(self, dt):
+        s = self.solver
+        _native.check(s._lib.xpbd_substep_adjoint(s._handle, float(dt), self.tape, self.adj, s._stream()))
 
     def rho_copy_to(self, dst):
         """Stream-ordered copy of the device rho_hat into a 1-element float64 tensor."""
@@ -91,41 +182,26 @@ class DiffSim:
 class _Simulate(_torch().autograd.Function):
     @staticmethod
     def forward(ctx, x0, v0, log_E, nu, sim, frames):
-        torch = _torch()
         s = sim.solver
-        lib, stream = s._lib, s._stream()
         s.set_tet_materials(log_E.detach(), nu.detach())
         sim.set_state(x0.detach(), v0.detach())
         s.rho_hat = sim.initial_rho_hat
-        dts = sim.substep_dts(frames)
-        ckpts = []
-        rho = torch.empty(len(dts), dtype=torch.float64, device=s._device)
-        for k, dt in enumerate(dts):
-            sim.rho_copy_to(rho[k:k + 1])
-            ckpts.append((s._x4.clone(), s._v4.clone(), rho[k:k + 1]))
-            _native.check(lib.xpbd_substep(s._handle, float(dt), 0, stream))
-        ctx.sim, ctx.dts, ctx.ckpts = sim, dts, ckpts
+        plan = _plan(sim, frames)
+        ctx.sim, ctx.plan, ctx.generation = sim, plan, plan.forward(sim)
         ctx.save_for_backward(log_E, nu)
         return sim.positions()
 
     @staticmethod
     def backward(ctx, g_out):
         torch = _torch()
-        sim, dts, ckpts = ctx.sim, ctx.dts, ctx.ckpts
+        sim = ctx.sim
         log_E, nu = ctx.saved_tensors
-        s = sim.solver
-        lib, stream = s._lib, s._stream()
         sim._gx.zero_()
         sim._gv.zero_()
         sim._gx[:, :3] = g_out.to(torch.float32)[sim._vperm]
         sim._gmu.zero_()
         sim._gla.zero_()
-        for dt, (x4, v4, rho) in zip(reversed(dts), reversed(ckpts)):
-            s._x4.copy_(x4)
-            s._v4.copy_(v4)
-            sim.rho_load_from(rho)
-            _native.check(lib.xpbd_substep_tape(s._handle, float(dt), sim.tape, stream))
-            _native.check(lib.xpbd_substep_adjoint(s._handle, float(dt), sim.tape, sim.adj, stream))
+        ctx.plan.backward(sim, ctx.generation)
         gx = torch.empty((sim.V, 3), dtype=torch.float32, device=g_out.device)
         gv = torch.empty_like(gx)
         gx[sim._vperm] = sim._gx[:, :3]
@@ -171,7 +247,7 @@ class BatchedDiffSim:
     its own Chebyshev state, so the gradients of each body equal those of the
     same body simulated alone."""
 
-    def __init__(self, bodies, sdf, **kw):
+    def __init__(self, bodies, sdf, use_graphs=True, **kw):
         from xpbd_gpu.batched import Body, XPBDBatchedSolver
         kw.setdefault("block_neohookean_enable", True)
         if not kw["block_neohookean_enable"]:
@@ -203,6 +279,25 @@ class BatchedDiffSim:
                                        s._cnt.data_ptr())
         self.initial_rho_hat = torch.empty(s.n_bodies, dtype=torch.float64, device=dev)
         self.rho_copy_to(self.initial_rho_hat)
+        self.n_rho = s.n_bodies
+        self.use_graphs = bool(use_graphs)
+
+    # -- the steps of a plan ---------------------------------------------------
+    def _state(self):
+        return self.batch._x4, self.batch._v4
+
+    def _substep(self, dt):
+        s = self.batch
+        _native.check(s._lib.xpbd_batch_substep(s._handle, float(dt), 0, s._stream()), batch=True)
+
+    def _tape(self, dt):
+        s = self.batch
+        _native.check(s._lib.xpbd_batch_substep_tape(s._handle, float(dt), self.tape, s._stream()), batch=True)
+
+    def _adjoint(self, dt):
+        s = self.batch
+        _native.check(s._lib.xpbd_batch_substep_adjoint(s._handle, float(dt), self.tape, self.adj, s._stream()),
+                      batch=True)
 
     def rho_copy_to(self, dst):
         s = self.batch
@@ -239,42 +334,27 @@ def _n_tets(rest_pose):
 class _SimulateBatch(_torch().autograd.Function):
     @staticmethod
     def forward(ctx, x0, v0, log_E, nu, sim, frames):
-        torch = _torch()
         s = sim.batch
-        lib, stream = s._lib, s._stream()
         s.set_tet_materials(log_E.detach(), nu.detach())
         sim.set_state(x0.detach(), v0.detach())
         sim.rho_load_from(sim.initial_rho_hat)
-        dts = sim.substep_dts(frames)
-        ckpts = []
-        rho = torch.empty((len(dts), s.n_bodies), dtype=torch.float64, device=s._device)
-        for k, dt in enumerate(dts):
-            sim.rho_copy_to(rho[k])
-            ckpts.append((s._x4.clone(), s._v4.clone(), rho[k]))
-            _native.check(lib.xpbd_batch_substep(s._handle, float(dt), 0, stream), batch=True)
-        ctx.sim, ctx.dts, ctx.ckpts = sim, dts, ckpts
+        plan = _plan(sim, frames)
+        ctx.sim, ctx.plan, ctx.generation = sim, plan, plan.forward(sim)
         ctx.save_for_backward(log_E, nu)
         return sim.positions()
 
     @staticmethod
     def backward(ctx, g_out):
         torch = _torch()
-        sim, dts, ckpts = ctx.sim, ctx.dts, ctx.ckpts
+        sim = ctx.sim
         log_E, nu = ctx.saved_tensors
         s = sim.batch
-        lib, stream = s._lib, s._stream()
         sim._gx.zero_()
         sim._gv.zero_()
         sim._gx[s._vert_slot, :3] = g_out.to(torch.float32)
         sim._gmu.zero_()
         sim._gla.zero_()
-        for dt, (x4, v4, rho) in zip(reversed(dts), reversed(ckpts)):
-            s._x4.copy_(x4)
-            s._v4.copy_(v4)
-            sim.rho_load_from(rho)
-            _native.check(lib.xpbd_batch_substep_tape(s._handle, float(dt), sim.tape, stream), batch=True)
-            _native.check(lib.xpbd_batch_substep_adjoint(s._handle, float(dt), sim.tape, sim.adj, stream),
-                          batch=True)
+        ctx.plan.backward(sim, ctx.generation)
         gx = sim._gx[s._vert_slot, :3].clone()
         gv = sim._gv[s._vert_slot, :3].clone()
         gmu = sim._gmu[s._tet_slot]

@@ -114,3 +114,39 @@ def test_batched_per_tet_forward_matches_single_body():
             diag = float(np.linalg.norm(x.max(0) - x.min(0)))
             assert np.abs(X[batch.body_vert_slices[k]] - x).max() <= 1e-4 * diag
     batch.check_status()
+
+
+def test_graph_and_direct_plans_agree_and_guard_reuse():
+    """The captured-graph plan and the directly launched one give the same
+    positions and gradients (to float-atomic ordering); a backward after a
+    newer forward of the same simulation object is refused."""
+    import torch
+    from xpbd_gpu.batched import Body
+    from xpbd_gpu.differentiable import BatchedDiffSim, xpbd_simulate_batch
+    from xpbd_gpu.sdf import PlaneSdf
+    meshes = _bodies()[:2]
+    rng = np.random.default_rng(5)
+    logE = [np.log(1e5) + 0.2 * rng.normal(size=m.n_tets) for m in meshes]
+    kw = dict(frame_dt=1 / 60, dt=1 / 60, substeps_num=2, constraints_iter=6, cheb_enable=True, cheb_warmup=2)
+    dev = torch.device("cuda")
+    out = []
+    for graphs in (True, False):
+        sim = BatchedDiffSim([Body(m, tet_young_modulus=np.exp(le), tet_poisson_ratio=0.4, total_mass=1.0)
+                              for m, le in zip(meshes, logE)], [PlaneSdf([0, 0, 0], [0, 1, 0], True)],
+                             use_graphs=graphs, **kw)
+        x0 = torch.tensor(np.concatenate([m.points for m in meshes]), dtype=torch.float32, device=dev)
+        v0 = torch.zeros_like(x0, requires_grad=True)
+        le = torch.tensor(np.concatenate(logE), dtype=torch.float64, device=dev, requires_grad=True)
+        nu = torch.full((le.shape[0],), 0.4, dtype=torch.float64, device=dev)
+        xf = xpbd_simulate_batch(sim, x0, v0, le, nu, 2)
+        (xf ** 2).sum().backward()
+        out.append((xf.detach().cpu().numpy(), le.grad.cpu().numpy(), v0.grad.cpu().numpy()))
+        if graphs:
+            a = xpbd_simulate_batch(sim, x0, v0, le, nu, 2)
+            xpbd_simulate_batch(sim, x0, v0, le, nu, 2)
+            with pytest.raises(RuntimeError):
+                (a ** 2).sum().backward()
+    (xa, ga, va), (xb, gb, vb) = out
+    assert np.abs(xa - xb).max() <= 1e-6
+    assert np.linalg.norm(ga - gb) <= 1e-4 * np.linalg.norm(gb)
+    assert np.linalg.norm(va - vb) <= 1e-4 * np.linalg.norm(vb)
