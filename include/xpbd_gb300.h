@@ -45,13 +45,15 @@ enum xpbd_status {
 /* sdf.py:60-124 */
 enum xpbd_sdf_kind { XPBD_SDF_PLANE = 0, XPBD_SDF_SPHERE = 1, XPBD_SDF_CUBE = 2 };
 
-/* Scatter variants of the Jacobi accumulation. */
 /* Scatter variants of the Jacobi accumulation.
  *  ATOMIC: one thread per tet, four red.global.add.v4.f32 per tet.
  *  GATHER: per-corner contributions, then a deterministic vertex->tet CSR sum.
- *  PATCH:  one CTA per patch of P Morton-consecutive tets; the patch's vertex
- *          neighbourhood is staged in shared memory, contributions accumulate
- *          there and one red.global.add.v4.f32 per patch vertex is issued. */
+ *  PATCH:  one CTA per patch of P consecutive tets; the patch's vertex
+ *          neighbourhood is staged in shared memory once.  Each thread
+ *          projects tets_per_thread consecutive tets and merges the corners
+ *          they share in registers before red.global.add.v4.f32 (or, with
+ *          patch_reduce, contributions are summed per patch vertex in shared
+ *          memory and one reduction is issued per patch vertex). */
 enum xpbd_scatter { XPBD_SCATTER_ATOMIC = 0, XPBD_SCATTER_GATHER = 1, XPBD_SCATTER_PATCH = 2 };
 
 /* One SDF obstacle (sdf.py:7-124).  48 bytes. */

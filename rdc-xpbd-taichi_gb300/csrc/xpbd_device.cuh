@@ -341,7 +341,7 @@ __device__ __forceinline__ void add4(float4& a, const float4 b) {
   a.w += b.w;
 }
 
-// Tile projection of kTPT Morton-consecutive tets of one thread (records
+// Tile projection of kTPT consecutive tets of one thread (records
 // A, B, C, lid; multipliers L, stored to lam_out[k] as each tet is done), n of
 // them valid.  Vertex
 // positions come from the patch tile sp (global ids sg).  Consecutive tets of

@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float cD, fl
 }
 
 // ---------------------------------------------------------------------------
-// Tile variant.  Patch p = kP Morton-consecutive tets (arrays padded to a
+// Tile variant.  Patch p = kP consecutive tets of the solver order (arrays padded to a
 // multiple of the patch size) whose <= 256 vertices are listed in
 // pverts[voff[p] .. voff[p+1]).  Persistent CTAs walk the patches; one thread
 // streams the next patch's tet records (48 bytes per tet: 4 u8 local corner
@@ -709,7 +709,7 @@ __global__ void __launch_bounds__(kP) k_project_patch1(Dev d, int cur, float cD,
   }
 }
 
-// Tile variant, one CTA per patch, kTPT Morton-consecutive tets per thread;
+// Tile variant, one CTA per patch, kTPT consecutive tets per thread;
 // corners shared along a thread's chain are summed in registers before the
 // global reduction (project_chain).
 template <bool kBlockMode, bool kFirst, bool kPrecise, int kP, int kTPT>

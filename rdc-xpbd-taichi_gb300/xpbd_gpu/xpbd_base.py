@@ -323,7 +323,7 @@ class XPBDSolverBase:
         self._corner = torch.zeros((4 * T, 4), dtype=torch.float32, device=self._device)
 
     def _ensure_patch_buffers(self):
-        """Patches of P Morton-consecutive tets with <= 256 vertices each (P =
+        """Patches of P consecutive tets (solver order) with <= 256 vertices each (P =
         the largest of 256, 128, 64 not above ``patch_tets`` whose patches all
         fit); returns False if none fits."""
         if self._tet_lid is not None:
