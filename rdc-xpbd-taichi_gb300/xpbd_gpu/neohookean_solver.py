@@ -236,6 +236,14 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         return a, b
 
     # -- history ------------------------------------------------------------------
+    @property
+    def residual_history(self):
+        """r_hat of every Jacobi iteration of the last frame (or of the last
+        monitored substep), in iteration order: the residual curve that drives
+        the Chebyshev omega (neohookean_solver.py:492-504)."""
+        rows = self.read_history(self.constraints_iter if self.monitor_convergence else None)
+        return rows[:, 0].tolist()
+
     def read_history(self, n=None):
         """(n, 4) float64 rows {r_hat, omega, hydro_error, dev_error} of the last
         frame (or of the last solve_step), in iteration order."""

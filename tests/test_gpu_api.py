@@ -135,3 +135,13 @@ def test_profiling_counts_launches_and_keeps_results(use_graph):
         assert (v["ms"] > 0.0) == (v["launches"] > 0), (k, v)
     np.testing.assert_array_equal(s.mesh.verts.x.to_numpy(), ref.mesh.verts.x.to_numpy())
     assert s.read_profile()["project"]["launches"] == 0
+
+
+def test_residual_history_is_the_last_frames_curve():
+    _, s = _solver(monitor_convergence=False)
+    s.solve()
+    from xpbd_gpu.neohookean_solver import frame_chunks
+    r = s.residual_history
+    assert len(r) == len(frame_chunks(s.frame_dt, s.dt)) * s.substeps_num * s.constraints_iter
+    np.testing.assert_array_equal(np.asarray(r), s.read_history()[:, 0])
+    assert all(np.isfinite(r)) and max(r) > 0.0
