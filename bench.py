@@ -549,8 +549,8 @@ def fp64_error(solver_factory, mesh, specs, kw, frames, warm_start=11, warm_fram
     `warm_frames` frames in contact, all runs started from the GPU state after `warm_start`
     frames; in (b) also the deviation of the FP32 C restatement from the same state (what an
     FP32 run of the reference algorithm itself departs from FP64) and the relative difference
-    of the per-iteration residual curves (only where the float64 r_hat is above 1e-5, the
-    FP32 round-off floor of a body at rest)."""
+    of the per-iteration residual curves (only where the float64 r_hat is above 1e-4, well
+    above the FP32 floor of about 1e-5 of a body at rest on this mesh)."""
     threads = os.cpu_count() or 1
     S, K = kw["substeps_num"], kw["constraints_iter"]
     diag = float(np.linalg.norm(mesh.points.max(0) - mesh.points.min(0)))
@@ -588,7 +588,7 @@ def fp64_error(solver_factory, mesh, specs, kw, frames, warm_start=11, warm_fram
             f32.solve()
         mx32 = float(np.abs(f32.x.astype(np.float64) - ref.x).max()) / diag
         r_gpu = solver.read_history()[:S * K, 0]
-        live = hist > 1e-5
+        live = hist > 1e-4
         rel = np.abs(r_gpu - hist)[live] / hist[live]
         out["in_contact"] = {"start_frame": max(warm_start, frames), "frames": warm_frames,
                              "max_dev_over_bbox_diag": mx, "rms_dev_over_bbox_diag": rms,

@@ -31,8 +31,9 @@ def test_c2_size_against_float64_reference():
     gpu.solve()
     ref.solve(1, hist)
     assert np.abs(gpu.mesh.verts.x.to_numpy() - ref.x).max() <= 1e-4 * diag
-    # free fall in the first frame: r_hat is FP32 round-off on the GPU, ~0 in FP64
-    assert np.abs(gpu.read_history()[:S * K, 0]).max() <= 1e-5
+    # free fall in the first frame: r_hat is the FP32 floor on the GPU (positions
+    # near 2 m carry 2.4e-7 m ulps against 1/64 m cells), ~0 in FP64
+    assert np.abs(gpu.read_history()[:S * K, 0]).max() <= 5e-5
     # in contact
     for _ in range(10):
         gpu.solve()
@@ -51,7 +52,7 @@ def test_c2_size_against_float64_reference():
     dev_f32 = np.abs(f32.x.astype(np.float64) - ref.x).max()
     assert dev_gpu <= dev_f32 + 1e-4 * diag, (dev_gpu / diag, dev_f32 / diag)
     r = gpu.read_history()[:S * K, 0]
-    live = hist > 1e-5
+    live = hist > 1e-4  # well above the FP32 floor of a body at rest
     assert live.sum() > 0.5 * live.size
     rel = np.abs(r[live] - hist[live]) / hist[live]
     rel32 = np.abs(hist32[live] - hist[live]) / hist[live]
