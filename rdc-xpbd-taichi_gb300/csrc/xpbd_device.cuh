@@ -332,8 +332,9 @@ __device__ __forceinline__ float det9(const float m[9]) {
 // Resident CTAs per SM the tile projections are compiled for, by tets per
 // thread: with 2, 9 CTAs of 128 threads cap a thread at 56 registers.  The
 // chain needs 72 without spills, but the few spilled bytes (16-24 per
-// thread) cost less than the latency that two more CTAs hide: the C2
-// projection measured 37.5 us at 7 CTAs, 36.5 at 8 and 35.7 at 9; 10 CTAs
+// thread) cost less than the latency that two more CTAs hide: on a 64^3-cell
+// Kuhn cube (1.57 M tets) the projection measured 37.5 us at 7 CTAs, 36.5 at
+// 8 and 35.7 at 9; 10 CTAs
 // (48 registers) spill 60-84 bytes.  Otherwise no minimum.
 __host__ __device__ constexpr int project_min_blocks(int tpt) { return tpt == 2 ? 9 : 1; }
 
