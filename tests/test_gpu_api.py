@@ -145,3 +145,26 @@ def test_residual_history_is_the_last_frames_curve():
     assert len(r) == len(frame_chunks(s.frame_dt, s.dt)) * s.substeps_num * s.constraints_iter
     np.testing.assert_array_equal(np.asarray(r), s.read_history()[:, 0])
     assert all(np.isfinite(r)) and max(r) > 0.0
+
+
+def test_usda_export_from_device(tmp_path):
+    """The solver's positions leave the GPU through pinned buffers and land in
+    the layer as one time sample per rendered frame (usd_export.py:58-92)."""
+    from xpbd_gpu.usda import USDMeshRenderer, add_sdfs, read_usda_points
+    _, s = _solver(monitor_convergence=False)
+    r = USDMeshRenderer(str(tmp_path / "run.usda"), 4, 60)
+    r.add_dynamic_mesh(s.mesh.verts.x, s.indices, "deformable_mesh")
+    add_sdfs(r, s.sdfs)
+    frames = []
+    for _ in range(4):
+        s.solve()
+        r.render()
+        frames.append(s.mesh.verts.x.to_numpy())
+    r.save()
+    r.close()
+    samples = read_usda_points(r.filepath)
+    assert sorted(samples) == [1, 2, 3, 4]
+    for t, x in enumerate(frames, start=1):
+        np.testing.assert_allclose(samples[t], x, rtol=1e-7, atol=1e-7)
+    text = open(r.filepath).read()
+    assert text.count("def Sphere") + text.count("def Cube") + text.count("def Mesh") == 1 + len(s.sdfs)
