@@ -345,29 +345,45 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
 }
 
 // post_solve + Chebyshev mix with the omega of the vertex block's body.
+// Each thread takes kBUpdateBlocks vertices, one in each of consecutive
+// 256-vertex blocks, so that all of its loads are in flight together.
+constexpr int kBUpdateBlocks = 2;
 template <bool kCheb, bool kFirstIt>
 __global__ void __launch_bounds__(256) kb_update(BDev d, int cur, float gamma) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.V) return;
+  const int vb0 = blockIdx.x * kBUpdateBlocks;
   // every load is issued before the first store: as far as the compiler
   // knows the buffers may alias, so a load after a store would wait for it
-  const float4 pc = d.p[cur][i];
-  const float4 D = d.dx[i];
-  float4 yp = pc;
-  float om = 1.f;
-  if (kCheb) {
-    if (!kFirstIt) yp = d.p[cur ^ 1][i];
-    om = (float)d.bs[__ldg(d.vblock_body + blockIdx.x)].omega;
+  float4 pc[kBUpdateBlocks], D[kBUpdateBlocks], yp[kBUpdateBlocks];
+  float om[kBUpdateBlocks];
+#pragma unroll
+  for (int k = 0; k < kBUpdateBlocks; ++k) {
+    const int i = (vb0 + k) * 256 + threadIdx.x;
+    om[k] = 1.f;
+    if (i < d.V) {
+      pc[k] = d.p[cur][i];
+      D[k] = d.dx[i];
+      yp[k] = pc[k];
+      if (kCheb) {
+        if (!kFirstIt) yp[k] = d.p[cur ^ 1][i];
+        om[k] = (float)d.bs[__ldg(d.vblock_body + vb0 + k)].omega;
+      }
+    }
   }
-  d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  const float3 xp = post_position(pc, D);
-  if (kCheb) {
-    const float nx = gamma * (xp.x - pc.x) + pc.x;
-    const float ny = gamma * (xp.y - pc.y) + pc.y;
-    const float nz = gamma * (xp.z - pc.z) + pc.z;
-    d.p[cur ^ 1][i] = make_float4(yp.x + om * (nx - yp.x), yp.y + om * (ny - yp.y), yp.z + om * (nz - yp.z), pc.w);
-  } else {
-    d.p[cur][i] = make_float4(xp.x, xp.y, xp.z, pc.w);
+#pragma unroll
+  for (int k = 0; k < kBUpdateBlocks; ++k) {
+    const int i = (vb0 + k) * 256 + threadIdx.x;
+    if (i >= d.V) break;
+    d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float3 xp = post_position(pc[k], D[k]);
+    if (kCheb) {
+      const float nx = gamma * (xp.x - pc[k].x) + pc[k].x;
+      const float ny = gamma * (xp.y - pc[k].y) + pc[k].y;
+      const float nz = gamma * (xp.z - pc[k].z) + pc[k].z;
+      d.p[cur ^ 1][i] = make_float4(yp[k].x + om[k] * (nx - yp[k].x), yp[k].y + om[k] * (ny - yp[k].y),
+                                    yp[k].z + om[k] * (nz - yp[k].z), pc[k].w);
+    } else {
+      d.p[cur][i] = make_float4(xp.x, xp.y, xp.z, pc[k].w);
+    }
   }
 }
 
@@ -666,7 +682,7 @@ void iteration_b(Batch* s, int it, float dt, int rec, cudaStream_t st) {
     else residual_b<false, true>(s, a, st);
   }
   BProf pr(s, XPBD_K_UPDATE, st);
-  const int g = nblk(s->d.V);
+  const int g = (nblk(s->d.V) + kBUpdateBlocks - 1) / kBUpdateBlocks;
   if (cheb) {
     if (it == 0) kb_update<true, true><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma);
     else kb_update<true, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma);

@@ -264,6 +264,45 @@ __device__ __forceinline__ void red_add_v4(float4* addr, float a, float b, float
                : "memory");
 }
 
+// L2 eviction priority for read-only tet records.  With `keep` the records
+// are loaded evict_last, so a mesh whose records fit in L2 keeps them there
+// from one sweep to the next instead of losing them to the position and
+// accumulator traffic; otherwise evict_normal (a plain load).
+__device__ __forceinline__ uint64_t l2_policy(bool keep) {
+  uint64_t pol;
+  if (keep)
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  else
+    asm("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+__device__ __forceinline__ float4 ldg_hint(const float4* p, uint64_t pol) {
+  float4 r;
+  asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+      : "l"(p), "l"(pol));
+  return r;
+}
+
+__device__ __forceinline__ float ldg_hint(const float* p, uint64_t pol) {
+  float r;
+  asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(r) : "l"(p), "l"(pol));
+  return r;
+}
+
+__device__ __forceinline__ uint32_t ldg_hint(const uint32_t* p, uint64_t pol) {
+  uint32_t r;
+  asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+  return r;
+}
+
+__device__ __forceinline__ int ldg_hint(const int* p, uint64_t pol) {
+  int r;
+  asm("ld.global.nc.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+  return r;
+}
+
 // ---------------------------------------------------------------------------
 // Bulk asynchronous copies (TMA, cp.async.bulk) tracked by an mbarrier.
 // ---------------------------------------------------------------------------

@@ -30,6 +30,7 @@
 namespace xpbd {
 
 constexpr int kBlock = 256;
+constexpr int kUpdateVerts = 2;  // vertices per thread in k_update
 
 // FP64 solver state that lives on the device (neohookean_solver.py:59-69).
 struct DevState {
@@ -63,6 +64,7 @@ struct Dev {
   float4* corner;
   const int* perm;  // solver vertex i <- caller vertex perm[i] (nullptr = identity)
   int paired;       // tets laid out by xpbd_pair_tets
+  int l2_keep;      // tile sweeps load the tet records evict_last
   // tile variant: patch p = tets [p*P, (p+1)*P), vertices verts[voff[p]..voff[p+1])
   int n_patches, P, n_pverts;
   const uint32_t* lid;
@@ -152,32 +154,42 @@ __global__ void __launch_bounds__(kBlock) k_gather(Dev d) {
 // is written to p[1-cur] (which held y_prev), else x_post goes to p[cur].
 template <bool kCheb, bool kFirstIt, bool kResetDx>
 __global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.V) return;
+  // kUpdateVerts vertices per thread, kBlock apart: all of a thread's loads
+  // are in flight together, and the grid is a quarter of a one-per-vertex one
+  const int base = blockIdx.x * (kBlock * kUpdateVerts) + threadIdx.x;
   // every load is issued before the first store: as far as the compiler
   // knows the buffers may alias, so a load after a store would wait for it
-  const float4 pc = d.p[cur][i];
-  const float4 D = d.dx[i];
-  float4 yp = pc;
-  float om = 1.f;
-  if (kCheb) {
-    if (!kFirstIt) yp = d.p[cur ^ 1][i];
-    om = (float)d.st->omega;
+  float4 pc[kUpdateVerts], D[kUpdateVerts], yp[kUpdateVerts];
+#pragma unroll
+  for (int k = 0; k < kUpdateVerts; ++k) {
+    const int i = base + k * kBlock;
+    if (i < d.V) {
+      pc[k] = d.p[cur][i];
+      D[k] = d.dx[i];
+      yp[k] = (kCheb && !kFirstIt) ? d.p[cur ^ 1][i] : pc[k];
+    }
   }
-  if (kResetDx) d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  float3 xp = make_float3(pc.x, pc.y, pc.z);
-  if (D.w > 0.f) {
-    xp.x += D.x / D.w;
-    xp.y += D.y / D.w;
-    xp.z += D.z / D.w;
-  }
-  if (kCheb) {
-    const float nx = gamma * (xp.x - pc.x) + pc.x;
-    const float ny = gamma * (xp.y - pc.y) + pc.y;
-    const float nz = gamma * (xp.z - pc.z) + pc.z;
-    d.p[cur ^ 1][i] = make_float4(yp.x + om * (nx - yp.x), yp.y + om * (ny - yp.y), yp.z + om * (nz - yp.z), pc.w);
-  } else {
-    d.p[cur][i] = make_float4(xp.x, xp.y, xp.z, pc.w);
+  const float om = kCheb ? (float)d.st->omega : 1.f;
+#pragma unroll
+  for (int k = 0; k < kUpdateVerts; ++k) {
+    const int i = base + k * kBlock;
+    if (i >= d.V) break;
+    if (kResetDx) d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float3 xp = make_float3(pc[k].x, pc[k].y, pc[k].z);
+    if (D[k].w > 0.f) {
+      xp.x += D[k].x / D[k].w;
+      xp.y += D[k].y / D[k].w;
+      xp.z += D[k].z / D[k].w;
+    }
+    if (kCheb) {
+      const float nx = gamma * (xp.x - pc[k].x) + pc[k].x;
+      const float ny = gamma * (xp.y - pc[k].y) + pc[k].y;
+      const float nz = gamma * (xp.z - pc[k].z) + pc[k].z;
+      d.p[cur ^ 1][i] = make_float4(yp[k].x + om * (nx - yp[k].x), yp[k].y + om * (ny - yp[k].y),
+                                    yp[k].z + om * (nz - yp[k].z), pc[k].w);
+    } else {
+      d.p[cur][i] = make_float4(xp.x, xp.y, xp.z, pc[k].w);
+    }
   }
 }
 
@@ -728,6 +740,7 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) k_project
   float C[kTPT];
   uint32_t lid[kTPT];
   float2 L[kTPT];
+  const uint64_t pol = l2_policy(d.l2_keep != 0);
 #pragma unroll
   for (int k = 0; k < kTPT; ++k) {
     A[k] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -736,16 +749,16 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) k_project
     lid[k] = 0u;
     L[k] = make_float2(0.f, 0.f);
     if (l0 + k < nt) {
-      A[k] = __ldg(d.dm_a + t0 + l0 + k);
-      B[k] = __ldg(d.dm_b + t0 + l0 + k);
-      C[k] = __ldg(d.dm_c + t0 + l0 + k);
-      lid[k] = __ldg(d.lid + t0 + l0 + k);
+      A[k] = ldg_hint(d.dm_a + t0 + l0 + k, pol);
+      B[k] = ldg_hint(d.dm_b + t0 + l0 + k, pol);
+      C[k] = ldg_hint(d.dm_c + t0 + l0 + k, pol);
+      lid[k] = ldg_hint(d.lid + t0 + l0 + k, pol);
       if (!kFirst) L[k] = d.lam[t0 + l0 + k];
     }
   }
   const float4* P = d.p[cur];
   for (int j = threadIdx.x; j < nv; j += kThreads) {
-    const int g = __ldg(d.pverts + vb + j);
+    const int g = ldg_hint(d.pverts + vb + j, pol);
     sg[j] = g;
     sp[j] = ldg4(P + g);
   }
@@ -808,6 +821,7 @@ __global__ void __launch_bounds__(kP / kTPT) k_residual_patchN(Dev d, SweepArgs 
   const float4* P = d.p[a.cur];
   const int n = d.n_patches;
   const int l0 = kTPT * threadIdx.x;
+  const uint64_t pol = l2_policy(d.l2_keep != 0);
   for (int q = blockIdx.x; q < n; q += gridDim.x) {
     const int p = a.reverse ? n - 1 - q : q;
     const int vb = __ldg(d.voff + p);
@@ -820,16 +834,16 @@ __global__ void __launch_bounds__(kP / kTPT) k_residual_patchN(Dev d, SweepArgs 
 #pragma unroll
     for (int k = 0; k < kTPT; ++k) {
       if (t0 + k < d.T) {
-        A[k] = __ldg(d.dm_a + t0 + k);
-        B[k] = __ldg(d.dm_b + t0 + k);
-        C[k] = __ldg(d.dm_c + t0 + k);
-        lid[k] = __ldg(d.lid + t0 + k);
+        A[k] = ldg_hint(d.dm_a + t0 + k, pol);
+        B[k] = ldg_hint(d.dm_b + t0 + k, pol);
+        C[k] = ldg_hint(d.dm_c + t0 + k, pol);
+        lid[k] = ldg_hint(d.lid + t0 + k, pol);
         L[k] = kRes ? d.lam[t0 + k] : make_float2(0.f, 0.f);
       }
     }
     __syncthreads();  // the previous patch's readers are done with sp
     for (int j = threadIdx.x; j < nv; j += kThreads) {
-      const int g = __ldg(d.pverts + vb + j);
+      const int g = ldg_hint(d.pverts + vb + j, pol);
       const float3 x = post_position(ldg4(P + g), ldg4(d.dx + g));
       sp[j] = make_float4(x.x, x.y, x.z, 0.f);
     }
@@ -1319,7 +1333,7 @@ void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
   }
   const bool cheb = p.cheb_enable != 0, mon = p.monitor != 0;
   if (cheb || mon) launch_residual(s, sweep_args(s, it, dt, rec), st);
-  const int g = blocks_for(s->d.V);
+  const int g = (s->d.V + kBlock * kUpdateVerts - 1) / (kBlock * kUpdateVerts);
   const bool reset = p.scatter != XPBD_SCATTER_GATHER;
   Prof prof(s, XPBD_K_UPDATE, st);
   if (cheb) {
@@ -1572,6 +1586,15 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
   if (has_patch) {
     e = cudaMemcpy(&d.n_pverts, d.voff + d.n_patches, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cleanup(fail(XPBD_ERR_CUDA, std::string("patch offsets: ") + cudaGetErrorString(e)));
+    // The tile sweeps load the read-only records (inv_Dm, local ids, patch
+    // vertex lists) evict_last when they and the per-iteration state
+    // (positions, previous positions, accumulators, multipliers) fit in
+    // 80% of L2; past that, evict_last records would push the state out.
+    int l2 = 0;
+    if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, s->device) != cudaSuccess) l2 = 0;
+    const double records = 40.0 * d.T + 4.0 * d.n_pverts;
+    const double state = 48.0 * d.V + 8.0 * d.T;
+    d.l2_keep = records + state <= 0.8 * l2;
   }
   {
     int bps = 0;
