@@ -861,8 +861,11 @@ def run_gb300(args):
     traffic = {("patch", 2): 89.10e6, ("patch", 1): 89.4e6}.get((scatter, tpt))
     if scatter == "atomic":
         traffic = 115.2e6
+    # the same with warm caches inside a frame (ncu --cache-control none, mean of
+    # two launches; profiles/l2_residency_c2_64cube.md): the sweeps run mostly from L2
+    traffic_in_frame = 29.05e6 if (scatter, tpt) == ("patch", 2) else None
     if pipe != 0 or args.patch_reduce != 0 or args.workload != "c2" or (scatter == "patch" and patch_tets != 256):
-        traffic = None
+        traffic = traffic_in_frame = None
     iter_bytes = 136.0 * T + 128.0 * V
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -877,7 +880,7 @@ def run_gb300(args):
         "gpu_launches": launches_per_frame * args.steps,
         "roofline": {"bound": "hbm", "kernel": kernel_name,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "traffic": traffic,
+                     "peak_source": peak_src, "traffic": traffic, "traffic_in_frame": traffic_in_frame,
                      "bytes_per_launch": proj_bytes, "ms_per_launch": proj_ms,
                      "timing": "CUDA events recorded by event nodes inside the frame graph (the timed "
                                "region's graph plus those nodes), %d frames after the timed region"
