@@ -874,6 +874,7 @@ def run_gb300(args):
         "config": {"workload": desc, "step": "one frame (%d tet-iterations)" % frame_units,
                    "scatter": scatter, "patch_tets": patch_tets, "sweep_order": args.sweep_order,
                    "patch_pipeline": pipe, "tets_per_thread": tpt, "tet_pairs": solver.n_tet_pairs,
+                   "records_evict_last": bool(solver.set_l2_hint()),
                    "l2": "flushed between steps (%d MiB write)" % (L2_FLUSH_BYTES >> 20),
                    "parallelism": "replicas" if world > 1 else "single GPU", "graph": "one CUDA graph per frame"},
         "frames_per_s": 1e3 / ms_per_step * world,

@@ -225,6 +225,14 @@ enum xpbd_kernel_class {
  * solve_step, neohookean_solver.py:454-560.) */
 int xpbd_set_profiling(void* handle, int32_t enable);
 
+/* L2 eviction policy of the read-only tet records in the tile (PATCH)
+ * sweeps.  mode -1: automatic, the default: evict_last when the records and
+ * the per-iteration state fit in 80% of the device's L2, else plain loads;
+ * 0: plain loads; 1: evict_last.  `active` (may be NULL) receives the
+ * policy in force (0 or 1).  Results do not depend on it.  No counterpart in
+ * the reference (Taichi leaves caching to the hardware). */
+int xpbd_set_l2_hint(void* handle, int32_t mode, int32_t* active);
+
 /* Accumulated device milliseconds and launch counts per kernel class
  * (arrays of n <= XPBD_K_COUNT); synchronises `stream`; `reset` clears. */
 int xpbd_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, int32_t reset, void* stream);

@@ -1093,6 +1093,7 @@ struct GraphKey {
 struct Solver {
   // profiling (xpbd_set_profiling): event pairs per kernel class
   bool profiling = false;
+  int l2_auto = 0;  // automatic L2 policy of the tile sweeps (xpbd_set_l2_hint)
   std::vector<cudaEvent_t> pool;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[XPBD_K_COUNT];
   double prof_ms[XPBD_K_COUNT] = {0, 0, 0, 0, 0, 0};
@@ -1594,7 +1595,8 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
     if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, s->device) != cudaSuccess) l2 = 0;
     const double records = 40.0 * d.T + 4.0 * d.n_pverts;
     const double state = 48.0 * d.V + 8.0 * d.T;
-    d.l2_keep = records + state <= 0.8 * l2;
+    s->l2_auto = records + state <= 0.8 * l2;
+    d.l2_keep = s->l2_auto;
   }
   {
     int bps = 0;
@@ -1808,6 +1810,19 @@ int xpbd_set_profiling(void* handle, int32_t enable) {
   Solver* s = static_cast<Solver*>(handle);
   if (!s) return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle");
   s->profiling = enable != 0;
+  return XPBD_OK;
+}
+
+int xpbd_set_l2_hint(void* handle, int32_t mode, int32_t* active) {
+  Solver* s = static_cast<Solver*>(handle);
+  if (!s) return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle");
+  if (mode < -1 || mode > 1) return fail(XPBD_ERR_INVALID_ARGUMENT, "l2 hint mode must be -1, 0 or 1");
+  const int keep = mode < 0 ? s->l2_auto : mode;
+  if (keep != s->d.l2_keep) {
+    s->d.l2_keep = keep;
+    drop_graph(s);  // the frame graph holds the kernels' Dev by value
+  }
+  if (active) *active = s->d.l2_keep;
   return XPBD_OK;
 }
 

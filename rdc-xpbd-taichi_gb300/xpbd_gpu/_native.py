@@ -125,6 +125,7 @@ _SIGNATURES = {
     "xpbd_residual_noalloc": (ctypes.c_int, [ctypes.POINTER(XpbdBody), _P, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_float, ctypes.c_int32, _P, _P]),
     "xpbd_set_profiling": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "xpbd_set_l2_hint": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
     "xpbd_read_profile": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
                                          ctypes.c_int32, ctypes.c_int32, _P]),
     "xpbd_morton_order": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int32, _P, _P]),

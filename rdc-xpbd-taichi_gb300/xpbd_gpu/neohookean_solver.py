@@ -260,6 +260,14 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         frame graph carries them as event record nodes)."""
         _native.check(self._lib.xpbd_set_profiling(self._handle, 1 if enable else 0))
 
+    def set_l2_hint(self, mode=-1):
+        """L2 policy of the tile sweeps' read-only tet records: -1 automatic
+        (evict_last when records + state fit in 80% of L2), 0 plain loads,
+        1 evict_last.  Returns the policy in force (0 or 1)."""
+        on = _native.ctypes.c_int32(0)
+        _native.check(self._lib.xpbd_set_l2_hint(self._handle, int(mode), _native.ctypes.byref(on)))
+        return int(on.value)
+
     def read_profile(self, reset=False):
         """{kernel class: {'ms': total device ms, 'launches': n}} since the last reset."""
         n = len(_native.KERNEL_CLASSES)

@@ -168,3 +168,30 @@ def test_usda_export_from_device(tmp_path):
         np.testing.assert_allclose(samples[t], x, rtol=1e-7, atol=1e-7)
     text = open(r.filepath).read()
     assert text.count("def Sphere") + text.count("def Cube") + text.count("def Mesh") == 1 + len(s.sdfs)
+
+
+def test_l2_hint_modes_keep_results():
+    """The tile sweeps' L2 policy (evict_last records or plain loads) changes
+    no result beyond the float-atomic ordering noise of the patch scatter;
+    the automatic policy keeps records of a small mesh, and the forced
+    modes are reported back."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
+    mesh, specs, kw, _ = bench.workload("c1")
+    kw = dict(kw, scatter="patch")
+    xs = []
+    for mode in (0, 1):
+        s = XPBDNeoHookeanSolver(mesh, bench.product_sdfs(specs), **kw)
+        assert s.set_l2_hint() == 1
+        assert s.set_l2_hint(mode) == mode
+        for _ in range(3):
+            s.solve()
+        s.check_status()
+        xs.append(s.mesh.verts.x.to_numpy())
+    with pytest.raises(RuntimeError):
+        s.set_l2_hint(2)
+    diag = float(np.linalg.norm(mesh.points.max(0) - mesh.points.min(0)))
+    assert np.abs(xs[0] - xs[1]).max() <= 1e-5 * diag
