@@ -8,8 +8,9 @@
 //                  Jacobi scatter of dx + constraint count       neohookean_solver.py:144-254,358-451
 //     [gather](V): deterministic CSR sum of per-corner dx (gather variant only)
 //     residual(T): r_hat / monitoring sums at post-Jacobi positions,
-//                  FP64 reduction, last block updates rho_hat/omega  :298-329, :492-546
-//     update  (V): post_solve + Chebyshev mix, dx reset          :115-142, :548-549
+//                  FP64 block reduction into the sweep's sums    :298-329, :492-504
+//     update  (V): rho_hat / omega from those sums (per CTA),
+//                  post_solve + Chebyshev mix, dx reset          :115-142, :537-549
 //   end     (V): velocity update                                xpbd_base.py:148-160
 // The predicted positions ping-pong between p0/p1: the Chebyshev mix writes
 // x_{k+1} over y_{k-1} in place, so no buffer copies are needed
@@ -33,13 +34,21 @@ constexpr int kBlock = 256;
 constexpr int kUpdateVerts = 2;  // vertices per thread in k_update
 
 // FP64 solver state that lives on the device (neohookean_solver.py:59-69).
-struct DevState {
-  double acc[3];        // residual sum, |C_H| sum, |C_D| sum of the running sweep
-  unsigned int ticket;  // blocks finished in the running sweep
-  int has_prev;         // prev_r_hat is not None
-  double rho_hat;       // persists across substeps and frames
+// Chebyshev state entering one Jacobi iteration of a substep.
+struct SweepSlot {
+  double rho_hat;
   double prev_r_hat;
-  double omega;         // omega of the latest iteration of this substep
+  double omega;  // omega of the previous iteration of this substep
+  int has_prev;  // prev_r_hat is not None
+};
+
+// Iteration k's residual sweep adds into acc[k & 1]; iteration k's update
+// reads slot[k & 1] and acc[k & 1], and its first CTA writes slot[(k+1) & 1]
+// and clears acc[(k+1) & 1], so no kernel reads what it writes.
+struct DevState {
+  double acc[2][3];     // residual sum, |C_H| sum, |C_D| sum of a sweep
+  SweepSlot slot[2];
+  double rho_hat;       // persists across substeps and frames
   int nonfinite;        // sticky: a residual sum was NaN/Inf
   int bad_mesh;         // set by the index validation kernel
   int timeout;          // sticky: a bounded mbarrier wait gave up
@@ -91,8 +100,12 @@ template <bool kPredict, bool kSdf>
 __global__ void __launch_bounds__(kBlock) k_begin(Dev d, float dt, float gx, float gy, float gz, int dst) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (kSdf && i == 0) {
-    d.st->has_prev = 0;
-    d.st->omega = 1.0;
+    SweepSlot& s0 = d.st->slot[0];
+    s0.rho_hat = d.st->rho_hat;
+    s0.prev_r_hat = 0.0;
+    s0.omega = 1.0;
+    s0.has_prev = 0;
+    d.st->acc[0][0] = d.st->acc[0][1] = d.st->acc[0][2] = 0.0;
   }
   if (i >= d.V) return;
   const float4 xi = d.x[i];
@@ -152,8 +165,61 @@ __global__ void __launch_bounds__(kBlock) k_gather(Dev d) {
 // (:131-142, :548-549).  x_post = p[cur] + dx / count; with kCheb the result
 //   y_prev + omega * (gamma * (x_post - y_curr) + y_curr - y_prev)
 // is written to p[1-cur] (which held y_prev), else x_post goes to p[cur].
+// What the update of iteration `it` needs to finish its residual sweep.
+struct UpdArgs {
+  int it, rec, last, warmup;
+  int res, mon;  // the sweep summed residuals (Chebyshev) / monitoring means
+  double rho_min, rho_max, rho_beta;
+};
+
+// The end of a residual sweep (neohookean_solver.py:495-504, :537-546): r_hat
+// from the sweep's sums, the rho_hat recurrence and omega of iteration u.it.
+// Every CTA of the update evaluates it (thread 0); CTA 0 also stores the
+// state entering the next iteration, clears the next sweep's accumulators,
+// writes history row `rec` = {r_hat, omega, hydro, dev}, and at the last
+// iteration the persistent rho_hat.
+__device__ __forceinline__ float sweep_step(const Dev& d, const UpdArgs& u) {
+  DevState* st = d.st;
+  const SweepSlot c = st->slot[u.it & 1];
+  const double* acc = st->acc[u.it & 1];
+  const double S = acc[0], Hs = acc[1], Ds = acc[2];
+  const double n = (double)d.T;
+  SweepSlot nx = c;
+  double r_hat = 0.0, omega = 1.0;
+  if (u.res) {
+    r_hat = d.T > 0 ? S / n : 0.0;
+    if (c.has_prev && c.prev_r_hat > 1e-12) {
+      double rho_inst = r_hat / (c.prev_r_hat + 1e-12);
+      rho_inst = fmax(u.rho_min, fmin(u.rho_max, rho_inst));
+      nx.rho_hat = (1.0 - u.rho_beta) * c.rho_hat + u.rho_beta * rho_inst;
+    }
+    nx.prev_r_hat = r_hat;
+    nx.has_prev = 1;
+    const double rho2 = nx.rho_hat * nx.rho_hat;
+    if (u.it < u.warmup) omega = 1.0;
+    else if (u.it == u.warmup) omega = 2.0 / (2.0 - rho2);
+    else omega = 4.0 / (4.0 - rho2 * c.omega);
+    nx.omega = omega;
+  }
+  if (blockIdx.x == 0) {
+    if (u.res && !isfinite(S)) st->nonfinite = 1;
+    st->slot[(u.it + 1) & 1] = nx;
+    double* an = st->acc[(u.it + 1) & 1];
+    an[0] = an[1] = an[2] = 0.0;
+    if (u.last) st->rho_hat = nx.rho_hat;
+    if (u.rec >= 0) {
+      double* h = d.hist + 4 * (size_t)u.rec;
+      h[0] = r_hat;
+      h[1] = omega;
+      h[2] = u.mon && d.T > 0 ? Hs / n : 0.0;
+      h[3] = u.mon && d.T > 0 ? Ds / n : 0.0;
+    }
+  }
+  return (float)omega;
+}
+
 template <bool kCheb, bool kFirstIt, bool kResetDx>
-__global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma) {
+__global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma, UpdArgs u) {
   // kUpdateVerts vertices per thread, kBlock apart: all of a thread's loads
   // are in flight together, and the grid is a quarter of a one-per-vertex one
   const int base = blockIdx.x * (kBlock * kUpdateVerts) + threadIdx.x;
@@ -169,7 +235,10 @@ __global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma) 
       yp[k] = (kCheb && !kFirstIt) ? d.p[cur ^ 1][i] : pc[k];
     }
   }
-  const float om = kCheb ? (float)d.st->omega : 1.f;
+  __shared__ float s_om;
+  if (threadIdx.x == 0) s_om = (u.res || u.mon) ? sweep_step(d, u) : 1.f;
+  __syncthreads();
+  const float om = kCheb ? s_om : 1.f;
 #pragma unroll
   for (int k = 0; k < kUpdateVerts; ++k) {
     const int i = base + k * kBlock;
@@ -427,13 +496,12 @@ struct SweepArgs {
   double rho_min, rho_max, rho_beta;
 };
 
-// Block + grid FP64 reduction of the per-thread partial sums; the last block to
-// finish applies the rho_hat / omega recurrence (neohookean_solver.py:495-504,
-// :537-546) and writes history row `rec` = {r_hat, omega, hydro, dev}.
+// Block FP64 reduction of the per-thread partial sums, added into the
+// sweep's accumulators.  The rho_hat / omega recurrence runs in the update
+// that follows (sweep_step), so the sweep ends with its last reduction.
 template <bool kRes, bool kMon>
 __device__ __forceinline__ void finish_residual(const Dev& d, const SweepArgs& a, float sr, float sh, float sd) {
   __shared__ double red[3][32];
-  __shared__ bool last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   const double r0 = warp_sum((double)sr), r1 = warp_sum((double)sh), r2 = warp_sum((double)sd);
   if (lane == 0) {
@@ -442,56 +510,18 @@ __device__ __forceinline__ void finish_residual(const Dev& d, const SweepArgs& a
     red[2][warp] = r2;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double b0 = 0.0, b1 = 0.0, b2 = 0.0;
-    for (int k = 0; k < nw; ++k) {
-      b0 += red[0][k];
-      b1 += red[1][k];
-      b2 += red[2][k];
-    }
-    if (kRes) atomicAdd(&d.st->acc[0], b0);
-    if (kMon) {
-      atomicAdd(&d.st->acc[1], b1);
-      atomicAdd(&d.st->acc[2], b2);
-    }
-    __threadfence();
-    const unsigned int tk = atomicAdd(&d.st->ticket, 1u);
-    last = (tk == gridDim.x - 1);
+  if (threadIdx.x != 0) return;
+  double b0 = 0.0, b1 = 0.0, b2 = 0.0;
+  for (int k = 0; k < nw; ++k) {
+    b0 += red[0][k];
+    b1 += red[1][k];
+    b2 += red[2][k];
   }
-  __syncthreads();
-  if (!last || threadIdx.x != 0) return;
-  __threadfence();
-  volatile DevState* st = d.st;
-  const double S = st->acc[0], Hs = st->acc[1], Ds = st->acc[2];
-  st->acc[0] = 0.0;
-  st->acc[1] = 0.0;
-  st->acc[2] = 0.0;
-  st->ticket = 0u;
-  const double n = (double)d.T;
-  double r_hat = 0.0, omega = 1.0;
-  if (kRes) {
-    r_hat = d.T > 0 ? S / n : 0.0;
-    if (!isfinite(S)) st->nonfinite = 1;
-    if (st->has_prev && st->prev_r_hat > 1e-12) {
-      double rho_inst = r_hat / (st->prev_r_hat + 1e-12);
-      rho_inst = fmax(a.rho_min, fmin(a.rho_max, rho_inst));
-      st->rho_hat = (1.0 - a.rho_beta) * st->rho_hat + a.rho_beta * rho_inst;
-    }
-    st->prev_r_hat = r_hat;
-    st->has_prev = 1;
-    const double rho = st->rho_hat;
-    const double rho2 = rho * rho;
-    if (a.it < a.warmup) omega = 1.0;
-    else if (a.it == a.warmup) omega = 2.0 / (2.0 - rho2);
-    else omega = 4.0 / (4.0 - rho2 * st->omega);
-    st->omega = omega;
-  }
-  if (a.rec >= 0) {
-    double* h = d.hist + 4 * (size_t)a.rec;
-    h[0] = r_hat;
-    h[1] = omega;
-    h[2] = kMon && d.T > 0 ? Hs / n : 0.0;
-    h[3] = kMon && d.T > 0 ? Ds / n : 0.0;
+  double* acc = d.st->acc[a.it & 1];
+  if (kRes) atomicAdd(acc, b0);
+  if (kMon) {
+    atomicAdd(acc + 1, b1);
+    atomicAdd(acc + 2, b2);
   }
 }
 
@@ -1336,19 +1366,29 @@ void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
   if (cheb || mon) launch_residual(s, sweep_args(s, it, dt, rec), st);
   const int g = (s->d.V + kBlock * kUpdateVerts - 1) / (kBlock * kUpdateVerts);
   const bool reset = p.scatter != XPBD_SCATTER_GATHER;
+  UpdArgs u;
+  u.it = it;
+  u.rec = rec;
+  u.last = it == p.constraints_iter - 1;
+  u.warmup = p.cheb_warmup;
+  u.res = cheb;
+  u.mon = mon;
+  u.rho_min = p.rho_min;
+  u.rho_max = p.rho_max;
+  u.rho_beta = p.rho_beta;
   Prof prof(s, XPBD_K_UPDATE, st);
   if (cheb) {
     if (it == 0) {
-      if (reset) k_update<true, true, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma);
-      else k_update<true, true, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma);
+      if (reset) k_update<true, true, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
+      else k_update<true, true, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
     } else {
-      if (reset) k_update<true, false, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma);
-      else k_update<true, false, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma);
+      if (reset) k_update<true, false, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
+      else k_update<true, false, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
     }
     s->cur ^= 1;
   } else {
-    if (reset) k_update<false, false, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma);
-    else k_update<false, false, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma);
+    if (reset) k_update<false, false, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
+    else k_update<false, false, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
   }
 }
 
@@ -1631,7 +1671,6 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
   }
   DevState h{};
   h.rho_hat = 0.999;  // neohookean_solver.py:65
-  h.omega = 1.0;
   e = cudaMemcpy(d.st, &h, sizeof(h), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(d.hist, 0, sizeof(double) * 4 * (size_t)(max_records > 0 ? max_records : 1));
   if (e != cudaSuccess) return cleanup(fail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
