@@ -863,7 +863,7 @@ def run_gb300(args):
         traffic = 115.2e6
     # the same with warm caches inside a frame (ncu --cache-control none, mean of
     # two launches; profiles/l2_residency_c2_64cube.md): the sweeps run mostly from L2
-    traffic_in_frame = 29.05e6 if (scatter, tpt) == ("patch", 2) else None
+    traffic_in_frame = 25.36e6 if (scatter, tpt) == ("patch", 2) else None
     if pipe != 0 or args.patch_reduce != 0 or args.workload != "c2" or (scatter == "patch" and patch_tets != 256):
         traffic = traffic_in_frame = None
     iter_bytes = 136.0 * T + 128.0 * V
