@@ -663,8 +663,8 @@ __global__ void __launch_bounds__(256) k_residual_tile(Dev d, SweepArgs a) {
     mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[k & 1]), (k >> 1) & 1, kMaxPolls);
     if (issued_next) mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[(k & 1) ^ 1]), ((k + 1) >> 1) & 1, kMaxPolls);
   }
-  // every CTA joins the reduction so the ticket count stays whole; the sticky
-  // timeout flag marks the sweep invalid for the host
+  // every CTA adds its sums, even after a timeout; the sticky timeout flag
+  // marks the sweep invalid for the host
   finish_residual<kRes, kMon>(d, a, sr, sh, sd);
 }
 
