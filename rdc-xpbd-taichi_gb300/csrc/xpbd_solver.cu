@@ -38,8 +38,9 @@ constexpr int kUpdateVerts = 2;  // vertices per thread in k_update
 struct SweepSlot {
   double rho_hat;
   double prev_r_hat;
-  double omega;  // omega of the previous iteration of this substep
-  int has_prev;  // prev_r_hat is not None
+  double inv_prev;  // 1 / (prev_r_hat + 1e-12)
+  double omega;     // omega of the previous iteration of this substep
+  int has_prev;     // prev_r_hat is not None
 };
 
 // Iteration k's residual sweep adds into acc[k & 1]; iteration k's update
@@ -103,6 +104,7 @@ __global__ void __launch_bounds__(kBlock) k_begin(Dev d, float dt, float gx, flo
     SweepSlot& s0 = d.st->slot[0];
     s0.rho_hat = d.st->rho_hat;
     s0.prev_r_hat = 0.0;
+    s0.inv_prev = 0.0;
     s0.omega = 1.0;
     s0.has_prev = 0;
     d.st->acc[0][0] = d.st->acc[0][1] = d.st->acc[0][2] = 0.0;
@@ -169,6 +171,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(Dev d) {
 struct UpdArgs {
   int it, rec, last, warmup;
   int res, mon;  // the sweep summed residuals (Chebyshev) / monitoring means
+  double inv_n;  // 1 / tet count (0 for an empty mesh)
   double rho_min, rho_max, rho_beta;
 };
 
@@ -177,7 +180,9 @@ struct UpdArgs {
 // Every CTA of the update evaluates it (thread 0); CTA 0 also stores the
 // state entering the next iteration, clears the next sweep's accumulators,
 // writes history row `rec` = {r_hat, omega, hydro, dev}, and at the last
-// iteration the persistent rho_hat.
+// iteration the persistent rho_hat.  Every CTA runs one FP64 division (omega);
+// r_hat / n and r_hat / prev_r_hat are products with reciprocals that the
+// host (1 / n) and the previous iteration's CTA 0 (1 / prev) computed.
 __device__ __forceinline__ float sweep_step(const Dev& d, const UpdArgs& u) {
   DevState* st = d.st;
   const SweepSlot c = st->slot[u.it & 1];
@@ -187,9 +192,9 @@ __device__ __forceinline__ float sweep_step(const Dev& d, const UpdArgs& u) {
   SweepSlot nx = c;
   double r_hat = 0.0, omega = 1.0;
   if (u.res) {
-    r_hat = d.T > 0 ? S / n : 0.0;
+    r_hat = S * u.inv_n;
     if (c.has_prev && c.prev_r_hat > 1e-12) {
-      double rho_inst = r_hat / (c.prev_r_hat + 1e-12);
+      double rho_inst = r_hat * c.inv_prev;
       rho_inst = fmax(u.rho_min, fmin(u.rho_max, rho_inst));
       nx.rho_hat = (1.0 - u.rho_beta) * c.rho_hat + u.rho_beta * rho_inst;
     }
@@ -203,6 +208,7 @@ __device__ __forceinline__ float sweep_step(const Dev& d, const UpdArgs& u) {
   }
   if (blockIdx.x == 0) {
     if (u.res && !isfinite(S)) st->nonfinite = 1;
+    if (u.res) nx.inv_prev = 1.0 / (r_hat + 1e-12);
     st->slot[(u.it + 1) & 1] = nx;
     double* an = st->acc[(u.it + 1) & 1];
     an[0] = an[1] = an[2] = 0.0;
@@ -1373,6 +1379,7 @@ void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
   u.warmup = p.cheb_warmup;
   u.res = cheb;
   u.mon = mon;
+  u.inv_n = s->d.T > 0 ? 1.0 / (double)s->d.T : 0.0;
   u.rho_min = p.rho_min;
   u.rho_max = p.rho_max;
   u.rho_beta = p.rho_beta;
