@@ -60,6 +60,8 @@ def test_create_rejects_bad_arguments(native_lib):
     assert native_lib.xpbd_create(None, body, sdf, 1, 1, ctypes.byref(h)) == 1
     assert native_lib.xpbd_destroy(None) == 0
     assert native_lib.xpbd_substep(None, ctypes.c_float(0.01), 0, None) == 1
+    on = ctypes.c_int32(-1)
+    assert native_lib.xpbd_set_l2_hint(None, -1, ctypes.byref(on)) == 1 and on.value == -1
 
 
 def test_morton_order_is_a_permutation_with_locality(native_lib):
