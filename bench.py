@@ -138,6 +138,10 @@ def workload_c4(seed=0, n=16, sigma=2.0):
 
 
 def run_c4(args):
+    print(json.dumps(c4_block(args)), flush=True)
+
+
+def c4_block(args):
     """Differentiable single body: forward (checkpointed) vs adjoint cost, gradient checks."""
     import torch
     from oracle.xpbd_adjoint import DiffOracle, lame_inverse, lame_inverse_grad
@@ -224,7 +228,7 @@ def run_c4(args):
                                             "central finite differences), started from the GPU state",
                                "rel_l2_err": {"log_E": rel(g_le, g_le64), "v0": rel(g_v, vb), "nu": nu_err},
                                "max_directional_err_over_rms": {k: float(np.max(v)) for k, v in errs.items()}}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def workload_c5(seed=0, n_bodies=64, h=1.0 / 16, sigma=2.0):
@@ -375,135 +379,290 @@ def relative_residuals(hist, substeps, iters, floor=1e-5):
     return rel
 
 
-def run_c3(args):
-    """Batched form vs the plain one-body-per-launch form on the 256-body batch."""
-    import torch
+def c3_solvers(args, bodies, specs, kw, cap, target, floor):
+    """The batched form and the plain form (one single-body solver per body) of
+    the 256-body workload, both in stop mode with iteration cap `cap`."""
     from xpbd_gpu.batched import XPBDBatchedSolver
     from xpbd_gpu.mesh import TetMesh
     from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
-    torch.cuda.set_device(0)
-    bodies, specs, kw, desc = workload_c3()
-    units = sum(b.rest_pose.n_tets for b in bodies) * kw["substeps_num"] * kw["constraints_iter"]
+    kwc = dict(kw, constraints_iter=cap)
     btpt = "auto" if args.batch_tpt == "auto" else int(args.batch_tpt)
     batch = XPBDBatchedSolver(bodies, product_sdfs(specs), tets_per_thread=btpt, pair_tets=bool(args.pair_tets),
-                              **kw)
+                              target_rel_residual=target, residual_floor=floor, **kwc)
     plain = []
     for b in bodies:
         mesh = TetMesh(b.rest_pose.points @ b.rotation.T, b.rest_pose.tets)
         plain.append(XPBDNeoHookeanSolver(mesh, product_sdfs(specs), young_modulus=b.young_modulus,
                                           poisson_ratio=b.poisson_ratio, offset=b.offset, density=b.density,
                                           scatter="patch", tets_per_thread=args.tets_per_thread,
-                                          pair_tets=bool(args.pair_tets), **kw))
+                                          pair_tets=bool(args.pair_tets), target_rel_residual=target,
+                                          residual_floor=floor, **kwc))
+    return batch, plain
+
+
+def set_plain_mode(plain, target, floor, iters):
+    for s in plain:
+        s.target_rel_residual, s.residual_floor, s.constraints_iter = float(target), float(floor), int(iters)
+
+
+def load_plain_state(plain, batch, state):
+    """Positions, velocities and rho_hat of every body (the state a frame
+    starts from; multipliers and predicted positions restart each substep)."""
+    for k, s in enumerate(plain):
+        sl = batch.body_vert_slices[k]
+        s.mesh.verts.x.from_numpy(state["x"][sl])
+        s.mesh.verts.v.from_numpy(state["v"][sl])
+        s.rho_hat = float(state["rho"][k])
+
+
+def loop_launches(n):
+    """Kernel launches of one stop-mode substep whose longest body ran n
+    iterations: begin + end + 3 per iteration; past the first two iterations
+    the frame graph's WHILE node runs pairs of iterations."""
+    it = n if n <= 2 else 2 + 2 * ((n - 1) // 2)
+    return 2 + 3 * it
+
+
+def run_frames(step, n, flush, stream, after=None):
+    """n frames, each bracketed by CUDA events on `stream`, L2 flushed before
+    each; `after()` (outside the events) collects per-frame data."""
+    import torch
+    ms, data = [], []
+    for _ in range(n):
+        flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+        if after is not None:
+            data.append(after())
+    return ms, data
+
+
+def c3_headline(args, world=1, barrier=lambda: None):
+    """The metric's configuration: the 256-body batch, batched form against the
+    plain one-body-per-launch form at equal final relative residual.
+
+    Both forms start from the same settled state (the batch stepped
+    `c3_settle` frames at the reference's fixed 30 iterations, so every body
+    has landed) and run in stop mode: each body's substep iterates until
+    r_hat_k / r_hat_0 <= c3_target, or r_hat_k <= c3_floor (the FP32 round-off
+    level of a resting or free-falling body), with c3_cap iterations at the
+    most.  Both forms run the same per-body algorithm, so every body stops at
+    the same iteration with the same residual in both; the line reports the
+    counts' agreement.  `value` = executed tet-iterations per second of the
+    batched form; the plain form is timed on the first frames of the same
+    window.  The fixed 30-iteration comparison (the reference's own loop) is
+    reported beside it."""
+    import torch
+    rank, local_rank, _ = dist_info()
+    bodies, specs, kw, desc = workload_c3()
+    cap, target, floor = args.c3_cap, args.c3_target, args.c3_floor
+    K0 = kw["constraints_iter"]
+    S = kw["substeps_num"]
+    t_build = time.perf_counter()
+    batch, plain = c3_solvers(args, bodies, specs, kw, cap, target, floor)
+    t_build = time.perf_counter() - t_build
+    Tb = np.array([b.rest_pose.n_tets for b in bodies], dtype=np.float64)
+    Vb = np.array([b.rest_pose.n_verts for b in bodies], dtype=np.float64)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def timed(step):
-        for _ in range(max(args.warmup, 3)):
-            step()
-        torch.cuda.synchronize()
-        total = 0.0
-        with ClockSampler(torch.cuda.current_device()) as clk:
-            for _ in range(args.steps):
-                flush.fill_(1.0)
-                a = torch.cuda.Event(enable_timing=True)
-                b = torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                step()
-                b.record(stream)
-                torch.cuda.synchronize()
-                total += a.elapsed_time(b)
-        return total / args.steps, clk.summary()
-
-    def plain_step():
-        for s in plain:
-            s.solve()
-
-    ms_batch, clk_b = timed(batch.solve)
-    ms_plain, clk_p = timed(plain_step)
+    # settle at the fixed iteration count, then the shared starting state
+    batch.set_stop(0.0, 0.0, K0)
+    for _ in range(args.c3_settle):
+        batch.solve()
     batch.check_status()
-    S, K = kw["substeps_num"], kw["constraints_iter"]
-    rel_b = relative_residuals(batch.read_history(), S, K)
-    rel_p = np.stack([relative_residuals(s.read_history()[None], S, K)[0] for s in plain])
+    state = dict(x=batch.positions(), v=batch.velocities(), rho=batch.rho_hat, snap=batch.snapshot())
+
+    def batch_counts():
+        return batch.iterations_per_substep(S)
+
+    def plain_counts():
+        return np.stack([s.iterations_per_substep(S) for s in plain])
+
+    # batched, stop mode: warm-up from the shared state, then K timed frames from it
+    batch.set_stop(target, floor, cap)
+    for _ in range(max(args.warmup, 3)):
+        batch.solve()
+    batch.restore(state["snap"])
+    torch.cuda.synchronize()
+    barrier()
+    with ClockSampler(torch.cuda.current_device()) as clk_b:
+        ms_b, cnt_b = run_frames(batch.solve, args.steps, flush, stream, batch_counts)
+    barrier()
+    batch.check_status()
+    cnt_b = np.stack(cnt_b)  # frames, bodies, substeps
+    units_b = (cnt_b * Tb[None, :, None]).sum(axis=(1, 2))  # executed tet-iterations per frame
+    bytes_b = (cnt_b * (136.0 * Tb + 128.0 * Vb)[None, :, None]).sum(axis=(1, 2))
+    total_ms = max_over_ranks(float(sum(ms_b)), device="cuda")
+    value = float(units_b.sum()) * world / (total_ms * 1e-3)
+    launches = int(sum(loop_launches(int(n)) for n in cnt_b.max(axis=1).ravel()))
+    if rank != 0:
+        return None
+
+    # plain, stop mode, the first P frames of the same window
+    P = max(1, min(args.c3_plain_frames, args.steps))
+    load_plain_state(plain, batch, state)
+    for s in plain:
+        s.solve()  # warm-up: captures every body's frame graph
+    load_plain_state(plain, batch, state)
+    torch.cuda.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk_p:
+        ms_p, cnt_p = run_frames(lambda: [s.solve() for s in plain], P, flush, stream, plain_counts)
+    for s in plain:
+        s.check_status()
+    cnt_p = np.stack(cnt_p)
+    units_p = (cnt_p * Tb[None, :, None]).sum(axis=(1, 2))
+    hist_p = np.stack([s.read_history() for s in plain])
+
+    def rel_final(hist, counts):
+        """r_hat of each body-substep's last iteration over its first (last frame)."""
+        r = hist[:, :S * cap, 0].reshape(hist.shape[0], S, cap)
+        last = np.take_along_axis(r, (counts - 1)[:, :, None], axis=2)[:, :, 0]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return last / r[:, :, 0], last
+
+    # the batch's residuals of frame P (the plain form's last), untimed
+    batch.restore(state["snap"])
+    for _ in range(P):
+        batch.solve()
+    cnt_bP = batch_counts()
+    rel_b, last_b = rel_final(batch.read_history(), cnt_bP)
+    rel_p, last_p = rel_final(hist_p, cnt_p[-1])
+    met_b = (rel_b <= target) & (cnt_bP < cap)
+    floor_b = (last_b <= floor) & ~met_b
+
+    # the reference's fixed iteration count, both forms, the same P frames
+    batch.set_stop(0.0, 0.0, K0)
+    batch.restore(state["snap"])
+    batch.solve()
+    batch.restore(state["snap"])
+    torch.cuda.synchronize()
+    ms_bf, _ = run_frames(batch.solve, P, flush, stream)
+    set_plain_mode(plain, 0.0, 0.0, K0)
+    load_plain_state(plain, batch, state)
+    for s in plain:
+        s.solve()
+    load_plain_state(plain, batch, state)
+    torch.cuda.synchronize()
+    ms_pf, _ = run_frames(lambda: [s.solve() for s in plain], P, flush, stream)
+    units_f = float(Tb.sum()) * S * K0
+
+    # projection kernel of the batched form (fixed count: every patch works),
+    # CUDA events around each launch of one frame
+    batch.restore(state["snap"])
     batch.set_profiling(True)
     batch.read_profile(reset=True)
     flush.fill_(1.0)
     batch.solve()
     prof = batch.read_profile(reset=True)
     batch.set_profiling(False)
-    T = batch.n_tets
-    V = batch.n_verts
+    T, V = float(Tb.sum()), float(Vb.sum())
     proj_ms = prof["project"]["ms"] / max(1, prof["project"]["launches"])
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    peak = float(json.load(open(peaks_path))["hbm_gbs"]) if os.path.exists(peaks_path) else 6800.0
-    iter_bytes = 136.0 * T + 128.0 * V
-    conv = convergence_probe(batch, S, min(args.c3_conv_iters, batch._max_records))
+    peak, peak_src = measured_peak()
+    proj_bytes = 72.0 * T + 32.0 * V
+
+    # end to end through the public API: host state in, one frame, positions out
+    batch.set_stop(target, floor, cap)
+    x_host = torch.from_numpy(state["x"]).pin_memory()
+    v_host = torch.from_numpy(state["v"]).pin_memory()
+    e2e_ms, e2e_units = [], []
+    for k in range(args.e2e_steps + 1):
+        batch.restore(state["snap"])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        batch.set_positions(x_host)
+        batch.set_velocities(v_host)
+        batch.solve()
+        out = batch.positions()
+        t1 = time.perf_counter()
+        if k > 0:
+            e2e_ms.append((t1 - t0) * 1e3)
+            e2e_units.append(float((batch_counts() * Tb[:, None]).sum()))
+    assert out.shape == state["x"].shape
+    batch.check_status()
+
+    ms_step = total_ms / args.steps
+    n_sub = cnt_b.size
     line = {
-        "metric": METRIC, "value": units / (ms_batch * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": desc, "step": "one frame of all 256 bodies (%d tet-iterations)" % units,
-                   "form": "batched (one launch per phase over all bodies, CUDA graph per frame)",
-                   "l2": "flushed between steps"},
-        "frames_per_s": 1e3 / ms_batch,
-        "plain": {"form": "one body per launch sequence (256 single-body solvers, one CUDA graph each)",
-                  "value": units / (ms_plain * 1e-3), "ms_per_step": ms_plain, "clocks": clk_p},
-        "batched_over_plain": ms_plain / ms_batch,
-        "equal_residual": {"relative_residual_rK_over_r0_median": [float(np.nanmedian(rel_b)),
-                                                                    float(np.nanmedian(rel_p))],
-                           "max_abs_difference_batched_vs_plain": float(np.nanmax(np.abs(rel_b - rel_p))),
-                           "fraction_substeps_at_or_below_1e-3": [float(np.nanmean(rel_b <= 1e-3)),
-                                                                  float(np.nanmean(rel_p <= 1e-3))],
-                           "substeps_compared": int(np.sum(~np.isnan(rel_b))),
-                           "note": "substeps whose initial r_hat is below 1e-5 (bodies in free fall) excluded"},
-        "roofline": {"bound": "hbm", "kernel": "kb_project (batched tile projection)",
-                     "achieved": (72.0 * T + 32.0 * V) / (proj_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": (72.0 * T + 32.0 * V) / (proj_ms * 1e-3) / 1e9 / peak, "traffic": None,
-                     "ms_per_launch": proj_ms},
-        "iteration_roofline": {"achieved_GBps": iter_bytes * S * K / (ms_batch * 1e-3) / 1e9,
-                               "frac": iter_bytes * S * K / (ms_batch * 1e-3) / 1e9 / peak},
+        "config": {"workload": desc,
+                   "step": ("one frame of all 256 bodies; every body's substep iterates until r_hat_k/r_hat_0 <= "
+                            "%g or r_hat_k <= %g, at most %d iterations (value counts the tet-iterations run)"
+                            % (target, floor, cap)),
+                   "form": "batched (one launch per phase over all bodies; frame = one CUDA graph whose "
+                           "iterations loop in a WHILE conditional node while any body iterates)",
+                   "start": "the batch settled for %d frames at 30 iterations (all bodies landed); every timed "
+                            "frame of both forms starts from that state" % args.c3_settle,
+                   "l2": "flushed between steps (%d MiB write)" % (L2_FLUSH_BYTES >> 20),
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "construction_s": t_build},
+        "frames_per_s": 1e3 / ms_step * world,
+        "tet_iterations_per_frame": float(units_b.mean()),
+        "gpu_launches": launches,
+        "plain": {"form": "one body per launch sequence: 256 single-body solvers in stop mode, one CUDA graph "
+                          "each (WHILE node per substep)",
+                  "frames": P, "value": float(units_p.sum()) / (sum(ms_p) * 1e-3), "ms_per_step": float(np.mean(ms_p)),
+                  "clocks": clk_p.summary()},
+        "batched_over_plain": float(sum(ms_p) / sum(ms_b[:P])),
+        "equal_residual": {
+            "target_rel_residual": target, "residual_floor": floor, "iteration_cap": cap,
+            "iteration_counts_equal_fraction": float(np.mean(cnt_b[:P] == cnt_p)),
+            "iteration_counts_max_abs_diff": int(np.abs(cnt_b[:P] - cnt_p).max()),
+            "executed_tet_iterations_ratio_plain_over_batched": float(units_p.sum() / units_b[:P].sum()),
+            "rel_residual_final_median_frame_P": [float(np.nanmedian(rel_b)), float(np.nanmedian(rel_p))],
+            "rel_residual_final_max_abs_diff_frame_P": float(np.nanmax(np.abs(rel_b - rel_p))),
+            "body_substeps": int(n_sub),
+            "fraction_met_target": float(np.mean(met_b)),
+            "fraction_at_floor": float(np.mean(floor_b)),
+            "fraction_at_cap": float(np.mean(cnt_b == cap)),
+            "iterations_percentiles_10_50_90_max": [float(v) for v in np.percentile(cnt_b, [10, 50, 90, 100])],
+            "note": "met/floor fractions and the final r_hat_K/r_hat_0 over frame P's body-substeps (batched, then "
+                    "plain); cap fraction and percentiles over all timed frames of the batched form"},
+        "fixed_iterations": {"iterations": K0, "frames": P,
+                             "batched_ms_per_step": float(np.mean(ms_bf)), "plain_ms_per_step": float(np.mean(ms_pf)),
+                             "batched_value": units_f / (np.mean(ms_bf) * 1e-3),
+                             "plain_value": units_f / (np.mean(ms_pf) * 1e-3),
+                             "batched_over_plain": float(np.mean(ms_pf) / np.mean(ms_bf)),
+                             "note": "the reference's loop (neohookean_solver.py:474): every body runs 30 "
+                                     "iterations per substep"},
+        "roofline": {"bound": "hbm", "kernel": "kb_project (batched tile projection, all bodies active)",
+                     "achieved": proj_bytes / (proj_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": proj_bytes / (proj_ms * 1e-3) / 1e9 / peak, "peak_source": peak_src,
+                     "traffic": None, "bytes_per_launch": proj_bytes, "ms_per_launch": proj_ms,
+                     "timing": "CUDA events around each launch of one fixed-count frame (direct launches)"},
+        "iteration_roofline": {"bytes_per_frame": float(bytes_b.mean()),
+                               "achieved_GBps": float(bytes_b.sum()) / (sum(ms_b) * 1e-3) / 1e9,
+                               "frac": float(bytes_b.sum()) / (sum(ms_b) * 1e-3) / 1e9 / peak,
+                               "note": "136 B per tet + 128 B per vertex for every iteration a body ran"},
         "kernel_profile": {k: {"ms_per_launch": v["ms"] / max(1, v["launches"]), "launches": v["launches"]}
                            for k, v in prof.items() if v["launches"]},
-        "iterations_to_1e-3": conv,
-        "clocks": clk_b,
+        "e2e": {"value": float(np.sum(e2e_units)) / (np.sum(e2e_ms) * 1e-3), "unit": UNIT,
+                "h2d_bytes_per_step": 2 * int(state["x"].nbytes), "d2h_bytes_per_step": int(state["x"].nbytes),
+                "ms_per_step": float(np.mean(e2e_ms)),
+                "path": "XPBDBatchedSolver.set_positions / set_velocities from pinned host memory, solve(), "
+                        "positions() to host"},
+        "clocks": clk_b.summary(),
     }
     if batch.autotune_result is not None:
         line["config"]["autotune"] = {"tets_per_thread": batch.tets_per_thread,
                                       "cached": batch.autotune_result["cached"],
                                       "ms_per_substep": {"tpt%d" % r["tets_per_thread"]: r["ms"]
                                                          for r in batch.autotune_result["table"]}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
-def convergence_probe(batch, substeps, k_max, target=1e-3, floor=1e-5):
-    """Iterations every body needs per substep to reach r_hat_k / r_hat_0 <= target: one frame re-run
-    substep by substep with k_max iterations, from the batch's current state (restored afterwards).
-    Both forms run the identical per-body algorithm, so the counts hold for the plain form too."""
-    from xpbd_gpu import _native
-    snap = batch.snapshot()
-    K0 = batch.constraints_iter
-    batch.constraints_iter = k_max
-    _native.check(batch._lib.xpbd_batch_set_params(batch._handle, batch._params()), batch=True)
-    need = []
-    sub_dt = float(batch.dt) / substeps
-    for _ in range(substeps):
-        _native.check(batch._lib.xpbd_batch_substep(batch._handle, sub_dt, 0, batch._stream()), batch=True)
-        r = batch.read_history(k_max)[:, :, 0]
-        for b in range(r.shape[0]):
-            if r[b, 0] <= floor:
-                continue  # free fall: residual at FP32 round-off
-            hit = np.nonzero(r[b] / r[b, 0] <= target)[0]
-            need.append(int(hit[0]) + 1 if len(hit) else -1)
-    batch.constraints_iter = K0
-    _native.check(batch._lib.xpbd_batch_set_params(batch._handle, batch._params()), batch=True)
-    batch.restore(snap)
-    need = np.asarray(need)
-    ok = need[need > 0]
-    return {"target": target, "max_iterations": k_max, "substeps_counted": int(len(need)),
-            "fraction_reached": float(len(ok) / max(1, len(need))),
-            "iterations_median": float(np.median(ok)) if len(ok) else None,
-            "iterations_p90": float(np.percentile(ok, 90)) if len(ok) else None,
-            "fraction_within_configured_iterations": float(np.mean((need > 0) & (need <= K0))) if len(need) else None,
-            "note": "bodies' substeps with r_hat_0 <= %g (free fall) excluded" % floor}
+def measured_peak():
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        return float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
 
 
 def product_sdfs(specs):
@@ -548,9 +707,13 @@ def fp64_error(solver_factory, mesh, specs, kw, frames, warm_start=11, warm_fram
     bounding-box diagonal (a) over `frames` frames from the initial state and (b) over
     `warm_frames` frames in contact, all runs started from the GPU state after `warm_start`
     frames; in (b) also the deviation of the FP32 C restatement from the same state (what an
-    FP32 run of the reference algorithm itself departs from FP64) and the relative difference
-    of the per-iteration residual curves (only where the float64 r_hat is above 1e-4, well
-    above the FP32 floor of about 1e-5 of a body at rest on this mesh)."""
+    FP32 run of the reference algorithm itself departs from FP64), the GPU's deviation from
+    that FP32 run, the FP32 run's deviation from itself with its tets renumbered (the same
+    arithmetic summed in another order: what float-atomic order alone does to the
+    reference), and the relative difference of the per-iteration residual curves (only
+    where the float64 r_hat is above 1e-4, well above the FP32 floor of about 1e-5 of a
+    body at rest on this mesh)."""
+    from xpbd_gpu.mesh import TetMesh
     threads = os.cpu_count() or 1
     S, K = kw["substeps_num"], kw["constraints_iter"]
     diag = float(np.linalg.norm(mesh.points.max(0) - mesh.points.min(0)))
@@ -579,23 +742,39 @@ def fp64_error(solver_factory, mesh, specs, kw, frames, warm_start=11, warm_fram
         ref.v[:] = solver.mesh.verts.v.to_numpy()
         ref.rho_hat.value = solver.rho_hat
         f32 = cpu_oracle(mesh, specs, kw, S, threads, dtype=np.float32)
-        f32.x[:] = ref.x
-        f32.v[:] = ref.v
-        f32.rho_hat.value = ref.rho_hat.value
+        perm = np.random.default_rng(7).permutation(mesh.n_tets)
+        f32p = cpu_oracle(TetMesh(mesh.points, mesh.tets[perm]), specs, kw, S, threads, dtype=np.float32)
+        for o in (f32, f32p):
+            o.x[:] = ref.x
+            o.v[:] = ref.v
+            o.rho_hat.value = ref.rho_hat.value
         hist = np.zeros(S * K)
         mx, rms, t = run(solver, ref, warm_frames, hist)
+        h32, h32p = np.zeros(S * K), np.zeros(S * K)
         for _ in range(warm_frames):
-            f32.solve()
-        mx32 = float(np.abs(f32.x.astype(np.float64) - ref.x).max()) / diag
+            f32.solve(1, h32)
+            f32p.solve(1, h32p)
+        x_gpu = solver.mesh.verts.x.to_numpy().astype(np.float64)
+        x32, x32p = f32.x.astype(np.float64), f32p.x.astype(np.float64)
         r_gpu = solver.read_history()[:S * K, 0]
         live = hist > 1e-4
-        rel = np.abs(r_gpu - hist)[live] / hist[live]
+
+        def curve(a, b):
+            return float((np.abs(a - b)[live] / b[live]).max()) if live.any() else None
+
         out["in_contact"] = {"start_frame": max(warm_start, frames), "frames": warm_frames,
                              "max_dev_over_bbox_diag": mx, "rms_dev_over_bbox_diag": rms,
-                             "fp32_reference_max_dev_over_bbox_diag": mx32,
-                             "residual_curve_max_rel_diff": float(rel.max()) if live.any() else None,
+                             "fp32_reference_max_dev_over_bbox_diag": float(np.abs(x32 - ref.x).max()) / diag,
+                             "gpu_vs_fp32_reference_max_dev_over_bbox_diag": float(np.abs(x_gpu - x32).max()) / diag,
+                             "fp32_reference_reordered_vs_itself_max_dev_over_bbox_diag":
+                                 float(np.abs(x32p - x32).max()) / diag,
+                             "residual_curve_max_rel_diff": curve(r_gpu, hist),
+                             "residual_curve_max_rel_diff_fp32_reference_vs_fp64": curve(h32, hist),
+                             "residual_curve_max_rel_diff_gpu_vs_fp32_reference": curve(r_gpu, h32),
+                             "residual_curve_max_rel_diff_fp32_reordered_vs_fp32": curve(h32p, h32),
                              "residual_iterations_compared": int(live.sum()), "fp64_s_per_frame": t,
-                             "note": "both runs start from the GPU state (positions, velocities, rho_hat)"}
+                             "note": "every run starts from the GPU state (positions, velocities, rho_hat); the "
+                                     "reordered FP32 run numbers the tets in a random order (seed 7)"}
     return out
 
 
@@ -714,13 +893,69 @@ def replica_throughput(units_per_step, steps, world, max_total_ms):
     return units_per_step * steps * world / (max_total_ms * 1e-3)
 
 
+def c3_oracles(bodies, specs, kw, dtype=np.float32):
+    """The C restatement of every body of the 256-body workload, each stepping
+    one substep (the workload's constraints_iter iterations) per call; a body
+    uses one host thread per 8192 of its tets (all threads for the largest)."""
+    from xpbd_gpu.mesh import TetMesh
+    threads = os.cpu_count() or 1
+    out = []
+    for b in bodies:
+        pts = b.rest_pose.points @ b.rotation.T + np.asarray(b.offset, dtype=np.float64)
+        mesh = TetMesh(pts, b.rest_pose.tets)
+        kwb = dict(kw, young_modulus=b.young_modulus, poisson_ratio=b.poisson_ratio, density=b.density)
+        out.append(cpu_oracle(mesh, specs, kwb, 1, max(1, min(threads, mesh.n_tets // 8192)), dtype))
+    return out, threads
+
+
+def cpu_baseline_c3(bodies, specs, kw):
+    """One substep of all 256 bodies (30 iterations each, the reference's loop)
+    with the C restatement on the host cores: tet-iterations/s."""
+    oracles, threads = c3_oracles(bodies, specs, kw)
+    t0 = time.perf_counter()
+    for c in oracles:
+        c.solve()
+    el = time.perf_counter() - t0
+    units = sum(len(c.tets) for c in oracles) * kw["constraints_iter"]
+    return dict(value=units / el, unit=UNIT, cores=threads, kind="port",
+                sample="C restatement (FP32, up to %d threads per body): one substep of all 256 bodies x %d "
+                       "iterations from the initial state (%d tet-iterations, %.1f s)"
+                       % (threads, kw["constraints_iter"], units, el))
+
+
 def run_reference(args):
     """The reference arm: the reference's algorithm on the host cores.  The reference's
     own Taichi CPU backend cannot be installed on this machine (no Taichi wheel for
     Python 3.12, no network), so this times the C restatement on all host threads;
-    one step = one substep of the workload (constraints_iter Jacobi iterations)."""
+    one step = one substep of the workload (constraints_iter Jacobi iterations; for
+    c3 one substep of all 256 bodies, each at the reference's 30 iterations)."""
     rank, _, world = dist_info()
     if rank != 0:
+        return
+    if args.workload == "c3":
+        bodies, specs, kw, desc = workload_c3()
+        oracles, threads = c3_oracles(bodies, specs, kw)
+        step = lambda: [c.solve() for c in oracles]
+        for _ in range(args.warmup):
+            step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        el = time.perf_counter() - t0
+        units = sum(len(c.tets) for c in oracles) * kw["constraints_iter"] * args.steps
+        v = units / el
+        sample = ("C restatement of the reference substep (FP32, up to %d threads per body): %d substeps of all 256 "
+                  "bodies x %d iterations, %.1f s" % (threads, args.steps, kw["constraints_iter"], el))
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic",
+                "config": {"workload": desc, "step": "one substep of all 256 bodies at the reference's fixed "
+                                                     "30 iterations (%d tet-iterations)" % (units // args.steps)},
+                "frames_per_s": v / (units / args.steps * kw["substeps_num"]),
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
         return
     mesh, specs, kw, desc = workload(args.workload)
     threads = os.cpu_count() or 1
@@ -747,17 +982,15 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def run_gb300(args):
+def c2_line(args, workload_name, world=1, barrier=lambda: None, cpu_substeps=None):
+    """The single-body plain GPU form on `workload_name` (c2: the 64^3 cube):
+    frames replayed from the frame graph, per-kernel times, e2e, CPU
+    baseline, error against the FP64 run.  Returns the JSON dict (None on
+    ranks other than 0)."""
     import torch
-    rank, local_rank, world = dist_info()
-    torch.cuda.set_device(local_rank)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    from xpbd_gpu import _native
     from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver, frame_chunks
-
-    mesh, specs, kw, desc = workload(args.workload)
+    rank = dist_info()[0]
+    mesh, specs, kw, desc = workload(workload_name)
     t_build = time.perf_counter()
     solver = XPBDNeoHookeanSolver(mesh, product_sdfs(specs), scatter=args.scatter, sweep_order=args.sweep_order,
                                   patch_pipeline=args.patch_pipeline, patch_reduce=args.patch_reduce,
@@ -772,11 +1005,6 @@ def run_gb300(args):
     launches_per_frame = n_chunks * kw["substeps_num"] * per_substep
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
 
     for _ in range(max(args.warmup, 3)):
         solver.solve()
@@ -830,13 +1058,8 @@ def run_gb300(args):
     assert out.shape == (V, 3)
 
     if rank != 0:
-        return
-    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(peaks_path):
-        peak = float(json.load(open(peaks_path))["hbm_gbs"])
-        peak_src = "measured"
-    else:
-        peak, peak_src = 6800.0, "fallback"
+        return None
+    peak, peak_src = measured_peak()
     K = kw["constraints_iter"]
     n_proj = prof["project"]["launches"]
     # algorithmic bytes of one projection launch (per-unit figures of the
@@ -855,17 +1078,6 @@ def run_gb300(args):
     else:
         kernel_name = {"atomic": "k_project (one thread per tet, red.global.add.v4 per corner)",
                        "gather": "k_project (per-corner buffer + deterministic vertex gather)"}[scatter]
-    # dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel on this
-    # workload, from the ncu captures summarised in profiles/k_project_*_c2_64cube.md
-    # (k_project_patchN for 2 tets per thread, k_project_patch1 for 1)
-    traffic = {("patch", 2): 89.10e6, ("patch", 1): 89.4e6}.get((scatter, tpt))
-    if scatter == "atomic":
-        traffic = 115.2e6
-    # the same with warm caches inside a frame (ncu --cache-control none, mean of
-    # two launches; profiles/l2_residency_c2_64cube.md): the sweeps run mostly from L2
-    traffic_in_frame = 25.36e6 if (scatter, tpt) == ("patch", 2) else None
-    if pipe != 0 or args.patch_reduce != 0 or args.workload != "c2" or (scatter == "patch" and patch_tets != 256):
-        traffic = traffic_in_frame = None
     iter_bytes = 136.0 * T + 128.0 * V
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -881,7 +1093,7 @@ def run_gb300(args):
         "gpu_launches": launches_per_frame * args.steps,
         "roofline": {"bound": "hbm", "kernel": kernel_name,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "traffic": traffic, "traffic_in_frame": traffic_in_frame,
+                     "peak_source": peak_src, "traffic": None,
                      "bytes_per_launch": proj_bytes, "ms_per_launch": proj_ms,
                      "timing": "CUDA events recorded by event nodes inside the frame graph (the timed "
                                "region's graph plus those nodes), %d frames after the timed region"
@@ -903,7 +1115,7 @@ def run_gb300(args):
             "ms_per_substep": {"%s/P%s/tpt%s/pipe%s" % (c["scatter"], c["patch_tets"], c["tets_per_thread"],
                                                          c["patch_pipeline"]): c["ms"] for c in r["table"]}}
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(mesh, specs, kw, substeps=args.cpu_substeps)
+        line["cpu_baseline"] = cpu_baseline(mesh, specs, kw, substeps=cpu_substeps or args.cpu_substeps)
     if args.fp64_frames > 0:
         del solver
         line["fp64_error"] = fp64_error(
@@ -911,6 +1123,38 @@ def run_gb300(args):
                                          patch_pipeline=pipe, patch_reduce=args.patch_reduce, tets_per_thread=tpt,
                                          patch_tets=patch_tets or 256, pair_tets=bool(args.pair_tets), **kw),
             mesh, specs, kw, args.fp64_frames, warm_start=args.fp64_warm_start, warm_frames=args.fp64_warm_frames)
+    return line
+
+
+def run_gb300(args):
+    """The GB300 arm.  Default (c3): the metric's 256-body batch at equal
+    residual, with the 64^3 single body (c2) and the differentiable cube's
+    adjoint cost (c4) as extra keys of the same line."""
+    import torch
+    rank, local_rank, world = dist_info()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    if args.workload == "c3":
+        line = c3_headline(args, world, barrier)
+        if line is None:
+            return
+        bodies, specs, kw, _ = workload_c3()
+        line["cpu_baseline"] = cpu_baseline_c3(bodies, specs, kw)
+        if not args.no_extra:
+            line["c2"] = c2_line(args, "c2", cpu_substeps=5)
+            line["c4"] = c4_block(args)
+    else:
+        line = c2_line(args, args.workload, world, barrier)
+        if line is None:
+            return
     print(json.dumps(line), flush=True)
 
 
@@ -965,7 +1209,13 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c3", choices=["c2", "c1", "c3", "c4", "c5"])
+    ap.add_argument("--c3-cap", type=int, default=200, help="iteration cap of the equal-residual runs")
+    ap.add_argument("--c3-target", type=float, default=1e-3, help="r_hat_k / r_hat_0 target")
+    ap.add_argument("--c3-floor", type=float, default=1e-5, help="r_hat below which a substep has converged")
+    ap.add_argument("--c3-settle", type=int, default=90, help="frames stepped before the timed window")
+    ap.add_argument("--c3-plain-frames", type=int, default=4, help="timed frames of the plain form")
+    ap.add_argument("--no-extra", action="store_true", help="c3 line without the c2 / c4 keys")
     ap.add_argument("--c5-frames", type=int, default=30)
     ap.add_argument("--c5-adam-steps", type=int, default=200)
     ap.add_argument("--c5-lr", type=float, default=0.05)
@@ -982,7 +1232,6 @@ def main():
     ap.add_argument("--batch-tpt", default="auto", choices=["auto", "1", "2"])
     ap.add_argument("--pair-tets", type=int, default=1, choices=[0, 1],
                     help="order face-adjacent tets in corner-aligned pairs (xpbd_pair_tets)")
-    ap.add_argument("--c3-conv-iters", type=int, default=150)
     ap.add_argument("--profile-steps", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-substeps", type=int, default=20)
@@ -995,8 +1244,6 @@ def main():
     args = ap.parse_args()
     if args.mode == "profile":
         run_profile(args)
-    elif args.workload == "c3" and args.impl != "reference":
-        run_c3(args)
     elif args.workload == "c4" and args.impl != "reference":
         run_c4(args)
     elif args.workload == "c5" and args.impl != "reference":

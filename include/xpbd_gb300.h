@@ -5,7 +5,7 @@
  * Python class XPBDNeoHookeanSolver (xpbd_gpu/neohookean_solver.py:16-587)
  * over Taichi kernels; it has no FFI of its own.  Each entry point below
  * replaces one method of that class (cited beside it), so a Python host
- * binds them with ctypes (see INTEGRATION.md) and keeps the class interface.
+ * binds them with ctypes and keeps the class interface.
  *
  * Conventions
  *  - Every function returns an int status (XPBD_OK == 0).
@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define XPBD_ABI_VERSION 1
+#define XPBD_ABI_VERSION 2
 
 enum xpbd_status {
   XPBD_OK = 0,
@@ -92,6 +92,18 @@ typedef struct xpbd_params {
                                    2 or 4 = that many consecutive tets per thread, corners
                                    shared along the chain summed in registers */
   double rho_min, rho_max, rho_beta; /* neohookean_solver.py:66-68 */
+  /* Stop mode (off when both are 0, the reference's fixed iteration count,
+   * neohookean_solver.py:474): a substep ends after the first iteration k
+   * whose residual (compute_xpbd_residual, :298-329) satisfies
+   *   r_hat_k <= target_rel_residual * r_hat_0  or  r_hat_k <= residual_floor,
+   * and after constraints_iter iterations at the most.  The positions are
+   * those of a fixed-count run of k + 1 iterations.  Under xpbd_solve's
+   * graph the remaining iterations launch nothing (a conditional WHILE node
+   * of the frame graph loops over pairs of iterations); direct launches run
+   * the cap and the kernels of stopped iterations return at once.  The
+   * adjoint entry points reject it. */
+  double target_rel_residual;
+  double residual_floor;
 } xpbd_params;
 
 /* Caller-owned device buffers of one body (already in solver vertex/tet order). */
@@ -194,6 +206,14 @@ int xpbd_solve(void* handle, double frame_dt, double dt, int32_t substeps, void*
  * to host memory; synchronises `stream`. */
 int xpbd_read_history(void* handle, double* host_out, int32_t n, void* stream);
 
+/* Jacobi iterations run by substeps [0, n) of the last frame (or, for
+ * xpbd_substep / xpbd_solve_step, by the substep whose record_base is
+ * s * constraints_iter); n <= 256.  `total` (may be NULL) receives the
+ * iterations run since xpbd_create by the substeps that summed a residual
+ * (Chebyshev, monitoring or stop mode).  Synchronises `stream`.  No
+ * counterpart in the reference, whose iteration count is fixed. */
+int xpbd_read_iterations(void* handle, int32_t* host_out, int32_t n, int64_t* total, void* stream);
+
 /* Spectral-radius estimate rho_hat (neohookean_solver.py:65, persists across
  * substeps); get synchronises `stream`. */
 int xpbd_get_rho_hat(void* handle, double* out, void* stream);
@@ -289,15 +309,21 @@ int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xp
  *   out[0] = r_hat  (compute_xpbd_residual, neohookean_solver.py:298-329),
  *   out[1] = mean |det F - 1|, out[2] = mean |tr F^T F - 3|
  * into the caller's device array `out` (3 doubles), using only body->tets,
- * dm_a, dm_b, dm_c, v0, lam and dx (atomic-variant layout) and pred_x
- * ([V][4]); tet ids are not re-checked, so pass a body that xpbd_create has
- * validated.  It calls no cudaMalloc, cudaFree or allocating library routine:
+ * dm_a, dm_b, dm_c, v0, lam, dx and, when set, tet_inv_mu / tet_inv_lambda
+ * (then the compliances are per tet and lame_mu / lame_lambda are unused),
+ * and pred_x ([V][4]).  Every scatter variant's body works: tets, inv_Dm, V0
+ * and lambda are per tet in the same solver order in all of them (the tile
+ * variant's padding records past n_tets are not read).  Tet ids are not
+ * re-checked, so pass a body that xpbd_create has validated.
+ * It calls no cudaMalloc, cudaFree or allocating library routine:
  * its scratch is a static device array of (3 * 8192 + 1) doubles (192 KiB)
  * that every GPU loading the library keeps until the process exits, so one
  * call handles at most 8192 * 256 = 2,097,152 tets; larger meshes get
  * XPBD_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress) with that device current; make that
- * first call before any stream capture.  All calls share the array and it
+ * first call before any stream capture.  The address is that of the runtime's
+ * primary context: it is not looked up again after cudaDeviceReset, and
+ * contexts created through the driver API are not supported.  All calls share the array and it
  * keeps the last call's contents (the call clears the ticket it needs), so
  * calls that overlap on the GPU -- on different streams, or from different
  * threads -- race and must be serialised by the caller. */
@@ -401,11 +427,19 @@ int xpbd_batch_destroy(void* handle);
 /* One substep of every body (neohookean_solver.py:577-579). */
 int xpbd_batch_substep(void* handle, float dt, int32_t record_base, void* stream);
 
-/* One frame of every body (neohookean_solver.py:562-587), cached CUDA graph. */
+/* One frame of every body (neohookean_solver.py:562-587), cached CUDA graph.
+ * In stop mode (xpbd_params) every body stops at its own residual target; the
+ * frame graph loops while any body still iterates, and the kernels skip the
+ * patches and vertex blocks of the bodies that have stopped. */
 int xpbd_batch_solve(void* handle, double frame_dt, double dt, int32_t substeps, void* stream);
 
 /* History rows [0, n) of every body, host layout [n_bodies][n][4]; synchronises. */
 int xpbd_batch_read_history(void* handle, double* host_out, int32_t n, void* stream);
+
+/* Jacobi iterations every body ran in substeps [0, n) of the last frame,
+ * host layout [n_bodies][n], n <= 256 (stop mode: xpbd_params); synchronises.
+ * No counterpart in the reference, whose iteration count is fixed. */
+int xpbd_batch_read_iterations(void* handle, int32_t* host_out, int32_t n, void* stream);
 
 /* rho_hat of every body (host [n_bodies]); synchronises. */
 int xpbd_batch_get_rho_hat(void* handle, double* host_out, void* stream);

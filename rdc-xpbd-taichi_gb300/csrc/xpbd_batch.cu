@@ -31,12 +31,26 @@ struct BodyState {
   double rho_hat;
   double prev_r_hat;
   double omega;
+  double r0;    // r_hat of the substep's first iteration (stop mode)
+  int stop_at;  // iterations the body runs this substep (stop mode lowers it)
+  int pad;
 };
 
 struct Flags {
   int nonfinite;
   int bad_mesh;
 };
+
+// Iteration control: it[k & 1] = k while iteration k runs (written by the
+// previous iteration's update); n_active = bodies still iterating (stop mode).
+struct Ctl {
+  int it[2];
+  int n_active;
+  int pad;
+};
+
+// Substeps of one frame whose per-body iteration counts are kept.
+constexpr int kMaxCountedSubsteps = 256;
 
 struct BDev {
   int V, T, n_patches, n_bodies, n_sdf, n_pverts;
@@ -67,7 +81,19 @@ struct BDev {
   Flags* flags;
   double* hist;  // [n_bodies][max_records][4]
   int max_records;
+  Ctl* ctl;
+  int* iters;    // [n_bodies][kMaxCountedSubsteps] iterations run per substep
+  // stop mode: parity of the launched iteration (its index & 1), whose index
+  // the kernels read from ctl->it[stop_par]; -1 = fixed iteration count
+  int stop_par;
 };
+
+// Stop mode: body b does not run the launched iteration.
+__device__ __forceinline__ bool body_stopped(const BDev& d, int b, int k) { return k >= d.bs[b].stop_at; }
+
+__device__ __forceinline__ int launched_iteration(const BDev& d) {
+  return d.stop_par >= 0 ? *reinterpret_cast<const volatile int*>(&d.ctl->it[d.stop_par]) : 0;
+}
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
@@ -84,13 +110,20 @@ __device__ __forceinline__ float3 post_position(const float4 p, const float4 D) 
 
 // Begin of a substep for every body: per-body reset of prev_r_hat / omega
 // (neohookean_solver.py:461, :466) and predict + sequential SDF projection.
-__global__ void __launch_bounds__(256) kb_begin(BDev d, float dt, float gx, float gy, float gz) {
+__global__ void __launch_bounds__(256) kb_begin(BDev d, float dt, float gx, float gy, float gz, int K) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (blockIdx.x == 0)
+  if (blockIdx.x == 0) {
     for (int b = threadIdx.x; b < d.n_bodies; b += blockDim.x) {
       d.bs[b].has_prev = 0;
       d.bs[b].omega = 1.0;
+      d.bs[b].r0 = 0.0;
+      d.bs[b].stop_at = K;
     }
+    if (threadIdx.x == 0) {
+      d.ctl->it[0] = 0;
+      d.ctl->n_active = d.n_bodies;
+    }
+  }
   if (i >= d.V) return;
   const float4 xi = d.x[i];
   float4 vi = d.v[i];
@@ -106,9 +139,16 @@ __global__ void __launch_bounds__(256) kb_begin(BDev d, float dt, float gx, floa
   d.p[0][i] = make_float4(p.x, p.y, p.z, w);
 }
 
-__global__ void __launch_bounds__(256) kb_end(BDev d, int cur, float dt, float damping) {
+// advance (xpbd_base.py:148-160).  dyn (stop mode): body b ran stop_at
+// iterations, so its positions are in p[stop_at & 1] with Chebyshev (p[0]
+// without); `sub` >= 0 records every body's count for that substep.
+__global__ void __launch_bounds__(256) kb_end(BDev d, int cur, float dt, float damping, int dyn, int cheb, int sub) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0 && sub >= 0 && sub < kMaxCountedSubsteps)
+    for (int b = threadIdx.x; b < d.n_bodies; b += blockDim.x)
+      d.iters[(size_t)b * kMaxCountedSubsteps + sub] = d.bs[b].stop_at;
   if (i >= d.V) return;
+  if (dyn) cur = cheb ? (d.bs[__ldg(d.vblock_body + (i >> 8))].stop_at & 1) : 0;
   const float4 xi = d.x[i];
   if (xi.w <= 0.f) {
     d.p[cur][i] = xi;
@@ -132,6 +172,7 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_projec
   __shared__ int sg[256];
   const int p = blockIdx.x;
   const int b = __ldg(d.patch_body + p);
+  if (d.stop_par >= 0 && body_stopped(d, b, launched_iteration(d))) return;
   const int vb = __ldg(d.voff + p);
   const int nv = __ldg(d.voff + p + 1) - vb;
   const int nt = __ldg(d.patch_ntets + p);
@@ -190,8 +231,13 @@ __device__ __forceinline__ double warp_sum(double v) {
 struct BSweep {
   int cur;
   float inv_dt2;
-  int it, warmup, rec;
+  int par;       // the iteration's index & 1 (its index is ctl->it[par])
+  int warmup;
+  int rec_base;  // history row of the substep's iteration 0 (-1: none)
+  int res;       // Chebyshev recurrence
+  int stop;      // stop mode
   double rho_min, rho_max, rho_beta;
+  double target, floor;
 };
 
 // Add a CTA's partial sums over `npatch` patches of body b to the body's FP64
@@ -199,8 +245,8 @@ struct BSweep {
 // rho_hat / omega recurrence (neohookean_solver.py:495-504, :537-546) and
 // writes the body's history row.  All threads of the CTA call it.
 template <bool kRes, bool kMon, int kWarps>
-__device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int b, int npatch, float sr, float sh,
-                                           float sd, double (*red)[kWarps]) {
+__device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int it, int b, int npatch, float sr,
+                                           float sh, float sd, double (*red)[kWarps]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const double r0 = warp_sum((double)sr), r1 = warp_sum((double)sh), r2 = warp_sum((double)sd);
   __syncthreads();  // red[] of the previous flush has been consumed
@@ -239,6 +285,8 @@ __device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int b
   if (kRes) {
     r_hat = ntb > 0 ? S / n : 0.0;
     if (!isfinite(S)) d.flags->nonfinite = 1;
+  }
+  if (kRes && a.res) {
     if (st->has_prev && st->prev_r_hat > 1e-12) {
       double rho_inst = r_hat / (st->prev_r_hat + 1e-12);
       rho_inst = fmax(a.rho_min, fmin(a.rho_max, rho_inst));
@@ -247,13 +295,22 @@ __device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int b
     st->prev_r_hat = r_hat;
     st->has_prev = 1;
     const double rho2 = st->rho_hat * st->rho_hat;
-    if (a.it < a.warmup) omega = 1.0;
-    else if (a.it == a.warmup) omega = 2.0 / (2.0 - rho2);
+    if (it < a.warmup) omega = 1.0;
+    else if (it == a.warmup) omega = 2.0 / (2.0 - rho2);
     else omega = 4.0 / (4.0 - rho2 * st->omega);
     st->omega = omega;
   }
-  if (a.rec >= 0) {
-    double* h = d.hist + 4 * ((size_t)b * d.max_records + a.rec);
+  // stop mode: the body's last iteration is this one once r_hat meets the
+  // target (or the floor); it still finishes (update) in this iteration
+  if (kRes && a.stop) {
+    if (it == 0) st->r0 = r_hat;
+    if ((r_hat <= a.target * st->r0 || r_hat <= a.floor) && it + 1 < st->stop_at) {
+      st->stop_at = it + 1;
+      atomicSub(&d.ctl->n_active, 1);
+    }
+  }
+  if (a.rec_base >= 0) {
+    double* h = d.hist + 4 * ((size_t)b * d.max_records + a.rec_base + it);
     h[0] = r_hat;
     h[1] = omega;
     h[2] = kMon && ntb > 0 ? Hs / n : 0.0;
@@ -273,10 +330,12 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
   const int c1 = c0 + chunk < d.n_patches ? c0 + chunk : d.n_patches;
   const float4* P = d.p[a.cur];
   const int l0 = kTPT * threadIdx.x;
+  const int it = *reinterpret_cast<const volatile int*>(&d.ctl->it[a.par]);
   float sr = 0.f, sh = 0.f, sd = 0.f;
   int run = 0;
   for (int p = c0; p < c1; ++p) {
     const int b = __ldg(d.patch_body + p);
+    if (a.stop && body_stopped(d, b, it)) continue;  // the whole body is skipped: no flush
     const int vb = __ldg(d.voff + p);
     const int nv = __ldg(d.voff + p + 1) - vb;
     const int nt = __ldg(d.patch_ntets + p);
@@ -337,7 +396,7 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
     }
     ++run;
     if (p + 1 == c1 || __ldg(d.patch_body + p + 1) != b) {
-      flush_body<kRes, kMon, kThreads / 32>(d, a, b, run, sr, sh, sd, red);
+      flush_body<kRes, kMon, kThreads / 32>(d, a, it, b, run, sr, sh, sd, red);
       sr = sh = sd = 0.f;
       run = 0;
     }
@@ -348,18 +407,39 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
 // Each thread takes kBUpdateBlocks vertices, one in each of consecutive
 // 256-vertex blocks, so that all of its loads are in flight together.
 constexpr int kBUpdateBlocks = 2;
+
+// Iteration control of one update launch: CTA 0 advances the iteration
+// index and (stop mode, under a frame graph) sets the loop condition.
+struct BUpd {
+  int par;       // the iteration's index & 1
+  int K;         // iterations per substep (stop mode: the cap)
+  int stop;
+  int use_cond;
+  cudaGraphConditionalHandle cond;
+};
+
 template <bool kCheb, bool kFirstIt>
-__global__ void __launch_bounds__(256) kb_update(BDev d, int cur, float gamma) {
+__global__ void __launch_bounds__(256) kb_update(BDev d, int cur, float gamma, BUpd u) {
   const int vb0 = blockIdx.x * kBUpdateBlocks;
+  const int it = (u.stop || blockIdx.x == 0) ? *reinterpret_cast<const volatile int*>(&d.ctl->it[u.par]) : 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    d.ctl->it[u.par ^ 1] = it + 1;
+    if (u.use_cond) {
+      const bool more = it + 1 < u.K && *reinterpret_cast<const volatile int*>(&d.ctl->n_active) > 0;
+      cudaGraphSetConditional(u.cond, more ? 1u : 0u);
+    }
+  }
   // every load is issued before the first store: as far as the compiler
   // knows the buffers may alias, so a load after a store would wait for it
   float4 pc[kBUpdateBlocks], D[kBUpdateBlocks], yp[kBUpdateBlocks];
   float om[kBUpdateBlocks];
+  bool run[kBUpdateBlocks];
 #pragma unroll
   for (int k = 0; k < kBUpdateBlocks; ++k) {
     const int i = (vb0 + k) * 256 + threadIdx.x;
     om[k] = 1.f;
-    if (i < d.V) {
+    run[k] = i < d.V && !(u.stop && body_stopped(d, __ldg(d.vblock_body + vb0 + k), it));
+    if (run[k]) {
       pc[k] = d.p[cur][i];
       D[k] = d.dx[i];
       yp[k] = pc[k];
@@ -372,7 +452,7 @@ __global__ void __launch_bounds__(256) kb_update(BDev d, int cur, float gamma) {
 #pragma unroll
   for (int k = 0; k < kBUpdateBlocks; ++k) {
     const int i = (vb0 + k) * 256 + threadIdx.x;
-    if (i >= d.V) break;
+    if (!run[k]) continue;
     d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 xp = post_position(pc[k], D[k]);
     if (kCheb) {
@@ -567,7 +647,9 @@ struct Batch {
   BDev d{};
   int cur = 0;
   int n_out = 0;
+  bool capturing = false;
   cudaStream_t cap = nullptr;
+  cudaStream_t cap_body = nullptr;  // captures the body of a stop-mode loop node
   cudaGraphExec_t exec = nullptr;
   double key_frame_dt = -1, key_dt = -1;
   int key_sub = -1;
@@ -656,53 +738,113 @@ void residual_b(Batch* s, const BSweep& a, cudaStream_t st) {
   else residual_bm<kRes, kMon, false>(s, a, st);
 }
 
-void iteration_b(Batch* s, int it, float dt, int rec, cudaStream_t st) {
+inline bool stop_mode_b(const xpbd_params& p) { return p.target_rel_residual > 0.0 || p.residual_floor > 0.0; }
+
+// One Jacobi iteration of every body.  `first`: iteration 0 (lambda reset);
+// `par`: the iteration's index & 1 (the index itself is on the device);
+// `cond`: the loop condition of a stop-mode frame graph (nullptr: none).
+void iteration_b(Batch* s, bool first, int par, float dt, int rec_base, cudaStream_t st,
+                 const cudaGraphConditionalHandle* cond) {
   const xpbd_params& p = s->prm;
+  const bool stop = stop_mode_b(p);
   const float inv_dt2 = (float)(1.0 / ((double)dt * (double)dt));
+  s->d.stop_par = stop ? par : -1;
   {
     BProf pr(s, XPBD_K_PROJECT, st);
     const bool blk = p.block_mode != 0;
-    if (it == 0) blk ? project_b<true, true>(s, inv_dt2, st) : project_b<false, true>(s, inv_dt2, st);
+    if (first) blk ? project_b<true, true>(s, inv_dt2, st) : project_b<false, true>(s, inv_dt2, st);
     else blk ? project_b<true, false>(s, inv_dt2, st) : project_b<false, false>(s, inv_dt2, st);
   }
   const bool cheb = p.cheb_enable != 0, mon = p.monitor != 0;
-  if (cheb || mon) {
+  if (cheb || mon || stop) {
     BSweep a;
     a.cur = s->cur;
     a.inv_dt2 = inv_dt2;
-    a.it = it;
+    a.par = par;
     a.warmup = p.cheb_warmup;
-    a.rec = rec;
+    a.rec_base = rec_base;
+    a.res = cheb;
+    a.stop = stop;
     a.rho_min = p.rho_min;
     a.rho_max = p.rho_max;
     a.rho_beta = p.rho_beta;
+    a.target = p.target_rel_residual;
+    a.floor = p.residual_floor;
     BProf pr(s, XPBD_K_RESIDUAL, st);
-    if (cheb && mon) residual_b<true, true>(s, a, st);
-    else if (cheb) residual_b<true, false>(s, a, st);
+    if ((cheb || stop) && mon) residual_b<true, true>(s, a, st);
+    else if (cheb || stop) residual_b<true, false>(s, a, st);
     else residual_b<false, true>(s, a, st);
   }
   BProf pr(s, XPBD_K_UPDATE, st);
   const int g = (nblk(s->d.V) + kBUpdateBlocks - 1) / kBUpdateBlocks;
+  BUpd u{};
+  u.par = par;
+  u.K = p.constraints_iter;
+  u.stop = stop;
+  u.use_cond = cond != nullptr;
+  if (cond) u.cond = *cond;
   if (cheb) {
-    if (it == 0) kb_update<true, true><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma);
-    else kb_update<true, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma);
+    if (first) kb_update<true, true><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
+    else kb_update<true, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
     s->cur ^= 1;
   } else {
-    kb_update<false, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma);
+    kb_update<false, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
   }
+  s->d.stop_par = -1;
+}
+
+// Stop mode under capture: iterations 0 and 1 as plain nodes, then a WHILE
+// conditional node over iterations of parity 0 and 1, looping while any body
+// iterates (the condition comes from every update from iteration 1 on).
+int capture_stop_loop_b(Batch* s, float dt, int rec_base, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  B_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  if (cs != cudaStreamCaptureStatusActive || !g) return bfail(XPBD_ERR_CUDA, "stop-mode loop outside a capture");
+  cudaGraphConditionalHandle h = 0;
+  B_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+  iteration_b(s, true, 0, dt, rec_base, st, nullptr);
+  iteration_b(s, false, 1, dt, rec_base, st, &h);
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edges = nullptr;
+  size_t nd = 0;
+  B_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edges, &nd));
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  B_CUDA(cudaGraphAddNode(&node, g, deps, edges, nd, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  B_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  B_CUDA(cudaStreamBeginCaptureToGraph(s->cap_body, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  iteration_b(s, false, 0, dt, rec_base, s->cap_body, &h);
+  iteration_b(s, false, 1, dt, rec_base, s->cap_body, &h);
+  cudaGraph_t out = nullptr;
+  B_CUDA(cudaStreamEndCapture(s->cap_body, &out));
+  return XPBD_OK;
 }
 
 int substep_b(Batch* s, float dt, int rec_base, cudaStream_t st) {
   const int K = s->prm.constraints_iter;
   if (rec_base >= 0 && rec_base + K > s->d.max_records) return bfail(XPBD_ERR_HISTORY_FULL, "history full");
+  const bool stop = stop_mode_b(s->prm);
   s->cur = 0;
   {
     BProf pr(s, XPBD_K_BEGIN, st);
-    kb_begin<<<nblk(s->d.V), 256, 0, st>>>(s->d, dt, s->prm.gravity[0], s->prm.gravity[1], s->prm.gravity[2]);
+    kb_begin<<<nblk(s->d.V), 256, 0, st>>>(s->d, dt, s->prm.gravity[0], s->prm.gravity[1], s->prm.gravity[2], K);
   }
-  for (int it = 0; it < K; ++it) iteration_b(s, it, dt, rec_base >= 0 ? rec_base + it : -1, st);
+  if (stop && s->capturing && K > 2) {
+    int r = capture_stop_loop_b(s, dt, rec_base, st);
+    if (r) return r;
+  } else {
+    for (int it = 0; it < K; ++it) iteration_b(s, it == 0, it & 1, dt, rec_base, st, nullptr);
+  }
+  const int sub = rec_base >= 0 && K > 0 ? rec_base / K : -1;
   BProf pr(s, XPBD_K_END, st);
-  kb_end<<<nblk(s->d.V), 256, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
+  kb_end<<<nblk(s->d.V), 256, 0, st>>>(s->d, s->cur, dt, s->prm.damping, stop ? 1 : 0, s->prm.cheb_enable ? 1 : 0,
+                                      sub);
   return XPBD_OK;
 }
 
@@ -757,9 +899,12 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
   if ((body->tet_inv_mu == nullptr) != (body->tet_inv_lambda == nullptr))
     return bfail(XPBD_ERR_INVALID_ARGUMENT, "per-tet materials need both tet_inv_mu and tet_inv_lambda");
   if (max_records < 0) return bfail(XPBD_ERR_INVALID_ARGUMENT, "max_records < 0");
+  if (!(params->target_rel_residual >= 0.0) || !(params->residual_floor >= 0.0))
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "target_rel_residual and residual_floor must be >= 0");
   Batch* s = new (std::nothrow) Batch();
   if (!s) return bfail(XPBD_ERR_INVALID_ARGUMENT, "out of host memory");
   s->prm = *params;
+  s->d.stop_par = -1;
   s->n_out = body->n_out_verts;
   BDev& d = s->d;
   d.V = body->n_verts;
@@ -797,7 +942,10 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
     if (d.bs) cudaFree(d.bs);
     if (d.flags) cudaFree(d.flags);
     if (d.hist) cudaFree(d.hist);
+    if (d.ctl) cudaFree(d.ctl);
+    if (d.iters) cudaFree(d.iters);
     if (s->cap) cudaStreamDestroy(s->cap);
+    if (s->cap_body) cudaStreamDestroy(s->cap_body);
     delete s;
     return st;
   };
@@ -808,7 +956,10 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
   if (e == cudaSuccess) e = cudaMalloc(&d.bs, sizeof(BodyState) * d.n_bodies);
   if (e == cudaSuccess) e = cudaMalloc(&d.flags, sizeof(Flags));
   if (e == cudaSuccess) e = cudaMalloc(&d.hist, sizeof(double) * 4 * (size_t)d.max_records * d.n_bodies);
+  if (e == cudaSuccess) e = cudaMalloc(&d.ctl, sizeof(Ctl));
+  if (e == cudaSuccess) e = cudaMalloc(&d.iters, sizeof(int) * (size_t)kMaxCountedSubsteps * d.n_bodies);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_body, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cleanup(bfail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
   std::vector<BodyState> hb(d.n_bodies);
   for (auto& b : hb) {
@@ -820,6 +971,8 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
   e = cudaMemcpy(d.bs, hb.data(), sizeof(BodyState) * d.n_bodies, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(d.flags, &hf, sizeof(hf), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(d.hist, 0, sizeof(double) * 4 * (size_t)d.max_records * d.n_bodies);
+  if (e == cudaSuccess) e = cudaMemset(d.ctl, 0, sizeof(Ctl));
+  if (e == cudaSuccess) e = cudaMemset(d.iters, 0, sizeof(int) * (size_t)kMaxCountedSubsteps * d.n_bodies);
   if (e != cudaSuccess) return cleanup(bfail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
   {
     int dev = 0, sms = 0, bps = 0;
@@ -861,7 +1014,10 @@ int xpbd_batch_destroy(void* h) {
   cudaFree(s->d.bs);
   cudaFree(s->d.flags);
   cudaFree(s->d.hist);
+  cudaFree(s->d.ctl);
+  cudaFree(s->d.iters);
   if (s->cap) cudaStreamDestroy(s->cap);
+  if (s->cap_body) cudaStreamDestroy(s->cap_body);
   delete s;
   return XPBD_OK;
 }
@@ -889,7 +1045,9 @@ int xpbd_batch_solve(void* h, double frame_dt, double dt, int32_t substeps, void
   if (!(s->exec && s->key_frame_dt == frame_dt && s->key_dt == dt && s->key_sub == substeps)) {
     drop_b(s);
     B_CUDA(cudaStreamBeginCapture(s->cap, cudaStreamCaptureModeThreadLocal));
+    s->capturing = true;
     int r = frame_b(s, frame_dt, dt, substeps, s->cap);
+    s->capturing = false;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(s->cap, &g);
     if (r) {
@@ -921,6 +1079,18 @@ int xpbd_batch_read_history(void* h, double* out, int32_t n, void* stream) {
   return XPBD_OK;
 }
 
+int xpbd_batch_read_iterations(void* h, int32_t* host_out, int32_t n, void* stream) {
+  Batch* s = static_cast<Batch*>(h);
+  if (!s || !host_out || n < 0 || n > kMaxCountedSubsteps)
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "bad iteration-count read (n must be 0.." +
+                                                std::to_string(kMaxCountedSubsteps) + ")");
+  B_CUDA(cudaStreamSynchronize(BS(stream)));
+  for (int b = 0; b < s->d.n_bodies && n > 0; ++b)
+    B_CUDA(cudaMemcpy(host_out + (size_t)b * n, s->d.iters + (size_t)b * kMaxCountedSubsteps, sizeof(int) * (size_t)n,
+                      cudaMemcpyDeviceToHost));
+  return XPBD_OK;
+}
+
 int xpbd_batch_get_rho_hat(void* h, double* out, void* stream) {
   Batch* s = static_cast<Batch*>(h);
   if (!s || !out) return bfail(XPBD_ERR_INVALID_ARGUMENT, "bad argument");
@@ -943,6 +1113,8 @@ int xpbd_batch_check_status(void* h, void* stream) {
 int xpbd_batch_export_vec3(void* h, int32_t field, float* dst, void* stream) {
   Batch* s = static_cast<Batch*>(h);
   if (!s || !dst) return bfail(XPBD_ERR_INVALID_ARGUMENT, "bad argument");
+  if (field == XPBD_FIELD_PRED_X && stop_mode_b(s->prm))
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "in stop mode the predicted positions sit in a per-body buffer");
   const float4* f = field == XPBD_FIELD_X ? s->d.x : field == XPBD_FIELD_V ? s->d.v
                     : field == XPBD_FIELD_PRED_X ? s->d.p[s->cur] : nullptr;
   if (!f) return bfail(XPBD_ERR_INVALID_ARGUMENT, "unknown field");
@@ -954,6 +1126,8 @@ int xpbd_batch_export_vec3(void* h, int32_t field, float* dst, void* stream) {
 int xpbd_batch_import_vec3(void* h, int32_t field, const float* src, void* stream) {
   Batch* s = static_cast<Batch*>(h);
   if (!s || !src) return bfail(XPBD_ERR_INVALID_ARGUMENT, "bad argument");
+  if (field == XPBD_FIELD_PRED_X && stop_mode_b(s->prm))
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "in stop mode the predicted positions sit in a per-body buffer");
   float4* f = field == XPBD_FIELD_X ? s->d.x : field == XPBD_FIELD_V ? s->d.v
               : field == XPBD_FIELD_PRED_X ? s->d.p[s->cur] : nullptr;
   if (!f) return bfail(XPBD_ERR_INVALID_ARGUMENT, "unknown field");
@@ -1002,6 +1176,8 @@ int xpbd_batch_set_params(void* h, const xpbd_params* params) {
   if (!s || !params) return bfail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or params");
   if (params->constraints_iter < 0 || params->cheb_warmup < 0)
     return bfail(XPBD_ERR_INVALID_ARGUMENT, "constraints_iter and cheb_warmup must be >= 0");
+  if (!(params->target_rel_residual >= 0.0) || !(params->residual_floor >= 0.0))
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "target_rel_residual and residual_floor must be >= 0");
   if (std::memcmp(&s->prm, params, sizeof(xpbd_params)) != 0) drop_b(s);
   s->prm = *params;
   return XPBD_OK;
@@ -1025,6 +1201,7 @@ int xpbd_batch_load_rho_hat(void* h, const double* src_device, void* stream) {
 
 static int check_batch_diff(Batch* s) {
   if (!s->prm.block_mode) return bfail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint supports block mode only");
+  if (stop_mode_b(s->prm)) return bfail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint needs a fixed iteration count");
   if (s->prm.constraints_iter > s->d.max_records)
     return bfail(XPBD_ERR_HISTORY_FULL, "history shorter than constraints_iter");
   return XPBD_OK;
@@ -1043,16 +1220,16 @@ int xpbd_batch_substep_tape(void* h, float dt, const xpbd_tape* tape, void* stre
   const float* g = s->prm.gravity;
   k_tape_begin<BDev><<<nblk(V), 256, 0, st>>>(s->d, tp, dt, g[0], g[1], g[2]);
   s->cur = 0;
-  kb_begin<<<nblk(V), 256, 0, st>>>(s->d, dt, g[0], g[1], g[2]);
+  kb_begin<<<nblk(V), 256, 0, st>>>(s->d, dt, g[0], g[1], g[2], K);
   for (int it = 0; it < K; ++it) {
     B_CUDA(cudaMemcpyAsync(tp.xs + (size_t)it * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
     if (it == 0) B_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
     else
       B_CUDA(cudaMemcpyAsync(tp.lams + (size_t)it * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
-    iteration_b(s, it, dt, it, st);
+    iteration_b(s, it == 0, it & 1, dt, 0, st, nullptr);
   }
   B_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
-  kb_end<<<nblk(V), 256, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
+  kb_end<<<nblk(V), 256, 0, st>>>(s->d, s->cur, dt, s->prm.damping, 0, 0, -1);
   B_CUDA(cudaGetLastError());
   return XPBD_OK;
 }

@@ -40,8 +40,14 @@ struct SweepSlot {
   double prev_r_hat;
   double inv_prev;  // 1 / (prev_r_hat + 1e-12)
   double omega;     // omega of the previous iteration of this substep
+  double r0;        // r_hat of the substep's first iteration (stop mode)
   int has_prev;     // prev_r_hat is not None
+  int it;           // index of the iteration this slot enters
+  int active;       // stop mode: 0 once the substep has stopped iterating
 };
+
+// Substeps of one frame whose iteration counts are kept (DevState::iters).
+constexpr int kMaxCountedSubsteps = 256;
 
 // Iteration k's residual sweep adds into acc[k & 1]; iteration k's update
 // reads slot[k & 1] and acc[k & 1], and its first CTA writes slot[(k+1) & 1]
@@ -53,6 +59,10 @@ struct DevState {
   int nonfinite;        // sticky: a residual sum was NaN/Inf
   int bad_mesh;         // set by the index validation kernel
   int timeout;          // sticky: a bounded mbarrier wait gave up
+  int pos_cur;          // buffer p[] holding the predicted positions after
+                        // the last iteration that ran (stop mode)
+  int iters[kMaxCountedSubsteps];  // iterations run by substep s of the frame
+  unsigned long long total_iters;  // iterations run since create (residual sweeps ended)
 };
 
 struct Dev {
@@ -86,9 +96,20 @@ struct Dev {
   int n_sdf;
   DevState* st;
   double* hist;
+  // stop mode (xpbd_params.target_rel_residual > 0): the `active` flag of the
+  // slot entering the launched iteration; nullptr = always run
+  const int* act;
+  int dyn_end;  // stop mode: advance and the vertex-field accessors read p[st->pos_cur]
 };
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+// Stop mode: the iteration this launch belongs to is not run (the substep
+// already met its residual target or iteration cap).  Every CTA reads the
+// same flag, which an earlier kernel wrote.
+__device__ __forceinline__ bool stopped(const Dev& d) {
+  return d.act != nullptr && *reinterpret_cast<const volatile int*>(d.act) == 0;
+}
 
 // ---------------------------------------------------------------------------
 // vertex kernels
@@ -107,6 +128,10 @@ __global__ void __launch_bounds__(kBlock) k_begin(Dev d, float dt, float gx, flo
     s0.inv_prev = 0.0;
     s0.omega = 1.0;
     s0.has_prev = 0;
+    s0.r0 = 0.0;
+    s0.it = 0;
+    s0.active = 1;
+    d.st->pos_cur = dst;
     d.st->acc[0][0] = d.st->acc[0][1] = d.st->acc[0][2] = 0.0;
   }
   if (i >= d.V) return;
@@ -130,10 +155,12 @@ __global__ void __launch_bounds__(kBlock) k_begin(Dev d, float dt, float gx, flo
   d.p[dst][i] = make_float4(p.x, p.y, p.z, w);
 }
 
-// advance (xpbd_base.py:148-160) from p[cur].
+// advance (xpbd_base.py:148-160) from p[cur] (stop mode: from the buffer the
+// last iteration that ran left the positions in).
 __global__ void __launch_bounds__(kBlock) k_end(Dev d, int cur, float dt, float damping) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.V) return;
+  if (d.dyn_end) cur = d.st->pos_cur;
   const float4 xi = d.x[i];
   if (xi.w <= 0.f) {
     d.p[cur][i] = xi;  // fixed vertices do not move
@@ -150,7 +177,7 @@ __global__ void __launch_bounds__(kBlock) k_end(Dev d, int cur, float dt, float 
 // (tet, corner) order, i.e. the order of a sequential scatter.
 __global__ void __launch_bounds__(kBlock) k_gather(Dev d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= d.V) return;
+  if (i >= d.V || stopped(d)) return;
   const int b = d.v2t_off[i], e = d.v2t_off[i + 1];
   float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
   for (int k = b; k < e; ++k) {
@@ -167,32 +194,48 @@ __global__ void __launch_bounds__(kBlock) k_gather(Dev d) {
 // (:131-142, :548-549).  x_post = p[cur] + dx / count; with kCheb the result
 //   y_prev + omega * (gamma * (x_post - y_curr) + y_curr - y_prev)
 // is written to p[1-cur] (which held y_prev), else x_post goes to p[cur].
-// What the update of iteration `it` needs to finish its residual sweep.
+// What the update of one iteration needs to finish its residual sweep.  The
+// iteration's index comes from the slot it enters (slot[par]), so the same
+// launch can be replayed by a loop in the frame graph.
 struct UpdArgs {
-  int it, rec, last, warmup;
-  int res, mon;  // the sweep summed residuals (Chebyshev) / monitoring means
+  int par;       // slot parity of the iteration (its index & 1)
+  int rec_base;  // history row of the substep's iteration 0 (-1: no records)
+  int K;         // iterations per substep (stop mode: the cap)
+  int warmup;
+  int res, mon;  // Chebyshev recurrence / monitoring means
+  int stop;      // stop mode: end the substep at the residual target
+  int sub;       // substep index for DevState::iters (-1: not counted)
+  int cur_next;  // buffer holding the positions after this iteration
+  int use_cond;  // set the frame graph's loop condition (cond)
+  cudaGraphConditionalHandle cond;
   double inv_n;  // 1 / tet count (0 for an empty mesh)
   double rho_min, rho_max, rho_beta;
+  double target, floor;  // stop at r_hat <= target * r_hat_0 or r_hat <= floor
 };
 
 // The end of a residual sweep (neohookean_solver.py:495-504, :537-546): r_hat
-// from the sweep's sums, the rho_hat recurrence and omega of iteration u.it.
+// from the sweep's sums, the rho_hat recurrence and omega of the iteration.
 // Every CTA of the update evaluates it (thread 0); CTA 0 also stores the
 // state entering the next iteration, clears the next sweep's accumulators,
-// writes history row `rec` = {r_hat, omega, hydro, dev}, and at the last
-// iteration the persistent rho_hat.  Every CTA runs one FP64 division (omega);
-// r_hat / n and r_hat / prev_r_hat are products with reciprocals that the
-// host (1 / n) and the previous iteration's CTA 0 (1 / prev) computed.
+// writes history row rec_base + it = {r_hat, omega, hydro, dev}, and after
+// the substep's last iteration the persistent rho_hat.  Every CTA runs one
+// FP64 division (omega); r_hat / n and r_hat / prev_r_hat are products with
+// reciprocals that the host (1 / n) and the previous iteration's CTA 0
+// (1 / prev) computed.
+// Stop mode: the substep ends after iteration k once r_hat_k <= target *
+// r_hat_0 or r_hat_k <= floor (or at the cap); the remaining iterations'
+// kernels return at once, and CTA 0 sets the frame graph's loop condition.
 __device__ __forceinline__ float sweep_step(const Dev& d, const UpdArgs& u) {
   DevState* st = d.st;
-  const SweepSlot c = st->slot[u.it & 1];
-  const double* acc = st->acc[u.it & 1];
+  const SweepSlot c = st->slot[u.par];
+  const double* acc = st->acc[u.par];
   const double S = acc[0], Hs = acc[1], Ds = acc[2];
   const double n = (double)d.T;
+  const int it = c.it;
   SweepSlot nx = c;
   double r_hat = 0.0, omega = 1.0;
+  if (u.res || u.stop) r_hat = S * u.inv_n;
   if (u.res) {
-    r_hat = S * u.inv_n;
     if (c.has_prev && c.prev_r_hat > 1e-12) {
       double rho_inst = r_hat * c.inv_prev;
       rho_inst = fmax(u.rho_min, fmin(u.rho_max, rho_inst));
@@ -201,27 +244,48 @@ __device__ __forceinline__ float sweep_step(const Dev& d, const UpdArgs& u) {
     nx.prev_r_hat = r_hat;
     nx.has_prev = 1;
     const double rho2 = nx.rho_hat * nx.rho_hat;
-    if (u.it < u.warmup) omega = 1.0;
-    else if (u.it == u.warmup) omega = 2.0 / (2.0 - rho2);
+    if (it < u.warmup) omega = 1.0;
+    else if (it == u.warmup) omega = 2.0 / (2.0 - rho2);
     else omega = 4.0 / (4.0 - rho2 * c.omega);
     nx.omega = omega;
   }
+  bool more = it + 1 < u.K;
+  if (u.stop) {
+    if (it == 0) nx.r0 = r_hat;
+    if (r_hat <= u.target * nx.r0 || r_hat <= u.floor) more = false;
+  }
+  nx.it = it + 1;
+  nx.active = more ? 1 : 0;
   if (blockIdx.x == 0) {
-    if (u.res && !isfinite(S)) st->nonfinite = 1;
+    if ((u.res || u.stop) && !isfinite(S)) st->nonfinite = 1;
     if (u.res) nx.inv_prev = 1.0 / (r_hat + 1e-12);
-    st->slot[(u.it + 1) & 1] = nx;
-    double* an = st->acc[(u.it + 1) & 1];
+    st->slot[u.par ^ 1] = nx;
+    double* an = st->acc[u.par ^ 1];
     an[0] = an[1] = an[2] = 0.0;
-    if (u.last) st->rho_hat = nx.rho_hat;
-    if (u.rec >= 0) {
-      double* h = d.hist + 4 * (size_t)u.rec;
+    if (!more) st->rho_hat = nx.rho_hat;
+    if (u.rec_base >= 0) {
+      double* h = d.hist + 4 * ((size_t)u.rec_base + it);
       h[0] = r_hat;
       h[1] = omega;
       h[2] = u.mon && d.T > 0 ? Hs / n : 0.0;
       h[3] = u.mon && d.T > 0 ? Ds / n : 0.0;
     }
+    if (u.stop) st->pos_cur = u.cur_next;
+    if (u.sub >= 0 && u.sub < kMaxCountedSubsteps) st->iters[u.sub] = it + 1;
+    st->total_iters += 1ull;
+    if (u.use_cond) cudaGraphSetConditional(u.cond, more ? 1u : 0u);
   }
   return (float)omega;
+}
+
+// Stop mode, an iteration that does not run: CTA 0 carries the slot (and its
+// `active` = 0) over to the next parity and keeps the graph's loop closed.
+__device__ __forceinline__ void skip_step(const Dev& d, const UpdArgs& u) {
+  DevState* st = d.st;
+  SweepSlot nx = st->slot[u.par];
+  nx.it += 1;
+  st->slot[u.par ^ 1] = nx;
+  if (u.use_cond) cudaGraphSetConditional(u.cond, 0u);
 }
 
 template <bool kCheb, bool kFirstIt, bool kResetDx>
@@ -242,8 +306,15 @@ __global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma, 
     }
   }
   __shared__ float s_om;
-  if (threadIdx.x == 0) s_om = (u.res || u.mon) ? sweep_step(d, u) : 1.f;
+  __shared__ int s_run;
+  if (threadIdx.x == 0) {
+    const bool run = !stopped(d);
+    s_run = run;
+    if (run) s_om = (u.res || u.mon || u.stop) ? sweep_step(d, u) : 1.f;
+    else if (blockIdx.x == 0) skip_step(d, u);
+  }
   __syncthreads();
+  if (!s_run) return;
   const float om = kCheb ? s_om : 1.f;
 #pragma unroll
   for (int k = 0; k < kUpdateVerts; ++k) {
@@ -300,6 +371,7 @@ __device__ __forceinline__ void emit(const Dev& d, int t, int corner, int vid, f
 // cD, cH = 1 / (mu dt^2), 1 / (lambda dt^2): aD = alpha_D / dt^2 = cD / V0.
 template <bool kBlockMode, bool kFirst, bool kPrecise, bool kGather>
 __global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float cD, float cH, float relax_h, float relax_d) {
+  if (stopped(d)) return;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= d.T) return;
   int4 id;
@@ -400,6 +472,7 @@ __device__ __forceinline__ int walk_patch(int q, int n, bool reverse) { return r
 template <bool kBlockMode, bool kFirst, bool kPrecise>
 __global__ void __launch_bounds__(256) k_project_tile(Dev d, int cur, float cD, float cH, float relax_h,
                                                      float relax_d) {
+  if (stopped(d)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TileSmem<false>& sm = *reinterpret_cast<TileSmem<false>*>(smem_raw);
   __shared__ int abort_flag;
@@ -497,9 +570,8 @@ __device__ __forceinline__ float3 post_position(const float4 p, const float4 D) 
 struct SweepArgs {
   int cur;
   float cD, cH;  // 1 / (mu dt^2), 1 / (lambda dt^2)
-  int it, warmup, rec;
-  int reverse;  // tile residual: visit patches last-to-first
-  double rho_min, rho_max, rho_beta;
+  int par;       // accumulators acc[par] (the iteration's index & 1)
+  int reverse;   // tile residual: visit patches last-to-first
 };
 
 // Block FP64 reduction of the per-thread partial sums, added into the
@@ -523,7 +595,7 @@ __device__ __forceinline__ void finish_residual(const Dev& d, const SweepArgs& a
     b1 += red[1][k];
     b2 += red[2][k];
   }
-  double* acc = d.st->acc[a.it & 1];
+  double* acc = d.st->acc[a.par];
   if (kRes) atomicAdd(acc, b0);
   if (kMon) {
     atomicAdd(acc + 1, b1);
@@ -555,6 +627,7 @@ __device__ __forceinline__ void residual_terms(const Tet& tt, float2 L, float aD
 // FP32 partials, then finish_residual.
 template <bool kRes, bool kMon, bool kPrecise>
 __global__ void __launch_bounds__(kBlock) k_residual(Dev d, SweepArgs a) {
+  if (stopped(d)) return;
   float sr = 0.f, sh = 0.f, sd = 0.f;
   const float4* P = d.p[a.cur];
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < d.T; t += gridDim.x * blockDim.x) {
@@ -585,6 +658,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(Dev d, SweepArgs a) {
 // post-Jacobi positions in shared memory before the tets use them.
 template <bool kRes, bool kMon, bool kPrecise>
 __global__ void __launch_bounds__(256) k_residual_tile(Dev d, SweepArgs a) {
+  if (stopped(d)) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TileSmem<true>& sm = *reinterpret_cast<TileSmem<true>*>(smem_raw);
   __shared__ int abort_flag;
@@ -686,6 +760,7 @@ __global__ void __launch_bounds__(256) k_residual_tile(Dev d, SweepArgs a) {
 template <bool kBlockMode, bool kFirst, bool kPrecise, int kP, bool kReduce>
 __global__ void __launch_bounds__(kP) k_project_patch1(Dev d, int cur, float cD, float cH, float relax_h,
                                                       float relax_d) {
+  if (stopped(d)) return;
   __shared__ float4 sp[256];
   __shared__ int sg[256];
   __shared__ float4 sdp[kReduce ? 4 * kP : 1];
@@ -763,6 +838,7 @@ __global__ void __launch_bounds__(kP) k_project_patch1(Dev d, int cur, float cD,
 template <bool kBlockMode, bool kFirst, bool kPrecise, int kP, int kTPT>
 __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) k_project_patchN(Dev d, int cur, float cD, float cH, float relax_h,
                                                              float relax_d) {
+  if (stopped(d)) return;
   constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
   __shared__ int sg[256];
@@ -806,6 +882,7 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) k_project
 
 template <bool kRes, bool kMon, bool kPrecise, int kP>
 __global__ void __launch_bounds__(kP) k_residual_patch1(Dev d, SweepArgs a) {
+  if (stopped(d)) return;
   __shared__ float4 sp[256];
   float sr = 0.f, sh = 0.f, sd = 0.f;
   const float4* P = d.p[a.cur];
@@ -851,6 +928,7 @@ __global__ void __launch_bounds__(kP) k_residual_patch1(Dev d, SweepArgs a) {
 // the vertex tile lets both sets of loads be in flight together.
 template <bool kRes, bool kMon, bool kPrecise, int kP, int kTPT>
 __global__ void __launch_bounds__(kP / kTPT) k_residual_patchN(Dev d, SweepArgs a) {
+  if (stopped(d)) return;
   constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
   float sr = 0.f, sh = 0.f, sd = 0.f;
@@ -903,9 +981,11 @@ __global__ void __launch_bounds__(kP / kTPT) k_residual_patchN(Dev d, SweepArgs 
 }
 
 // Field transfer in caller vertex order (mesh.verts.<f>.from_numpy / to_numpy).
+// f == nullptr: the predicted positions of stop mode, p[st->pos_cur].
 __global__ void __launch_bounds__(kBlock) k_import(Dev d, float4* f, const float* __restrict__ src) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.V) return;
+  if (!f) f = d.p[d.st->pos_cur];
   const int j = d.perm ? d.perm[i] : i;
   float4 o = f[i];
   o.x = src[3 * (size_t)j];
@@ -917,6 +997,7 @@ __global__ void __launch_bounds__(kBlock) k_import(Dev d, float4* f, const float
 __global__ void __launch_bounds__(kBlock) k_export(Dev d, const float4* f, float* __restrict__ dst) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.V) return;
+  if (!f) f = d.p[d.st->pos_cur];
   const int j = d.perm ? d.perm[i] : i;
   const float4 o = f[i];
   dst[3 * (size_t)j] = o.x;
@@ -1011,7 +1092,12 @@ __global__ void __launch_bounds__(kBlock) k_residual_noalloc(Dev d, float cD, fl
       tt.p[c] = make_float4(q.x, q.y, q.z, 0.f);
     }
     const float inv_v0 = 1.f / tt.V0;
-    residual_terms<true, true, kPrecise>(tt, d.lam[t], cD * inv_v0, cH * inv_v0, sr, sh, sd);
+    float aD = cD * inv_v0, aH = cH * inv_v0;
+    if (d.tinv_mu) {  // per-tet materials: cD = cH = 1 / dt^2
+      aD *= __ldg(d.tinv_mu + t);
+      aH *= __ldg(d.tinv_la + t);
+    }
+    residual_terms<true, true, kPrecise>(tt, d.lam[t], aD, aH, sr, sh, sd);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const double r0 = warp_sum((double)sr), r1 = warp_sum((double)sh), r2 = warp_sum((double)sd);
@@ -1146,6 +1232,7 @@ struct Solver {
   int max_records = 0;
   int cur = 0;  // buffer holding the current predicted positions
   cudaStream_t cap = nullptr;
+  cudaStream_t cap_body = nullptr;  // captures the body of a stop-mode loop node
   cudaGraphExec_t exec = nullptr;
   GraphKey key;
   // profiling with use_graph: the frame graph carries an event record node
@@ -1208,8 +1295,13 @@ int check_params(const xpbd_params* p) {
     return fail(XPBD_ERR_INVALID_ARGUMENT, "tets_per_thread must be 0, 1, 2 or 4");
   if (!(p->lame_mu != 0.f) || !(p->lame_lambda != 0.f))
     return fail(XPBD_ERR_INVALID_ARGUMENT, "Lame parameters must be non-zero");
+  if (!(p->target_rel_residual >= 0.0) || !(p->residual_floor >= 0.0))
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "target_rel_residual and residual_floor must be >= 0");
   return XPBD_OK;
 }
+
+// Stop mode: each substep iterates until its residual target (or the cap).
+inline bool stop_mode(const xpbd_params& p) { return p.target_rel_residual > 0.0 || p.residual_floor > 0.0; }
 
 // ---- launch helpers (all stream-ordered, no sync) --------------------------
 
@@ -1334,58 +1426,67 @@ void launch_residual_t(Solver* s, const SweepArgs& a, int grid, cudaStream_t st)
   else k_residual<kRes, kMon, false><<<grid, kBlock, 0, st>>>(s->d, a);
 }
 
-SweepArgs sweep_args(Solver* s, int it, float dt, int rec) {
+SweepArgs sweep_args(Solver* s, int par, float dt) {
   const xpbd_params& p = s->prm;
   SweepArgs a;
   a.cur = s->cur;
   compliance_factors(s, dt, a.cD, a.cH);
-  a.it = it;
-  a.warmup = p.cheb_warmup;
-  a.rec = rec;
+  a.par = par;
   a.reverse = p.sweep_order == 1 ? 1 : 0;
-  a.rho_min = p.rho_min;
-  a.rho_max = p.rho_max;
-  a.rho_beta = p.rho_beta;
   return a;
 }
 
 void launch_residual(Solver* s, const SweepArgs& a, cudaStream_t st) {
-  const bool cheb = s->prm.cheb_enable != 0, mon = s->prm.monitor != 0;
+  // residuals are summed for the Chebyshev recurrence and for stop mode
+  const bool res = s->prm.cheb_enable != 0 || stop_mode(s->prm), mon = s->prm.monitor != 0;
   int grid = blocks_for(s->d.T);
   if (grid > s->res_grid) grid = s->res_grid;
   if (grid < 1) grid = 1;
   Prof prof(s, XPBD_K_RESIDUAL, st);
-  if (cheb && mon) launch_residual_t<true, true>(s, a, grid, st);
-  else if (cheb) launch_residual_t<true, false>(s, a, grid, st);
+  if (res && mon) launch_residual_t<true, true>(s, a, grid, st);
+  else if (res) launch_residual_t<true, false>(s, a, grid, st);
   else launch_residual_t<false, true>(s, a, grid, st);
 }
 
-// One Jacobi iteration (neohookean_solver.py:474-556).
-void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
+// One Jacobi iteration (neohookean_solver.py:474-556).  `first`: the
+// substep's iteration 0 (lambda reset); `par`: its index & 1; `sub`: the
+// substep's index in the frame (for the iteration counts, -1: none); `cond`:
+// the loop condition a stop-mode frame graph iterates on (nullptr: none).
+void launch_iteration(Solver* s, bool first, int par, float dt, int rec_base, int sub, cudaStream_t st,
+                      const cudaGraphConditionalHandle* cond) {
   const xpbd_params& p = s->prm;
-  launch_project(s, it == 0, dt, st);
+  const bool stop = stop_mode(p);
+  s->d.act = stop ? &s->d.st->slot[par].active : nullptr;
+  launch_project(s, first, dt, st);
   if (p.scatter == XPBD_SCATTER_GATHER) {
     Prof prof(s, XPBD_K_GATHER, st);
     k_gather<<<blocks_for(s->d.V), kBlock, 0, st>>>(s->d);
   }
   const bool cheb = p.cheb_enable != 0, mon = p.monitor != 0;
-  if (cheb || mon) launch_residual(s, sweep_args(s, it, dt, rec), st);
+  if (cheb || mon || stop) launch_residual(s, sweep_args(s, par, dt), st);
   const int g = (s->d.V + kBlock * kUpdateVerts - 1) / (kBlock * kUpdateVerts);
   const bool reset = p.scatter != XPBD_SCATTER_GATHER;
-  UpdArgs u;
-  u.it = it;
-  u.rec = rec;
-  u.last = it == p.constraints_iter - 1;
+  UpdArgs u{};
+  u.par = par;
+  u.rec_base = rec_base;
+  u.K = p.constraints_iter;
   u.warmup = p.cheb_warmup;
   u.res = cheb;
   u.mon = mon;
+  u.stop = stop;
+  u.sub = sub;
+  u.cur_next = cheb ? s->cur ^ 1 : s->cur;
+  u.use_cond = cond != nullptr;
+  if (cond) u.cond = *cond;
   u.inv_n = s->d.T > 0 ? 1.0 / (double)s->d.T : 0.0;
   u.rho_min = p.rho_min;
   u.rho_max = p.rho_max;
   u.rho_beta = p.rho_beta;
+  u.target = p.target_rel_residual;
+  u.floor = p.residual_floor;
   Prof prof(s, XPBD_K_UPDATE, st);
   if (cheb) {
-    if (it == 0) {
+    if (first) {
       if (reset) k_update<true, true, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
       else k_update<true, true, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
     } else {
@@ -1397,10 +1498,51 @@ void launch_iteration(Solver* s, int it, float dt, int rec, cudaStream_t st) {
     if (reset) k_update<false, false, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
     else k_update<false, false, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
   }
+  s->d.act = nullptr;
 }
 
-void launch_iterations(Solver* s, int K, float dt, int record_base, cudaStream_t st) {
-  for (int it = 0; it < K; ++it) launch_iteration(s, it, dt, record_base >= 0 ? record_base + it : -1, st);
+// Stop mode under capture: iterations 0 and 1 as plain nodes, then a WHILE
+// conditional node whose body is iterations of parity 0 and 1.  The update of
+// every iteration from 1 on sets the loop condition (CTA 0, after the
+// residual target test), so the graph launches no kernel of a substep that
+// has stopped, except the rest of a body pass that started before it stopped;
+// those kernels return at once.
+int capture_stop_loop(Solver* s, float dt, int record_base, int sub, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  XPBD_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  if (cs != cudaStreamCaptureStatusActive || !g) return fail(XPBD_ERR_CUDA, "stop-mode loop outside a capture");
+  cudaGraphConditionalHandle h = 0;
+  XPBD_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+  launch_iteration(s, true, 0, dt, record_base, sub, st, nullptr);
+  launch_iteration(s, false, 1, dt, record_base, sub, st, &h);
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* edges = nullptr;
+  size_t nd = 0;
+  XPBD_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edges, &nd));
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  XPBD_CUDA(cudaGraphAddNode(&node, g, deps, edges, nd, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  XPBD_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  XPBD_CUDA(cudaStreamBeginCaptureToGraph(s->cap_body, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  launch_iteration(s, false, 0, dt, record_base, sub, s->cap_body, &h);
+  launch_iteration(s, false, 1, dt, record_base, sub, s->cap_body, &h);
+  cudaGraph_t out = nullptr;
+  XPBD_CUDA(cudaStreamEndCapture(s->cap_body, &out));
+  return XPBD_OK;
+}
+
+int launch_iterations(Solver* s, int K, float dt, int record_base, cudaStream_t st) {
+  const int sub = record_base >= 0 && K > 0 ? record_base / K : -1;
+  if (stop_mode(s->prm) && s->capturing && !s->profiling && K > 2)
+    return capture_stop_loop(s, dt, record_base, sub, st);
+  for (int it = 0; it < K; ++it) launch_iteration(s, it == 0, it & 1, dt, record_base, sub, st, nullptr);
+  return XPBD_OK;
 }
 
 int do_solve_step(Solver* s, float dt, int record_base, cudaStream_t st) {
@@ -1408,8 +1550,7 @@ int do_solve_step(Solver* s, float dt, int record_base, cudaStream_t st) {
   if (record_base >= 0 && record_base + K > s->max_records)
     return fail(XPBD_ERR_HISTORY_FULL, "history holds " + std::to_string(s->max_records) + " records");
   launch_begin(s, false, true, dt, st);
-  launch_iterations(s, K, dt, record_base, st);
-  return XPBD_OK;
+  return launch_iterations(s, K, dt, record_base, st);
 }
 
 int do_substep(Solver* s, float dt, int record_base, cudaStream_t st) {
@@ -1418,7 +1559,8 @@ int do_substep(Solver* s, float dt, int record_base, cudaStream_t st) {
     return fail(XPBD_ERR_HISTORY_FULL, "history holds " + std::to_string(s->max_records) + " records");
   s->cur = 0;
   launch_begin(s, true, true, dt, st);
-  launch_iterations(s, K, dt, record_base, st);
+  int r = launch_iterations(s, K, dt, record_base, st);
+  if (r != XPBD_OK) return r;
   {
     Prof prof(s, XPBD_K_END, st);
     k_end<<<blocks_for(s->d.V), kBlock, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
@@ -1619,6 +1761,7 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
     if (d.st) cudaFree(d.st);
     if (d.hist) cudaFree(d.hist);
     if (s->cap) cudaStreamDestroy(s->cap);
+    if (s->cap_body) cudaStreamDestroy(s->cap_body);
     delete s;
     return status;
   };
@@ -1630,7 +1773,9 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
   if (e == cudaSuccess) e = cudaMalloc(&d.st, sizeof(DevState));
   if (e == cudaSuccess) e = cudaMalloc(&d.hist, sizeof(double) * 4 * (size_t)(max_records > 0 ? max_records : 1));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_body, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cleanup(fail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
+  d.dyn_end = stop_mode(*params) ? 1 : 0;
   if (has_patch) {
     e = cudaMemcpy(&d.n_pverts, d.voff + d.n_patches, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cleanup(fail(XPBD_ERR_CUDA, std::string("patch offsets: ") + cudaGetErrorString(e)));
@@ -1708,6 +1853,7 @@ int xpbd_destroy(void* handle) {
   if (s->d.st) cudaFree(s->d.st);
   if (s->d.hist) cudaFree(s->d.hist);
   if (s->cap) cudaStreamDestroy(s->cap);
+  if (s->cap_body) cudaStreamDestroy(s->cap_body);
   delete s;
   return XPBD_OK;
 }
@@ -1725,6 +1871,7 @@ int xpbd_set_params(void* handle, const xpbd_params* params) {
     return fail(XPBD_ERR_INVALID_ARGUMENT, "per-tet materials need the ATOMIC or GATHER variant");
   if (std::memcmp(&s->prm, params, sizeof(xpbd_params)) != 0) drop_graph(s);
   s->prm = *params;
+  s->d.dyn_end = stop_mode(*params) ? 1 : 0;
   return XPBD_OK;
 }
 
@@ -1835,6 +1982,22 @@ int xpbd_read_history(void* handle, double* host_out, int32_t n, void* stream) {
   return XPBD_OK;
 }
 
+int xpbd_read_iterations(void* handle, int32_t* host_out, int32_t n, int64_t* total, void* stream) {
+  Solver* s = static_cast<Solver*>(handle);
+  if (!s || (n > 0 && !host_out) || n < 0 || n > kMaxCountedSubsteps)
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "bad iteration-count read (n must be 0.." +
+                                               std::to_string(kMaxCountedSubsteps) + ")");
+  if (n > 0)
+    XPBD_CUDA(cudaMemcpyAsync(host_out, s->d.st->iters, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost,
+                              S(stream)));
+  unsigned long long tot = 0;
+  if (total)
+    XPBD_CUDA(cudaMemcpyAsync(&tot, &s->d.st->total_iters, sizeof(tot), cudaMemcpyDeviceToHost, S(stream)));
+  XPBD_CUDA(cudaStreamSynchronize(S(stream)));
+  if (total) *total = (int64_t)tot;
+  return XPBD_OK;
+}
+
 int xpbd_get_rho_hat(void* handle, double* out, void* stream) {
   Solver* s = static_cast<Solver*>(handle);
   if (!s || !out) return fail(XPBD_ERR_INVALID_ARGUMENT, "bad argument");
@@ -1902,11 +2065,19 @@ int xpbd_read_profile(void* handle, double* ms, int64_t* launches, int32_t n, in
   return XPBD_OK;
 }
 
-static float4* field_ptr(Solver* s, int32_t field) {
+// `known` = false for a valid field whose buffer only the device knows (the
+// predicted positions in stop mode); the kernels then get nullptr.
+static float4* field_ptr(Solver* s, int32_t field, bool& known) {
+  known = true;
   switch (field) {
     case XPBD_FIELD_X: return s->d.x;
     case XPBD_FIELD_V: return s->d.v;
-    case XPBD_FIELD_PRED_X: return s->d.p[s->cur];
+    case XPBD_FIELD_PRED_X:
+      if (s->d.dyn_end) {
+        known = false;
+        return nullptr;
+      }
+      return s->d.p[s->cur];
     default: return nullptr;
   }
 }
@@ -1914,8 +2085,9 @@ static float4* field_ptr(Solver* s, int32_t field) {
 int xpbd_import_vec3(void* handle, int32_t field, const float* src, void* stream) {
   Solver* s = static_cast<Solver*>(handle);
   if (!s || !src) return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or source");
-  float4* f = field_ptr(s, field);
-  if (!f) return fail(XPBD_ERR_INVALID_ARGUMENT, "unknown field");
+  bool known = true;
+  float4* f = field_ptr(s, field, known);
+  if (!f && known) return fail(XPBD_ERR_INVALID_ARGUMENT, "unknown field");
   k_import<<<blocks_for(s->d.V), kBlock, 0, S(stream)>>>(s->d, f, src);
   XPBD_CUDA(cudaGetLastError());
   return XPBD_OK;
@@ -1924,8 +2096,9 @@ int xpbd_import_vec3(void* handle, int32_t field, const float* src, void* stream
 int xpbd_export_vec3(void* handle, int32_t field, float* dst, void* stream) {
   Solver* s = static_cast<Solver*>(handle);
   if (!s || !dst) return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL handle or destination");
-  float4* f = field_ptr(s, field);
-  if (!f) return fail(XPBD_ERR_INVALID_ARGUMENT, "unknown field");
+  bool known = true;
+  float4* f = field_ptr(s, field, known);
+  if (!f && known) return fail(XPBD_ERR_INVALID_ARGUMENT, "unknown field");
   k_export<<<blocks_for(s->d.V), kBlock, 0, S(stream)>>>(s->d, f, dst);
   XPBD_CUDA(cudaGetLastError());
   return XPBD_OK;
@@ -1959,6 +2132,7 @@ int xpbd_check_status(void* handle, void* stream) {
 
 static int check_diff(Solver* s) {
   if (!s->prm.block_mode) return fail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint supports block mode only");
+  if (stop_mode(s->prm)) return fail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint needs a fixed iteration count");
   if (s->prm.scatter == XPBD_SCATTER_PATCH) return fail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint needs ATOMIC or GATHER");
   if (!s->d.tinv_mu) return fail(XPBD_ERR_INVALID_ARGUMENT, "the adjoint needs per-tet materials");
   if (s->prm.constraints_iter > s->max_records)
@@ -1985,7 +2159,7 @@ int xpbd_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* strea
     if (it == 0) XPBD_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
     else
       XPBD_CUDA(cudaMemcpyAsync(tp.lams + (size_t)it * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
-    launch_iteration(s, it, dt, it, st);
+    launch_iteration(s, it == 0, it & 1, dt, 0, -1, st, nullptr);
   }
   XPBD_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
   k_end<<<blocks_for(V), kBlock, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
@@ -2035,7 +2209,10 @@ int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xp
 }
 
 // Per-device address of g_noalloc_scratch, looked up once per device (with
-// that device current) on the first call made on it.
+// that device current) on the first call made on it.  The address belongs to
+// the runtime's primary context of that device: the cache is not refreshed
+// after cudaDeviceReset, and contexts created through the driver API are not
+// supported.
 static std::mutex g_noalloc_mu;
 static double* g_noalloc_ptr[256] = {nullptr};
 
@@ -2049,7 +2226,10 @@ int xpbd_residual_noalloc(const xpbd_body* body, const float* pred_x, float dt, 
                                                std::to_string(body->n_tets));
   if (!body->tets || !body->dm_a || !body->dm_b || !body->dm_c || !body->v0 || !body->lam || !body->dx)
     return fail(XPBD_ERR_INVALID_ARGUMENT, "NULL body buffer");
-  if (!(dt > 0.f) || !(lame_mu != 0.f) || !(lame_lambda != 0.f))
+  if ((body->tet_inv_mu == nullptr) != (body->tet_inv_lambda == nullptr))
+    return fail(XPBD_ERR_INVALID_ARGUMENT, "per-tet materials need both tet_inv_mu and tet_inv_lambda");
+  const bool tet_mat = body->tet_inv_mu != nullptr;
+  if (!(dt > 0.f) || (!tet_mat && (!(lame_mu != 0.f) || !(lame_lambda != 0.f))))
     return fail(XPBD_ERR_INVALID_ARGUMENT, "need dt > 0 and non-zero Lame parameters");
   int dev = 0;
   XPBD_CUDA(cudaGetDevice(&dev));
@@ -2077,9 +2257,13 @@ int xpbd_residual_noalloc(const xpbd_body* body, const float* pred_x, float dt, 
   d.dm_c = body->dm_c;
   d.v0 = body->v0;
   d.lam = reinterpret_cast<float2*>(body->lam);
+  d.tinv_mu = body->tet_inv_mu;
+  d.tinv_la = body->tet_inv_lambda;
+  // the allocating sweeps' compliance factors (compliance_factors): with
+  // per-tet materials 1 / dt^2, scaled per tet by its 1 / mu and 1 / lambda
   const double dt2 = (double)dt * (double)dt;
-  const float cD = (float)(1.0 / ((double)lame_mu * dt2));
-  const float cH = (float)(1.0 / ((double)lame_lambda * dt2));
+  const float cD = tet_mat ? (float)(1.0 / dt2) : (float)(1.0 / ((double)lame_mu * dt2));
+  const float cH = tet_mat ? (float)(1.0 / dt2) : (float)(1.0 / ((double)lame_lambda * dt2));
   cudaStream_t st = S(stream);
   // the ticket must start at zero; a clear, not an allocation
   XPBD_CUDA(cudaMemsetAsync(scratch + kNoAllocTicket, 0, sizeof(unsigned long long), st));

@@ -23,6 +23,7 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
 SOURCES = ["xpbd_solver.cu", "xpbd_batch.cu", "xpbd_mesh.cpp"]
 
+ABI_VERSION = 2  # XPBD_ABI_VERSION of include/xpbd_gb300.h
 XPBD_OK = 0
 STATUS_NAMES = {
     0: "XPBD_OK", 1: "XPBD_ERR_INVALID_ARGUMENT", 2: "XPBD_ERR_CUDA",
@@ -55,7 +56,8 @@ class XpbdParams(ctypes.Structure):
                 ("sweep_order", ctypes.c_int32), ("patch_pipeline", ctypes.c_int32),
                 ("patch_reduce", ctypes.c_int32), ("tets_per_thread", ctypes.c_int32),
                 ("rho_min", ctypes.c_double), ("rho_max", ctypes.c_double),
-                ("rho_beta", ctypes.c_double)]
+                ("rho_beta", ctypes.c_double),
+                ("target_rel_residual", ctypes.c_double), ("residual_floor", ctypes.c_double)]
 
 
 _P = ctypes.c_void_p
@@ -112,6 +114,7 @@ _SIGNATURES = {
     "xpbd_substep": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int32, _P]),
     "xpbd_solve": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_int32, _P]),
     "xpbd_read_history": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.c_int32, _P]),
+    "xpbd_read_iterations": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64), _P]),
     "xpbd_get_rho_hat": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _P]),
     "xpbd_set_rho_hat": (ctypes.c_int, [_P, ctypes.c_double, _P]),
     "xpbd_import_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
@@ -139,6 +142,7 @@ _SIGNATURES = {
     "xpbd_batch_substep": (ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int32, _P]),
     "xpbd_batch_solve": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_int32, _P]),
     "xpbd_batch_read_history": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P]),
+    "xpbd_batch_read_iterations": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P]),
     "xpbd_batch_get_rho_hat": (ctypes.c_int, [_P, _P, _P]),
     "xpbd_batch_check_status": (ctypes.c_int, [_P, _P]),
     "xpbd_batch_import_vec3": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P]),
@@ -224,7 +228,7 @@ def load():
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        if lib.xpbd_abi_version() != 1:
+        if lib.xpbd_abi_version() != ABI_VERSION:
             raise RuntimeError("libxpbd_gb300.so ABI mismatch")
         _lib = lib
         return lib

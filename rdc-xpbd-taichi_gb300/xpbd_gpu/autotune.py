@@ -165,8 +165,11 @@ def tune_single(solver_cls, ctor_args, warmup=2, reps=5, cache=True, log=None):
     for layout, members in groups.items():
         first = members[0]
         kw = dict(ctor_args)
+        # candidates are timed at the fixed iteration count (stop mode off), so
+        # that every replay does the same work
         kw.update(scatter="gather" if layout[0] == "csr" else "patch", patch_tets=first[1] or 256,
-                  tets_per_thread=first[2], patch_pipeline=first[3], use_graph=True, monitor_convergence=False)
+                  tets_per_thread=first[2], patch_pipeline=first[3], use_graph=True, monitor_convergence=False,
+                  target_rel_residual=0.0, residual_floor=0.0)
         try:
             s = solver_cls(**kw)
         except (RuntimeError, ValueError) as e:
@@ -211,6 +214,9 @@ def tune_batch(batch, warmup=2, reps=5, cache=True, log=None):
             return dict(hit, cached=True)
     snap = batch.snapshot()
     sub_dt = min(float(batch.dt) / max(1, int(batch.substeps_num)), float(batch.frame_dt) or 1.0)
+    # timed at the fixed iteration count (stop mode off): every replay does the same work
+    stop = (batch.target_rel_residual, batch.residual_floor)
+    batch.target_rel_residual = batch.residual_floor = 0.0
     table = []
     for tpt in BATCH_CANDIDATES:
         batch.set_tets_per_thread(tpt)
@@ -219,6 +225,7 @@ def tune_batch(batch, warmup=2, reps=5, cache=True, log=None):
         table.append(row)
         if log:
             log(row)
+    batch.target_rel_residual, batch.residual_floor = stop
     batch.restore(snap)
     best = table[pick([r["ms"] for r in table])]
     out = dict(tets_per_thread=best["tets_per_thread"], ms_per_substep=best["ms"], table=table, key=key)

@@ -51,7 +51,7 @@ class XPBDBatchedSolver:
                  hydrostatic_relaxation=1.2, deviatoric_relaxation=1.2, cheb_enable=True, cheb_warmup=5,
                  cheb_gamma=0.6666, block_neohookean_enable=True, monitor_convergence=False,
                  gravity=(0.0, -9.8, 0.0), precise_hydro=None, use_graph=True, tets_per_thread=2,
-                 autotune_cache=True, pair_tets=True):
+                 autotune_cache=True, pair_tets=True, target_rel_residual=0.0, residual_floor=0.0):
         if isinstance(sdf, (list, tuple)):
             self.sdfs = [s for s in sdf if s is not None]
         else:
@@ -66,6 +66,10 @@ class XPBDBatchedSolver:
         self.bodies = list(bodies)
         self.frame_dt, self.dt, self.substeps_num = frame_dt, dt, substeps_num
         self.constraints_iter = constraints_iter
+        # stop mode: each body ends its substep at r_hat <= target * r_hat_0 or
+        # r_hat <= floor (constraints_iter is then the cap)
+        self.target_rel_residual = float(target_rel_residual)
+        self.residual_floor = float(residual_floor)
         self.hydrostatic_relaxation = hydrostatic_relaxation
         self.deviatoric_relaxation = deviatoric_relaxation
         self.cheb_enable, self.cheb_warmup, self.cheb_gamma = cheb_enable, cheb_warmup, cheb_gamma
@@ -302,7 +306,28 @@ class XPBDBatchedSolver:
         p.use_graph = 1 if self.use_graph else 0
         p.tets_per_thread = self.tets_per_thread
         p.rho_min, p.rho_max, p.rho_beta = self.rho_min, self.rho_max, self.rho_beta
+        p.target_rel_residual = self.target_rel_residual
+        p.residual_floor = self.residual_floor
         return p
+
+    def set_stop(self, target_rel_residual, residual_floor=0.0, constraints_iter=None):
+        """Switch stop mode (0, 0: the fixed iteration count) and optionally the
+        iteration cap between frames; the frame graph is recaptured."""
+        self.target_rel_residual = float(target_rel_residual)
+        self.residual_floor = float(residual_floor)
+        if constraints_iter is not None:
+            if int(constraints_iter) * len(frame_chunks(self.frame_dt, self.dt)) * self.substeps_num > self._max_records:
+                raise ValueError("constraints_iter above the history capacity given at construction")
+            self.constraints_iter = int(constraints_iter)
+        _native.check(self._lib.xpbd_batch_set_params(self._handle, self._params()), batch=True)
+
+    def iterations_per_substep(self, n=None):
+        """(n_bodies, n) Jacobi iterations every body ran in each substep of the last frame."""
+        n = len(frame_chunks(self.frame_dt, self.dt)) * self.substeps_num if n is None else int(n)
+        out = np.zeros((self.n_bodies, n), dtype=np.int32)
+        _native.check(self._lib.xpbd_batch_read_iterations(self._handle, out.ctypes.data, n, self._stream()),
+                      batch=True)
+        return out
 
     def _stream(self):
         return _torch().cuda.current_stream(self._device).cuda_stream

@@ -22,7 +22,12 @@ red.global.add, 'gather' = deterministic vertex->tet CSR), ``precise_hydro``
 ``use_graph``, ``reorder`` (Morton order on the device) and ``pair_tets``
 (face-adjacent tets ordered in pairs with aligned corners, so the
 two-tets-per-thread kernels merge their shared corners without comparing
-vertex ids; on by default).  With
+vertex ids; on by default), and ``target_rel_residual`` / ``residual_floor``
+(stop mode: each substep ends after the first iteration whose r_hat is at most
+``target_rel_residual`` times the substep's first r_hat, or at most
+``residual_floor``, with ``constraints_iter`` as the cap; the reference always
+runs ``constraints_iter`` iterations, :474; ``iterations_per_substep()``
+returns the counts of the last frame).  With
 ``scatter="auto"`` the scatter variant, patch size, tets per thread and
 tile pipeline are measured on this mesh and GPU (``xpbd_gpu.autotune``) and
 the choice is kept in ``autotune_result``.
@@ -63,7 +68,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
                  monitor_convergence=False, *, total_mass=1.0, density=None, gravity=(0.0, -9.8, 0.0),
                  scatter="patch", precise_hydro=None, use_graph=True, reorder=True, sweep_order=1,
                  patch_pipeline=0, patch_reduce=0, tets_per_thread=2, patch_tets=256, tet_young_modulus=None,
-                 tet_poisson_ratio=None, autotune_cache=True, pair_tets=True):
+                 tet_poisson_ratio=None, autotune_cache=True, pair_tets=True, target_rel_residual=0.0,
+                 residual_floor=0.0):
         self.autotune_result = None
         if scatter == "auto":
             from xpbd_gpu import autotune
@@ -74,6 +80,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
             scatter, patch_tets = r["scatter"], r["patch_tets"]
             tets_per_thread, patch_pipeline = r["tets_per_thread"], r["patch_pipeline"]
         self.constraints_iter = constraints_iter
+        self.target_rel_residual = float(target_rel_residual)
+        self.residual_floor = float(residual_floor)
         self.hydrostatic_relaxation = hydrostatic_relaxation
         self.deviatoric_relaxation = deviatoric_relaxation
         self.young_modulus = young_modulus
@@ -97,7 +105,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         self._timing_events = []
         self._time_done = 0.0
         self.solve_compute_calls = 0
-        self.solve_compute_iterations = 0
+        self._iterations_fixed = 0
+        self._iterations_device_base = 0
         if scatter not in _native.SCATTERS:
             raise ValueError("scatter must be one of %s" % sorted(_native.SCATTERS))
         self.scatter = scatter
@@ -192,7 +201,47 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         p.patch_reduce = self.patch_reduce
         p.tets_per_thread = self.tets_per_thread
         p.rho_min, p.rho_max, p.rho_beta = self.rho_min, self.rho_max, self.rho_beta
+        p.target_rel_residual = self.target_rel_residual
+        p.residual_floor = self.residual_floor
         return p
+
+    @property
+    def stop_mode(self):
+        return self.target_rel_residual > 0.0 or self.residual_floor > 0.0
+
+    # -- iteration counts (neohookean_solver.py:71-73) -----------------------------
+    def _device_iterations(self):
+        total = _native.ctypes.c_int64(0)
+        _native.check(self._lib.xpbd_read_iterations(self._handle, None, 0, _native.ctypes.byref(total),
+                                                     self._stream()))
+        return int(total.value)
+
+    @property
+    def solve_compute_iterations(self):
+        """Jacobi iterations run so far (reference attribute, :73); in stop mode
+        the device's count of the iterations that actually ran (synchronises)."""
+        if getattr(self, "_handle", None) is not None and self.stop_mode:
+            return self._iterations_fixed + self._device_iterations() - self._iterations_device_base
+        return self._iterations_fixed
+
+    @solve_compute_iterations.setter
+    def solve_compute_iterations(self, value):
+        self._iterations_fixed = int(value)
+        if getattr(self, "_handle", None) is not None:
+            self._iterations_device_base = self._device_iterations()
+
+    def _count_iterations(self, n):
+        if not self.stop_mode:
+            self._iterations_fixed += n
+
+    def iterations_per_substep(self, n=None):
+        """Jacobi iterations each substep of the last frame ran (constraints_iter
+        in the reference's fixed mode; in stop mode up to it)."""
+        n = len(frame_chunks(self.frame_dt, self.dt)) * self.substeps_num if n is None else int(n)
+        out = np.zeros(n, dtype=np.int32)
+        if n:
+            _native.check(self._lib.xpbd_read_iterations(self._handle, out.ctypes.data, n, None, self._stream()))
+        return out
 
     def _sync(self):
         super()._sync()
@@ -280,8 +329,8 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         """Raise if a residual reduction produced NaN/Inf (sticky device flag)."""
         _native.check(self._lib.xpbd_check_status(self._handle, self._stream()))
 
-    def _records_to_history(self, rows):
-        K = self.constraints_iter
+    def _records_to_history(self, rows, K=None):
+        K = self.constraints_iter if K is None else K
         for it in range(K):
             rec = dict(frame=self.current_frame, substep=self.current_substep, iter=it,
                        iter_compute_time_sec=0.0, hydro_error=float(rows[it, 2]),
@@ -300,16 +349,17 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
         b.record()
         self._timing_events.append((a, b))
         self.solve_compute_calls += 1
-        self.solve_compute_iterations += self.constraints_iter
+        self._count_iterations(self.constraints_iter)
+        n_it = int(self.iterations_per_substep(1)[0]) if self.stop_mode else self.constraints_iter
         if self.monitor_convergence:
             rows = self.read_history(self.constraints_iter)
-            t_it = a.elapsed_time(b) * 1e-3 / max(1, self.constraints_iter)
+            t_it = a.elapsed_time(b) * 1e-3 / max(1, n_it)
             start = len(self.convergence_history)
-            self._records_to_history(rows)
+            self._records_to_history(rows, n_it)
             for r in self.convergence_history[start:]:
                 r["iter_compute_time_sec"] = t_it
-        if self.cheb_enable and self.constraints_iter > 0:
-            self.prev_r_hat = float(self.read_history(self.constraints_iter)[-1, 0])
+        if self.cheb_enable and n_it > 0:
+            self.prev_r_hat = float(self.read_history(self.constraints_iter)[n_it - 1, 0])
 
     def solve(self):
         """neohookean_solver.py:562-587: one frame."""
@@ -325,7 +375,7 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
             self._timing_events.append((a, b))
             chunks = frame_chunks(self.frame_dt, self.dt)
             self.solve_compute_calls += len(chunks) * self.substeps_num
-            self.solve_compute_iterations += len(chunks) * self.substeps_num * self.constraints_iter
+            self._count_iterations(len(chunks) * self.substeps_num * self.constraints_iter)
             self.time += sum(chunks)
             if chunks:
                 self.current_substep = self.substeps_num - 1
@@ -342,10 +392,11 @@ class XPBDNeoHookeanSolver(XPBDSolverBase):
                 b.record()
                 self._timing_events.append((a, b))
                 self.solve_compute_calls += 1
-                self.solve_compute_iterations += self.constraints_iter
+                self._count_iterations(self.constraints_iter)
+                n_it = int(self.iterations_per_substep(1)[0]) if self.stop_mode else self.constraints_iter
                 rows = self.read_history(self.constraints_iter)
-                t_it = a.elapsed_time(b) * 1e-3 / max(1, self.constraints_iter)
-                self._records_to_history(rows)
+                t_it = a.elapsed_time(b) * 1e-3 / max(1, n_it)
+                self._records_to_history(rows, n_it)
                 for r in self.current_substep_convergence:
                     r["iter_compute_time_sec"] = t_it
                 if self.convergence_callback:

@@ -1,0 +1,37 @@
+"""Host-side helpers of bench.py that need no GPU: the launch count of a
+stop-mode frame and the 256-body workload's shape."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def test_stop_mode_launch_count():
+    import bench
+    # begin + end, three kernels per iteration; after iterations 0 and 1 the
+    # frame graph's WHILE node launches iterations two at a time
+    assert bench.loop_launches(1) == 2 + 3
+    assert bench.loop_launches(2) == 2 + 6
+    assert bench.loop_launches(3) == 2 + 12
+    assert bench.loop_launches(4) == 2 + 12
+    assert bench.loop_launches(5) == 2 + 18
+    assert bench.loop_launches(200) == 2 + 600
+
+
+def test_c3_workload_shape():
+    import bench
+    bodies, specs, kw, desc = bench.workload_c3()
+    assert len(bodies) == 256
+    assert kw["substeps_num"] == 5 and kw["constraints_iter"] == 30
+    # per-axis cells U{4..32}: between 384 and 196,608 tets per body
+    nt = np.array([b.rest_pose.n_tets for b in bodies])
+    assert nt.min() >= 6 * 4 ** 3 and nt.max() <= 6 * 32 ** 3
+    E = np.array([b.young_modulus for b in bodies])
+    nu = np.array([b.poisson_ratio for b in bodies])
+    assert E.min() >= 1e4 and E.max() <= 1e7
+    assert nu.min() >= 0.30 and nu.max() <= 0.495
+    assert sum(1 for k, _ in specs if k == "sphere") == 32

@@ -28,7 +28,25 @@ def test_header_declares_bound_functions():
 def test_library_exports_every_declared_symbol(native_lib):
     for name in declared_functions():
         assert hasattr(native_lib, name), name
-    assert native_lib.xpbd_abi_version() == 1
+    assert native_lib.xpbd_abi_version() == _native.ABI_VERSION
+    m = re.search(r"#define XPBD_ABI_VERSION (\d+)", open(HEADER).read())
+    assert int(m.group(1)) == _native.ABI_VERSION
+
+
+def test_stop_mode_parameters_are_checked(native_lib):
+    prm = _native.XpbdParams()
+    prm.lame_mu = prm.lame_lambda = 1.0
+    body = _native.XpbdBody()
+    sdf = (_native.XpbdSdf * 1)()
+    h = ctypes.c_void_p()
+    prm.target_rel_residual = -1e-3
+    assert native_lib.xpbd_create(prm, body, sdf, 1, 1, ctypes.byref(h)) == 1
+    assert b"target_rel_residual" in native_lib.xpbd_last_error()
+    prm.target_rel_residual = 1e-3
+    prm.residual_floor = float("nan")
+    assert native_lib.xpbd_create(prm, body, sdf, 1, 1, ctypes.byref(h)) == 1
+    prm.residual_floor = 0.0
+    assert native_lib.xpbd_create(prm, body, sdf, 1, 1, ctypes.byref(h)) == 5  # valid stop mode, empty mesh
 
 
 def test_status_strings(native_lib):

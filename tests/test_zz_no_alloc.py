@@ -25,17 +25,22 @@ pytestmark = pytest.mark.gpu
 RTOL, ATOL = 2e-3, 1e-6
 
 
-def _state():
+def _state(scatter="atomic", tet_materials=False):
     import torch
     from xpbd_gpu.mesh import kuhn_grid
     from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
     from xpbd_gpu.sdf import PlaneSdf, SphereSdf
     m = kuhn_grid(8, 6, 7, 0.05, origin=(0.1, 0.02, 0.1), jitter=0.1, seed=11)
+    extra = {}
+    if tet_materials:  # per-tet Young's moduli spread over two decades
+        extra["tet_young_modulus"] = np.exp(np.random.default_rng(5).uniform(np.log(2e4), np.log(2e6), m.n_tets))
     s = XPBDNeoHookeanSolver(m, [PlaneSdf([0, 0, 0], [0, 1, 0], True), SphereSdf([0.3, 0.0, 0.3], 0.1, True)],
                              young_modulus=2e5, poisson_ratio=0.45, frame_dt=0.01, dt=0.01, substeps_num=1,
                              constraints_iter=1, cheb_enable=True, cheb_warmup=5, cheb_gamma=1.0,
-                             block_neohookean_enable=True, monitor_convergence=True, scatter="atomic",
-                             total_mass=10.0)
+                             block_neohookean_enable=True, monitor_convergence=True, scatter=scatter,
+                             total_mass=10.0, **extra)
+    assert s.scatter == scatter
+    assert (s._tinv_mu is not None) == tet_materials
     # deform the body so the residual is well above round-off
     x = s.mesh.verts.x.to_numpy()
     s.mesh.verts.x.from_numpy(x * np.array([1.0, 0.9, 1.05], dtype=np.float32))
@@ -49,10 +54,13 @@ def _state():
     return s, row, pred
 
 
-def test_noalloc_residual_matches_allocating_path():
+@pytest.mark.parametrize("scatter,tet_materials", [("atomic", False), ("patch", False), ("atomic", True)])
+def test_noalloc_residual_matches_allocating_path(scatter, tet_materials):
+    """The entry point reads the per-tet records every scatter variant shares, and
+    with per-tet materials the compliance of each tet from its own 1 / mu, 1 / lambda."""
     import torch
     from xpbd_gpu import _native
-    s, row, pred = _state()
+    s, row, pred = _state(scatter, tet_materials)
     lib = _native.load()
     body = s._body()
     out = torch.full((3,), -1.0, dtype=torch.float64, device=pred.device)
