@@ -415,12 +415,14 @@ def load_plain_state(plain, batch, state):
         s.rho_hat = float(state["rho"][k])
 
 
-def loop_launches(n):
+def loop_launches(n, per_iteration=4):
     """Kernel launches of one stop-mode substep whose longest body ran n
-    iterations: begin + end + 3 per iteration; past the first two iterations
-    the frame graph's WHILE node runs pairs of iterations."""
+    iterations: begin + end + `per_iteration` per iteration (the batch:
+    projection, residual, update and the next iteration's patch list); past
+    the first two iterations the frame graph's WHILE node runs pairs of
+    iterations."""
     it = n if n <= 2 else 2 + 2 * ((n - 1) // 2)
-    return 2 + 3 * it
+    return 2 + per_iteration * it
 
 
 def run_frames(step, n, flush, stream, after=None):

@@ -43,10 +43,18 @@ struct Flags {
 
 // Iteration control: it[k & 1] = k while iteration k runs (written by the
 // previous iteration's update); n_active = bodies still iterating (stop mode).
+// Stop mode: iteration k's tet sweeps cover the patches listed in
+// act_patch[k & 1][0 .. n_act_patches[k & 1]), the patches of the bodies
+// still iterating in body order, and its update covers the vertex blocks in
+// act_vblock[k & 1].  kb_begin lists everything for iteration 0; kb_list,
+// which runs beside the update of iteration k, lists iteration k + 1's into
+// the other parity, so the sweeps are spread over the work that remains.
 struct Ctl {
   int it[2];
   int n_active;
   int pad;
+  int n_act_patches[2];
+  int n_act_vblocks[2];
 };
 
 // Substeps of one frame whose per-body iteration counts are kept.
@@ -82,21 +90,19 @@ struct BDev {
   double* hist;  // [n_bodies][max_records][4]
   int max_records;
   Ctl* ctl;
+  int* act_patch[2];      // [n_patches] patches of the iteration's sweeps, by parity (Ctl)
+  int* act_vblock[2];     // [V / 256] vertex blocks of the iteration's update, by parity
+  int* act_off;           // [n_bodies][2] a listed body's first patch / vertex-block position (-1: not listed)
+  const int* body_first;  // [n_bodies] first patch of every body
+  const int* body_vfirst; // [n_bodies] first 256-vertex block of every body
+  const int* body_vblocks; // [n_bodies] vertex blocks of every body
   int* iters;    // [n_bodies][kMaxCountedSubsteps] iterations run per substep
   // stop mode: parity of the launched iteration (its index & 1), whose index
   // the kernels read from ctl->it[stop_par]; -1 = fixed iteration count
   int stop_par;
 };
 
-// Stop mode: body b does not run the launched iteration.
-__device__ __forceinline__ bool body_stopped(const BDev& d, int b, int k) { return k >= d.bs[b].stop_at; }
-
-__device__ __forceinline__ int launched_iteration(const BDev& d) {
-  return d.stop_par >= 0 ? *reinterpret_cast<const volatile int*>(&d.ctl->it[d.stop_par]) : 0;
-}
-
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
-
 
 __device__ __forceinline__ float3 post_position(const float4 p, const float4 D) {
   float3 r = make_float3(p.x, p.y, p.z);
@@ -106,6 +112,69 @@ __device__ __forceinline__ float3 post_position(const float4 p, const float4 D) 
     r.z += D.z / D.w;
   }
   return r;
+}
+
+// Stop mode, beside the update of iteration k (parity par): the patches and
+// vertex blocks of the bodies that run iteration k + 1 (their stop_at lies
+// beyond it), into the lists of parity par ^ 1; one CTA.  A block scan over
+// the bodies in order gives each listed body its first positions; then every
+// warp writes the patch and vertex-block ids of some of the bodies.
+__global__ void __launch_bounds__(1024) kb_list(BDev d, int par) {
+  __shared__ int s_wp[32], s_wv[32];
+  __shared__ int s_bp, s_bv;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int next = *reinterpret_cast<const volatile int*>(&d.ctl->it[par]) + 1;
+  const int q = par ^ 1;
+  if (tid == 0) s_bp = s_bv = 0;
+  __syncthreads();
+  for (int b0 = 0; b0 < d.n_bodies; b0 += blockDim.x) {
+    const int b = b0 + tid;
+    const bool act = b < d.n_bodies && next < d.bs[b].stop_at;
+    const int np = act ? __ldg(d.body_patches + b) : 0, nv = act ? __ldg(d.body_vblocks + b) : 0;
+    int cp = np, cv = nv;  // inclusive warp scans
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int tp = __shfl_up_sync(0xffffffffu, cp, o), tv = __shfl_up_sync(0xffffffffu, cv, o);
+      if (lane >= o) {
+        cp += tp;
+        cv += tv;
+      }
+    }
+    if (lane == 31) {
+      s_wp[warp] = cp;
+      s_wv[warp] = cv;
+    }
+    __syncthreads();
+    int op = s_bp, ov = s_bv;
+    for (int w = 0; w < warp; ++w) {
+      op += s_wp[w];
+      ov += s_wv[w];
+    }
+    if (b < d.n_bodies) {
+      d.act_off[2 * b] = act ? op + cp - np : -1;
+      d.act_off[2 * b + 1] = ov + cv - nv;
+    }
+    __syncthreads();
+    if (tid == 0)
+      for (int w = 0; w < nw; ++w) {
+        s_bp += s_wp[w];
+        s_bv += s_wv[w];
+      }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    d.ctl->n_act_patches[q] = s_bp;
+    d.ctl->n_act_vblocks[q] = s_bv;
+  }
+  for (int b = warp; b < d.n_bodies; b += nw) {
+    const int op = d.act_off[2 * b];
+    if (op < 0) continue;
+    const int ov = d.act_off[2 * b + 1];
+    const int fp = __ldg(d.body_first + b), np = __ldg(d.body_patches + b);
+    const int fv = __ldg(d.body_vfirst + b), nv = __ldg(d.body_vblocks + b);
+    for (int i = lane; i < np; i += 32) d.act_patch[q][op + i] = fp + i;
+    for (int i = lane; i < nv; i += 32) d.act_vblock[q][ov + i] = fv + i;
+  }
 }
 
 // Begin of a substep for every body: per-body reset of prev_r_hat / omega
@@ -122,7 +191,13 @@ __global__ void __launch_bounds__(256) kb_begin(BDev d, float dt, float gx, floa
     if (threadIdx.x == 0) {
       d.ctl->it[0] = 0;
       d.ctl->n_active = d.n_bodies;
+      d.ctl->n_act_patches[0] = d.n_patches;
+      d.ctl->n_act_vblocks[0] = d.V >> 8;
     }
+  }
+  if (d.stop_par >= 0) {  // stop mode: iteration 0 lists every patch and vertex block
+    for (int q = i; q < d.n_patches; q += gridDim.x * blockDim.x) d.act_patch[0][q] = q;
+    if (i < (d.V >> 8)) d.act_vblock[0][i] = i;
   }
   if (i >= d.V) return;
   const float4 xi = d.x[i];
@@ -170,9 +245,12 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_projec
   constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
   __shared__ int sg[256];
-  const int p = blockIdx.x;
+  int p = blockIdx.x;
+  if (d.stop_par >= 0) {  // stop mode: CTA q takes listed patch q
+    if (p >= __ldg(&d.ctl->n_act_patches[d.stop_par])) return;
+    p = __ldg(d.act_patch[d.stop_par] + p);
+  }
   const int b = __ldg(d.patch_body + p);
-  if (d.stop_par >= 0 && body_stopped(d, b, launched_iteration(d))) return;
   const int vb = __ldg(d.voff + p);
   const int nv = __ldg(d.voff + p + 1) - vb;
   const int nt = __ldg(d.patch_ntets + p);
@@ -320,22 +398,32 @@ __device__ __forceinline__ void flush_body(const BDev& d, const BSweep& a, int i
 
 // Residual (neohookean_solver.py:298-329) and monitoring sums (:256-296).
 // Each CTA walks a contiguous run of `chunk` patches (patches are ordered by
-// body) and flushes its partial sums whenever the body changes.
+// body) and flushes its partial sums whenever the body changes.  In stop mode
+// the run is taken from the sweep's body list (Ctl), split evenly over the
+// grid, so the CTAs share the patches of the bodies still iterating.
 template <bool kRes, bool kMon, bool kPrecise, int kTPT, bool kTetMat>
 __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int chunk) {
   constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
   __shared__ double red[3][kThreads / 32];
+  int n_items = d.n_patches;
+  if (a.stop) {
+    n_items = __ldg(&d.ctl->n_act_patches[a.par]);
+    chunk = (n_items + gridDim.x - 1) / gridDim.x;
+  }
   const int c0 = blockIdx.x * chunk;
-  const int c1 = c0 + chunk < d.n_patches ? c0 + chunk : d.n_patches;
+  const int c1 = c0 + chunk < n_items ? c0 + chunk : n_items;
   const float4* P = d.p[a.cur];
   const int l0 = kTPT * threadIdx.x;
   const int it = *reinterpret_cast<const volatile int*>(&d.ctl->it[a.par]);
   float sr = 0.f, sh = 0.f, sd = 0.f;
   int run = 0;
-  for (int p = c0; p < c1; ++p) {
+  // stop mode: sweep position q is listed patch act_patch[q]
+  const int* list = d.act_patch[a.par];
+  int p = a.stop && c0 < c1 ? __ldg(list + c0) : c0;
+  for (int q = c0; q < c1; ++q) {
+    const int pn = q + 1 < c1 ? (a.stop ? __ldg(list + q + 1) : q + 1) : -1;
     const int b = __ldg(d.patch_body + p);
-    if (a.stop && body_stopped(d, b, it)) continue;  // the whole body is skipped: no flush
     const int vb = __ldg(d.voff + p);
     const int nv = __ldg(d.voff + p + 1) - vb;
     const int nt = __ldg(d.patch_ntets + p);
@@ -395,11 +483,12 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
       }
     }
     ++run;
-    if (p + 1 == c1 || __ldg(d.patch_body + p + 1) != b) {
+    if (pn < 0 || __ldg(d.patch_body + pn) != b) {
       flush_body<kRes, kMon, kThreads / 32>(d, a, it, b, run, sr, sh, sd, red);
       sr = sh = sd = 0.f;
       run = 0;
     }
+    p = pn;
   }
 }
 
@@ -421,38 +510,44 @@ struct BUpd {
 template <bool kCheb, bool kFirstIt>
 __global__ void __launch_bounds__(256) kb_update(BDev d, int cur, float gamma, BUpd u) {
   const int vb0 = blockIdx.x * kBUpdateBlocks;
-  const int it = (u.stop || blockIdx.x == 0) ? *reinterpret_cast<const volatile int*>(&d.ctl->it[u.par]) : 0;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    d.ctl->it[u.par ^ 1] = it + 1;
-    if (u.use_cond) {
-      const bool more = it + 1 < u.K && *reinterpret_cast<const volatile int*>(&d.ctl->n_active) > 0;
-      cudaGraphSetConditional(u.cond, more ? 1u : 0u);
+  if (blockIdx.x == 0) {
+    const int it = *reinterpret_cast<const volatile int*>(&d.ctl->it[u.par]);
+    if (threadIdx.x == 0) {
+      d.ctl->it[u.par ^ 1] = it + 1;
+      if (u.use_cond) {
+        const bool more = it + 1 < u.K && *reinterpret_cast<const volatile int*>(&d.ctl->n_active) > 0;
+        cudaGraphSetConditional(u.cond, more ? 1u : 0u);
+      }
     }
   }
   // every load is issued before the first store: as far as the compiler
   // knows the buffers may alias, so a load after a store would wait for it
   float4 pc[kBUpdateBlocks], D[kBUpdateBlocks], yp[kBUpdateBlocks];
   float om[kBUpdateBlocks];
-  bool run[kBUpdateBlocks];
+  int vi[kBUpdateBlocks];  // the thread's vertex in each of its blocks, -1: none
+  // stop mode: the CTA's blocks are entries of the iteration's vertex-block list
+  const int nlist = u.stop ? __ldg(&d.ctl->n_act_vblocks[u.par]) : 0;
 #pragma unroll
   for (int k = 0; k < kBUpdateBlocks; ++k) {
-    const int i = (vb0 + k) * 256 + threadIdx.x;
+    int vb = vb0 + k;
+    if (u.stop) vb = vb < nlist ? __ldg(d.act_vblock[u.par] + vb) : -1;
+    const int i = vb * 256 + threadIdx.x;
+    vi[k] = vb >= 0 && i < d.V ? i : -1;
     om[k] = 1.f;
-    run[k] = i < d.V && !(u.stop && body_stopped(d, __ldg(d.vblock_body + vb0 + k), it));
-    if (run[k]) {
+    if (vi[k] >= 0) {
       pc[k] = d.p[cur][i];
       D[k] = d.dx[i];
       yp[k] = pc[k];
       if (kCheb) {
         if (!kFirstIt) yp[k] = d.p[cur ^ 1][i];
-        om[k] = (float)d.bs[__ldg(d.vblock_body + vb0 + k)].omega;
+        om[k] = (float)d.bs[__ldg(d.vblock_body + vb)].omega;
       }
     }
   }
 #pragma unroll
   for (int k = 0; k < kBUpdateBlocks; ++k) {
-    const int i = (vb0 + k) * 256 + threadIdx.x;
-    if (!run[k]) continue;
+    const int i = vi[k];
+    if (i < 0) continue;
     d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 xp = post_position(pc[k], D[k]);
     if (kCheb) {
@@ -496,6 +591,9 @@ __global__ void kb_validate(BDev d, int n_out) {
   if (t < d.n_patches) {
     const int a = d.voff[t], e = d.voff[t + 1], b = d.patch_body[t], nt = d.patch_ntets[t];
     if (a < 0 || e < a || e > d.n_pverts || e - a > 256 || b < 0 || b >= d.n_bodies || nt < 0 || nt > kP)
+      d.flags->bad_mesh = 1;
+    // a body's patches are consecutive, from body_first[b] on
+    else if (t < d.body_first[b] || t >= d.body_first[b] + d.body_patches[b])
       d.flags->bad_mesh = 1;
     for (int q = 0; q < nt && !d.flags->bad_mesh; ++q) {
       const uint32_t l = d.lid[t * kP + q];
@@ -650,6 +748,10 @@ struct Batch {
   bool capturing = false;
   cudaStream_t cap = nullptr;
   cudaStream_t cap_body = nullptr;  // captures the body of a stop-mode loop node
+  cudaStream_t aux = nullptr;       // stop mode: kb_list beside the update
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t aux_body = nullptr;  // the same inside the body of a loop node
+  cudaEvent_t ev_fork_body = nullptr, ev_join_body = nullptr;
   cudaGraphExec_t exec = nullptr;
   double key_frame_dt = -1, key_dt = -1;
   int key_sub = -1;
@@ -740,11 +842,19 @@ void residual_b(Batch* s, const BSweep& a, cudaStream_t st) {
 
 inline bool stop_mode_b(const xpbd_params& p) { return p.target_rel_residual > 0.0 || p.residual_floor > 0.0; }
 
+// Second stream and events on which stop mode runs kb_list beside the update.
+// A stream that joins a capture belongs to it until that capture ends, so the
+// body of a loop node (captured while the frame's capture is open) has its own.
+struct Fork {
+  cudaStream_t aux;
+  cudaEvent_t fork, join;
+};
+
 // One Jacobi iteration of every body.  `first`: iteration 0 (lambda reset);
 // `par`: the iteration's index & 1 (the index itself is on the device);
 // `cond`: the loop condition of a stop-mode frame graph (nullptr: none).
-void iteration_b(Batch* s, bool first, int par, float dt, int rec_base, cudaStream_t st,
-                 const cudaGraphConditionalHandle* cond) {
+int iteration_b(Batch* s, bool first, int par, float dt, int rec_base, cudaStream_t st,
+                const cudaGraphConditionalHandle* cond, const Fork& fk) {
   const xpbd_params& p = s->prm;
   const bool stop = stop_mode_b(p);
   const float inv_dt2 = (float)(1.0 / ((double)dt * (double)dt));
@@ -775,6 +885,13 @@ void iteration_b(Batch* s, bool first, int par, float dt, int rec_base, cudaStre
     else if (cheb || stop) residual_b<true, false>(s, a, st);
     else residual_b<false, true>(s, a, st);
   }
+  if (stop) {
+    // the next iteration's lists, beside the update (both follow the residual)
+    B_CUDA(cudaEventRecord(fk.fork, st));
+    B_CUDA(cudaStreamWaitEvent(fk.aux, fk.fork, 0));
+    kb_list<<<1, 1024, 0, fk.aux>>>(s->d, par);
+    B_CUDA(cudaEventRecord(fk.join, fk.aux));
+  }
   BProf pr(s, XPBD_K_UPDATE, st);
   const int g = (nblk(s->d.V) + kBUpdateBlocks - 1) / kBUpdateBlocks;
   BUpd u{};
@@ -791,6 +908,8 @@ void iteration_b(Batch* s, bool first, int par, float dt, int rec_base, cudaStre
     kb_update<false, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
   }
   s->d.stop_par = -1;
+  if (stop) B_CUDA(cudaStreamWaitEvent(st, fk.join, 0));
+  return XPBD_OK;
 }
 
 // Stop mode under capture: iterations 0 and 1 as plain nodes, then a WHILE
@@ -803,8 +922,10 @@ int capture_stop_loop_b(Batch* s, float dt, int rec_base, cudaStream_t st) {
   if (cs != cudaStreamCaptureStatusActive || !g) return bfail(XPBD_ERR_CUDA, "stop-mode loop outside a capture");
   cudaGraphConditionalHandle h = 0;
   B_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
-  iteration_b(s, true, 0, dt, rec_base, st, nullptr);
-  iteration_b(s, false, 1, dt, rec_base, st, &h);
+  const Fork fk{s->aux, s->ev_fork, s->ev_join}, fkb{s->aux_body, s->ev_fork_body, s->ev_join_body};
+  int r = iteration_b(s, true, 0, dt, rec_base, st, nullptr, fk);
+  if (!r) r = iteration_b(s, false, 1, dt, rec_base, st, &h, fk);
+  if (r) return r;
   const cudaGraphNode_t* deps = nullptr;
   const cudaGraphEdgeData* edges = nullptr;
   size_t nd = 0;
@@ -819,10 +940,12 @@ int capture_stop_loop_b(Batch* s, float dt, int rec_base, cudaStream_t st) {
   cudaGraph_t body = np.conditional.phGraph_out[0];
   B_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
   B_CUDA(cudaStreamBeginCaptureToGraph(s->cap_body, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  iteration_b(s, false, 0, dt, rec_base, s->cap_body, &h);
-  iteration_b(s, false, 1, dt, rec_base, s->cap_body, &h);
+  r = iteration_b(s, false, 0, dt, rec_base, s->cap_body, &h, fkb);
+  if (!r) r = iteration_b(s, false, 1, dt, rec_base, s->cap_body, &h, fkb);
   cudaGraph_t out = nullptr;
-  B_CUDA(cudaStreamEndCapture(s->cap_body, &out));
+  const cudaError_t e = cudaStreamEndCapture(s->cap_body, &out);
+  if (r) return r;
+  B_CUDA(e);
   return XPBD_OK;
 }
 
@@ -833,13 +956,19 @@ int substep_b(Batch* s, float dt, int rec_base, cudaStream_t st) {
   s->cur = 0;
   {
     BProf pr(s, XPBD_K_BEGIN, st);
+    s->d.stop_par = stop ? 0 : -1;  // stop mode: kb_begin lists every patch
     kb_begin<<<nblk(s->d.V), 256, 0, st>>>(s->d, dt, s->prm.gravity[0], s->prm.gravity[1], s->prm.gravity[2], K);
+    s->d.stop_par = -1;
   }
   if (stop && s->capturing && K > 2) {
     int r = capture_stop_loop_b(s, dt, rec_base, st);
     if (r) return r;
   } else {
-    for (int it = 0; it < K; ++it) iteration_b(s, it == 0, it & 1, dt, rec_base, st, nullptr);
+    const Fork fk{s->aux, s->ev_fork, s->ev_join};
+    for (int it = 0; it < K; ++it) {
+      const int r = iteration_b(s, it == 0, it & 1, dt, rec_base, st, nullptr, fk);
+      if (r) return r;
+    }
   }
   const int sub = rec_base >= 0 && K > 0 ? rec_base / K : -1;
   BProf pr(s, XPBD_K_END, st);
@@ -943,6 +1072,18 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
     if (d.flags) cudaFree(d.flags);
     if (d.hist) cudaFree(d.hist);
     if (d.ctl) cudaFree(d.ctl);
+    if (d.act_patch[0]) cudaFree(d.act_patch[0]);
+    if (d.act_vblock[0]) cudaFree(d.act_vblock[0]);
+    if (d.act_off) cudaFree(d.act_off);
+    if (d.body_vfirst) cudaFree(const_cast<int*>(d.body_vfirst));
+    if (d.body_vblocks) cudaFree(const_cast<int*>(d.body_vblocks));
+    if (s->aux) cudaStreamDestroy(s->aux);
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_join) cudaEventDestroy(s->ev_join);
+    if (s->aux_body) cudaStreamDestroy(s->aux_body);
+    if (s->ev_fork_body) cudaEventDestroy(s->ev_fork_body);
+    if (s->ev_join_body) cudaEventDestroy(s->ev_join_body);
+    if (d.body_first) cudaFree(const_cast<int*>(d.body_first));
     if (d.iters) cudaFree(d.iters);
     if (s->cap) cudaStreamDestroy(s->cap);
     if (s->cap_body) cudaStreamDestroy(s->cap_body);
@@ -957,6 +1098,28 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
   if (e == cudaSuccess) e = cudaMalloc(&d.flags, sizeof(Flags));
   if (e == cudaSuccess) e = cudaMalloc(&d.hist, sizeof(double) * 4 * (size_t)d.max_records * d.n_bodies);
   if (e == cudaSuccess) e = cudaMalloc(&d.ctl, sizeof(Ctl));
+  const size_t nvb = (size_t)d.V / 256;
+  if (e == cudaSuccess) e = cudaMalloc(&d.act_patch[0], sizeof(int) * 2 * (size_t)d.n_patches);
+  if (e == cudaSuccess) e = cudaMalloc(&d.act_vblock[0], sizeof(int) * 2 * nvb);
+  if (e == cudaSuccess) e = cudaMalloc(&d.act_off, sizeof(int) * 2 * (size_t)d.n_bodies);
+  int *bvfirst = nullptr, *bvblocks = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&bvfirst, sizeof(int) * (size_t)d.n_bodies);
+  d.body_vfirst = bvfirst;
+  if (e == cudaSuccess) e = cudaMalloc(&bvblocks, sizeof(int) * (size_t)d.n_bodies);
+  d.body_vblocks = bvblocks;
+  if (e == cudaSuccess) {
+    d.act_patch[1] = d.act_patch[0] + d.n_patches;
+    d.act_vblock[1] = d.act_vblock[0] + nvb;
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->aux_body, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork_body, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join_body, cudaEventDisableTiming);
+  int* bfirst = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&bfirst, sizeof(int) * (size_t)d.n_bodies);
+  d.body_first = bfirst;
   if (e == cudaSuccess) e = cudaMalloc(&d.iters, sizeof(int) * (size_t)kMaxCountedSubsteps * d.n_bodies);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_body, cudaStreamNonBlocking);
@@ -972,6 +1135,39 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
   if (e == cudaSuccess) e = cudaMemcpy(d.flags, &hf, sizeof(hf), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(d.hist, 0, sizeof(double) * 4 * (size_t)d.max_records * d.n_bodies);
   if (e == cudaSuccess) e = cudaMemset(d.ctl, 0, sizeof(Ctl));
+  {
+    // first patch of every body: the exclusive prefix of the patch counts
+    std::vector<int> np(d.n_bodies), first(d.n_bodies);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(np.data(), body->body_n_patches, sizeof(int) * (size_t)d.n_bodies, cudaMemcpyDeviceToHost);
+    long long acc = 0;
+    for (int b = 0; b < d.n_bodies && e == cudaSuccess; ++b) {
+      first[b] = (int)acc;
+      acc += np[b] > 0 ? np[b] : 0;
+    }
+    if (e == cudaSuccess && acc != d.n_patches)
+      return cleanup(bfail(XPBD_ERR_BAD_MESH, "body_n_patches do not add up to n_patches"));
+    if (e == cudaSuccess) e = cudaMemcpy(bfirst, first.data(), sizeof(int) * (size_t)d.n_bodies, cudaMemcpyHostToDevice);
+    // every body's vertex blocks: a contiguous run of vblock_body
+    std::vector<int> vbody((size_t)d.V / 256), vf(d.n_bodies, -1), vn(d.n_bodies, 0);
+    if (e == cudaSuccess && !vbody.empty())
+      e = cudaMemcpy(vbody.data(), body->vblock_body, sizeof(int) * vbody.size(), cudaMemcpyDeviceToHost);
+    bool contiguous = true;
+    for (size_t k = 0; k < vbody.size() && e == cudaSuccess; ++k) {
+      const int b = vbody[k];
+      if (b < 0 || b >= d.n_bodies) {
+        contiguous = false;
+        break;
+      }
+      if (vn[b] == 0) vf[b] = (int)k;
+      else if (vf[b] + vn[b] != (int)k) contiguous = false;
+      ++vn[b];
+    }
+    if (e == cudaSuccess && !contiguous)
+      return cleanup(bfail(XPBD_ERR_BAD_MESH, "a body's vertex blocks must be consecutive"));
+    if (e == cudaSuccess) e = cudaMemcpy(bvfirst, vf.data(), sizeof(int) * (size_t)d.n_bodies, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(bvblocks, vn.data(), sizeof(int) * (size_t)d.n_bodies, cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess) e = cudaMemset(d.iters, 0, sizeof(int) * (size_t)kMaxCountedSubsteps * d.n_bodies);
   if (e != cudaSuccess) return cleanup(bfail(XPBD_ERR_CUDA, std::string("setup: ") + cudaGetErrorString(e)));
   {
@@ -1015,6 +1211,18 @@ int xpbd_batch_destroy(void* h) {
   cudaFree(s->d.flags);
   cudaFree(s->d.hist);
   cudaFree(s->d.ctl);
+  cudaFree(s->d.act_patch[0]);
+  cudaFree(s->d.act_vblock[0]);
+  cudaFree(s->d.act_off);
+  cudaFree(const_cast<int*>(s->d.body_vfirst));
+  cudaFree(const_cast<int*>(s->d.body_vblocks));
+  if (s->aux) cudaStreamDestroy(s->aux);
+  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+  if (s->ev_join) cudaEventDestroy(s->ev_join);
+  if (s->aux_body) cudaStreamDestroy(s->aux_body);
+  if (s->ev_fork_body) cudaEventDestroy(s->ev_fork_body);
+  if (s->ev_join_body) cudaEventDestroy(s->ev_join_body);
+  cudaFree(const_cast<int*>(s->d.body_first));
   cudaFree(s->d.iters);
   if (s->cap) cudaStreamDestroy(s->cap);
   if (s->cap_body) cudaStreamDestroy(s->cap_body);
@@ -1226,7 +1434,8 @@ int xpbd_batch_substep_tape(void* h, float dt, const xpbd_tape* tape, void* stre
     if (it == 0) B_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
     else
       B_CUDA(cudaMemcpyAsync(tp.lams + (size_t)it * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
-    iteration_b(s, it == 0, it & 1, dt, 0, st, nullptr);
+    const int r = iteration_b(s, it == 0, it & 1, dt, 0, st, nullptr, Fork{s->aux, s->ev_fork, s->ev_join});
+    if (r) return r;
   }
   B_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
   kb_end<<<nblk(V), 256, 0, st>>>(s->d, s->cur, dt, s->prm.damping, 0, 0, -1);

@@ -2,7 +2,7 @@
 
 Usage (only where the reference checkout is present):
 
-    python tests/golden/make_golden.py [--ref PATH] [--out DIR] [--only NAME ...]
+    python tests/golden/make_golden.py --ref PATH [--out DIR] [--only NAME ...]
 
 It imports the reference's ``xpbd_gpu.neohookean_solver`` and ``xpbd_gpu.sdf``
 unmodified (``neohookean_solver.py:16-587``, ``xpbd_base.py:11-204``,
@@ -173,11 +173,14 @@ def run_case(ref, name, spec, precision):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("XPBD_REFERENCE_DIR", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("XPBD_REFERENCE_DIR"),
+                    help="the reference checkout (or set XPBD_REFERENCE_DIR)")
     ap.add_argument("--out", default=HERE)
     ap.add_argument("--only", nargs="*", default=None)
     ap.add_argument("--precision", default="f64", choices=["f64", "f32"])
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref or set XPBD_REFERENCE_DIR")
     for name, spec in cases().items():
         if args.only and name not in args.only:
             continue

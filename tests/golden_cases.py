@@ -9,8 +9,9 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def golden_names():
+    """The solver fixtures of make_golden.py (not the driver trace of make_driver_trace.py)."""
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz"))
-                  if not p.endswith("_f32.npz"))
+                  if not p.endswith("_f32.npz") and not os.path.basename(p).startswith("driver_trace"))
 
 
 def load(name):

@@ -12,14 +12,16 @@ if ROOT not in sys.path:
 
 def test_stop_mode_launch_count():
     import bench
-    # begin + end, three kernels per iteration; after iterations 0 and 1 the
-    # frame graph's WHILE node launches iterations two at a time
-    assert bench.loop_launches(1) == 2 + 3
-    assert bench.loop_launches(2) == 2 + 6
-    assert bench.loop_launches(3) == 2 + 12
-    assert bench.loop_launches(4) == 2 + 12
-    assert bench.loop_launches(5) == 2 + 18
-    assert bench.loop_launches(200) == 2 + 600
+    # begin + end, three kernels per iteration (single body); after iterations
+    # 0 and 1 the frame graph's WHILE node launches iterations two at a time
+    assert bench.loop_launches(1, 3) == 2 + 3
+    assert bench.loop_launches(2, 3) == 2 + 6
+    assert bench.loop_launches(3, 3) == 2 + 12
+    assert bench.loop_launches(4, 3) == 2 + 12
+    assert bench.loop_launches(5, 3) == 2 + 18
+    assert bench.loop_launches(200, 3) == 2 + 600
+    # the batch adds the next iteration's patch list to every iteration
+    assert bench.loop_launches(5) == 2 + 24
 
 
 def test_c3_workload_shape():

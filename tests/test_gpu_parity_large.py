@@ -1,11 +1,21 @@
 """GPU parity at the benchmark's full single-body size (64^3 Kuhn cells,
-1,572,864 tets): one frame from rest against the float64 run of the
-reference algorithm (the C restatement built in FP64), within 1e-4 of the
-bounding-box diagonal and with matching per-iteration residual curves; then,
-in contact with the plane, spheres and box, one more frame started from the
-GPU state, where the GPU may depart from FP64 at most as far as an FP32 run
-of the reference algorithm does (plus 1e-4 of the diagonal), and its
-residual curve at most twice as far (plus 1%, median over the iterations)."""
+1,572,864 tets, nu = 0.49).
+
+* One frame from rest against the float64 run of the reference algorithm
+  (the C restatement built in FP64): within 1e-4 of the bounding-box
+  diagonal, with the residual at the FP32 floor of free fall.
+* One frame in contact with the plane, spheres and box, every run started
+  from the same GPU state, against the reference algorithm in its own
+  arithmetic type (the C restatement in FP32).  Two FP32 runs of the same
+  algorithm that only sum in another order (the tets renumbered) already
+  depart from each other by about 7e-5 of the diagonal in this frame, so
+  the GPU must stay within 1e-4 of the diagonal or within twice that
+  order-only deviation, whichever is larger; its per-iteration residual
+  curve must match the FP32 run's within 1e-2 relative (where r_hat is
+  above 1e-4, well above the FP32 floor).
+* Against FP64 in contact the GPU may depart at most as far as the FP32
+  run of the reference algorithm does, plus 1e-4 of the diagonal.
+"""
 import os
 import sys
 
@@ -38,22 +48,30 @@ def test_c2_size_against_float64_reference():
     for _ in range(10):
         gpu.solve()
     x, v, rho = gpu.mesh.verts.x.to_numpy(), gpu.mesh.verts.v.to_numpy(), gpu.rho_hat
+    from xpbd_gpu.mesh import TetMesh
     f32 = bench.cpu_oracle(mesh, specs, kw, S, threads, dtype=np.float32)
-    for o in (ref, f32):
+    perm = np.random.default_rng(7).permutation(mesh.n_tets)
+    f32p = bench.cpu_oracle(TetMesh(mesh.points, mesh.tets[perm]), specs, kw, S, threads, dtype=np.float32)
+    for o in (ref, f32, f32p):
         o.x[:] = x
         o.v[:] = v
         o.rho_hat.value = rho
-    hist32 = np.zeros(S * K)
+    hist32, hist32p = np.zeros(S * K), np.zeros(S * K)
     gpu.solve()
     ref.solve(1, hist)
     f32.solve(1, hist32)
+    f32p.solve(1, hist32p)
     gpu.check_status()
-    dev_gpu = np.abs(gpu.mesh.verts.x.to_numpy() - ref.x).max()
-    dev_f32 = np.abs(f32.x.astype(np.float64) - ref.x).max()
+    xg = gpu.mesh.verts.x.to_numpy().astype(np.float64)
+    x32, x32p = f32.x.astype(np.float64), f32p.x.astype(np.float64)
+    order_only = np.abs(x32p - x32).max() / diag
+    gpu_vs_f32 = np.abs(xg - x32).max() / diag
+    assert gpu_vs_f32 <= max(1e-4, 2.0 * order_only), (gpu_vs_f32, order_only)
+    dev_gpu = np.abs(xg - ref.x).max()
+    dev_f32 = np.abs(x32 - ref.x).max()
     assert dev_gpu <= dev_f32 + 1e-4 * diag, (dev_gpu / diag, dev_f32 / diag)
     r = gpu.read_history()[:S * K, 0]
-    live = hist > 1e-4  # well above the FP32 floor of a body at rest
+    live = hist32 > 1e-4  # well above the FP32 floor of a body at rest
     assert live.sum() > 0.5 * live.size
-    rel = np.abs(r[live] - hist[live]) / hist[live]
-    rel32 = np.abs(hist32[live] - hist[live]) / hist[live]
-    assert np.median(rel) <= 2.0 * np.median(rel32) + 1e-2, (np.median(rel), np.median(rel32))
+    rel = np.abs(r[live] - hist32[live]) / hist32[live]
+    assert rel.max() <= 1e-2, rel.max()
