@@ -258,15 +258,27 @@ def workload_c5(seed=0, n_bodies=64, h=1.0 / 16, sigma=2.0):
 
 
 def run_c5(args):
-    """Batched differentiable: Adam on every body's per-tet log E through the batched adjoint, against
-    the plain per-body form (one single-body adjoint per body) on a subset of the bodies."""
+    print(json.dumps(c5_block(args, args.c5_adam_steps, plain_accuracy_bodies=args.c5_plain_bodies)), flush=True)
+
+
+def c5_block(args, steps, plain_accuracy_bodies=4, plain_timing_steps=2, fp64_bodies=4):
+    """Batched differentiable: Adam on every body's per-tet log E through the
+    batched adjoint (forward + adjoint per substep, graph-captured), against the
+    plain per-body form (one single-body adjoint per body, also captured):
+    * timing: `steps` Adam steps of the batch; the plain form runs
+      `plain_timing_steps` Adam steps of every one of the 64 bodies;
+    * accuracy: the first `plain_accuracy_bodies` bodies run all `steps` Adam
+      steps in the plain form too, and their recovered fields are compared;
+    * error of the forward against FP64: `fp64_bodies` bodies (spread over the
+      sizes), one frame from the initial state, against the float64 oracle run
+      of each body with its own per-tet materials."""
     import torch
     from xpbd_gpu.batched import Body
     from xpbd_gpu.differentiable import BatchedDiffSim, DiffSim, xpbd_simulate, xpbd_simulate_batch
     torch.cuda.set_device(0)
     dev = torch.device("cuda")
     meshes, log_E_true, nus, specs, kw, desc = workload_c5()
-    frames, steps, lr = args.c5_frames, args.c5_adam_steps, args.c5_lr
+    frames, lr = args.c5_frames, args.c5_lr
     nb = len(meshes)
     T_all = sum(m.n_tets for m in meshes)
     nu_tet = np.concatenate([np.full(m.n_tets, nus[k]) for k, m in enumerate(meshes)])
@@ -281,8 +293,10 @@ def run_c5(args):
     with torch.no_grad():
         x_target = xpbd_simulate_batch(sim, x0, v0, torch.tensor(le_true, device=dev), nu_t, frames).clone()
     vcount = torch.tensor(np.concatenate([np.full(m.n_verts, 1.0 / m.n_verts) for m in meshes]), device=dev)
+    offs = np.concatenate([[0], np.cumsum([m.n_tets for m in meshes])])
+    voffs = np.concatenate([[0], np.cumsum([m.n_verts for m in meshes])])
 
-    def per_body_rel_err(theta, lo, truth, start):
+    def per_body_rel_err(theta, truth, start):
         return float(np.linalg.norm(theta - truth) / max(np.linalg.norm(start - truth), 1e-30))
 
     theta = torch.tensor(le0, dtype=torch.float64, device=dev, requires_grad=True)
@@ -304,15 +318,11 @@ def run_c5(args):
         losses.append(float(loss))
     sim.batch.check_status()
     th = theta.detach().cpu().numpy()
-    offs = np.concatenate([[0], np.cumsum([m.n_tets for m in meshes])])
-    errs = [per_body_rel_err(th[offs[k]:offs[k + 1]], 0, le_true[offs[k]:offs[k + 1]], le0[offs[k]:offs[k + 1]])
+    errs = [per_body_rel_err(th[offs[k]:offs[k + 1]], le_true[offs[k]:offs[k + 1]], le0[offs[k]:offs[k + 1]])
             for k in range(nb)]
     rel_l2 = float(np.linalg.norm(th - le_true) / np.linalg.norm(le_true))
 
-    # plain per-body form on the first bodies: one single-body adjoint per body, same Adam
-    plain = []
-    nplain = min(args.c5_plain_bodies, nb)
-    for k in range(nplain):
+    def plain_body(k, n_steps):
         m = meshes[k]
         ps = DiffSim(m, product_sdfs(specs), np.full(m.n_tets, np.log(1e5)), np.full(m.n_tets, nus[k]),
                      density=1000.0, poisson_ratio=float(nus[k]), **kw)
@@ -324,7 +334,7 @@ def run_c5(args):
         thk = torch.tensor(le0[offs[k]:offs[k + 1]], dtype=torch.float64, device=dev, requires_grad=True)
         optk = torch.optim.Adam([thk], lr=lr)
         ms = []
-        for it in range(steps):
+        for it in range(n_steps):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             optk.zero_grad()
             a.record()
@@ -336,25 +346,35 @@ def run_c5(args):
             b.synchronize()
             ms.append(a.elapsed_time(b))
         ps.solver.check_status()
-        tk = thk.detach().cpu().numpy()
-        plain.append(dict(ms_per_adam_step=float(np.mean(ms[1:] if len(ms) > 1 else ms)),
-                          rel_err=per_body_rel_err(tk, 0, log_E_true[k], le0[offs[k]:offs[k + 1]]),
+        return thk.detach().cpu().numpy(), ms
+
+    # plain form, timing: every body, `plain_timing_steps` Adam steps each (the first
+    # step of a body captures its graphs and is not counted when there are more)
+    plain_ms = []
+    for k in range(nb):
+        _, ms = plain_body(k, plain_timing_steps)
+        plain_ms.append(float(np.mean(ms[1:] if len(ms) > 1 else ms)))
+    # plain form, accuracy: the first bodies through all the Adam steps
+    plain = []
+    for k in range(min(plain_accuracy_bodies, nb)):
+        tk, _ = plain_body(k, steps)
+        plain.append(dict(rel_err=per_body_rel_err(tk, log_E_true[k], le0[offs[k]:offs[k + 1]]),
                           batched_rel_err=errs[k],
                           theta_rel_diff_vs_batched=float(np.linalg.norm(tk - th[offs[k]:offs[k + 1]]) /
                                                           np.linalg.norm(th[offs[k]:offs[k + 1]]))))
+    fp64 = c5_fp64_error(meshes, log_E_true, nus, specs, kw, sim, x0, v0, nu_t, le_true, voffs, fp64_bodies)
     sl = slice(1, None) if steps > 1 else slice(None)
     step_ms = float(np.mean(np.add(fwd_ms, bwd_ms)[sl]))
     units = T_all * frames * kw["substeps_num"] * kw["constraints_iter"]
-    plain_tets = sum(meshes[k].n_tets for k in range(nplain))
-    plain_ms = sum(p["ms_per_adam_step"] for p in plain)
-    plain_value = plain_tets * frames * kw["substeps_num"] * kw["constraints_iter"] / (plain_ms * 1e-3) if plain else None
-    line = {"metric": METRIC, "value": units / (step_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": steps,
+    plain_total_ms = float(np.sum(plain_ms))
+    return {"metric": METRIC, "value": units / (step_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": steps,
             "warmup": 1, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": desc,
                        "step": "one Adam step on all 64 bodies: checkpointed batched forward of %d frames + "
                                "batched adjoint (tet-iterations counted once, forward)" % frames,
-                       "form": "batched (one launch per phase over all bodies)"},
+                       "form": "batched (one launch per phase over all bodies, forward and adjoint each one "
+                               "CUDA graph)"},
             "forward_ms": float(np.mean(np.asarray(fwd_ms)[sl])), "backward_ms": float(np.mean(np.asarray(bwd_ms)[sl])),
             "backward_over_forward": float(np.mean(np.asarray(bwd_ms)[sl]) / np.mean(np.asarray(fwd_ms)[sl])),
             "adam": {"steps": steps, "lr": lr, "init": "log E = log 1e5 everywhere",
@@ -363,20 +383,41 @@ def run_c5(args):
                      "recovered_rel_err_mean": float(np.mean(errs)),
                      "recovered_rel_l2_of_log_E": rel_l2,
                      "rel_err_definition": "|theta - theta*| / |theta_0 - theta*| per body"},
-            "plain": {"form": "one single-body DiffSim per body (ATOMIC scatter), same Adam",
-                      "bodies": nplain, "value": plain_value, "per_body": plain},
-            "batched_over_plain": (plain_value and units / (step_ms * 1e-3) / plain_value)}
-    print(json.dumps(line), flush=True)
+            "plain": {"form": "one single-body DiffSim per body (ATOMIC scatter, per-tet materials), same Adam, "
+                              "forward and adjoint graph-captured",
+                      "bodies_timed": nb, "ms_per_adam_step_all_bodies": plain_total_ms,
+                      "value": units / (plain_total_ms * 1e-3),
+                      "accuracy_bodies": len(plain), "per_body": plain},
+            "batched_over_plain": plain_total_ms / step_ms,
+            "fp64_error": fp64}
 
 
-def relative_residuals(hist, substeps, iters, floor=1e-5):
-    """Per body and substep r_hat_K / r_hat_0 from a (bodies, rows, 4) history; NaN where
-    r_hat_0 is below `floor` (a free-falling body, residual at FP32 round-off)."""
-    r = hist[:, :substeps * iters, 0].reshape(hist.shape[0], substeps, iters)
-    with np.errstate(divide="ignore", invalid="ignore"):
-        rel = r[:, :, -1] / r[:, :, 0]
-    rel[r[:, :, 0] <= floor] = np.nan
-    return rel
+def c5_fp64_error(meshes, log_E, nus, specs, kw, sim, x0, v0, nu_t, le_true, voffs, n_bodies):
+    """The batched forward of one frame (true materials, from the initial state)
+    against the float64 oracle of each sampled body: max vertex deviation over
+    the body's bounding-box diagonal."""
+    import torch
+    from oracle.xpbd_adjoint import DiffOracle, lame_inverse
+    from oracle.xpbd_oracle import OracleSdf
+    from xpbd_gpu.differentiable import xpbd_simulate_batch
+    with torch.no_grad():
+        xg = xpbd_simulate_batch(sim, x0, v0, torch.tensor(le_true, device=x0.device), nu_t, 1).cpu().numpy()
+    sizes = np.array([m.n_tets for m in meshes])
+    pick = [int(k) for k in np.argsort(sizes)[np.linspace(0, len(meshes) - 1, n_bodies).astype(int)]]
+    okw = {k: v for k, v in kw.items() if k != "block_neohookean_enable"}
+    out = []
+    for k in pick:
+        m = meshes[k]
+        im, il = lame_inverse(log_E[k], nus[k])
+        total = 1000.0 * float(np.abs(_volume(m)).sum())
+        o = DiffOracle(m.points, m.tets, [OracleSdf(kk, **p) for kk, p in specs], im, il, total_mass=total, **okw)
+        xe, _, _, _ = o.run(m.points.astype(np.float64), np.zeros((m.n_verts, 3)), 1)
+        diag = float(np.linalg.norm(m.points.max(0) - m.points.min(0)))
+        out.append(dict(body=k, tets=int(m.n_tets),
+                        max_dev_over_bbox_diag=float(np.abs(xg[voffs[k]:voffs[k + 1]] - xe).max()) / diag))
+    return {"reference": "float64 oracle (oracle/xpbd_adjoint.py forward) with each body's per-tet materials",
+            "frames": 1, "bodies": out,
+            "max_over_bodies": max(b["max_dev_over_bbox_diag"] for b in out)}
 
 
 def c3_solvers(args, bodies, specs, kw, cap, target, floor):
@@ -554,6 +595,12 @@ def c3_headline(args, world=1, barrier=lambda: None):
     ms_pf, _ = run_frames(lambda: [s.solve() for s in plain], P, flush, stream)
     units_f = float(Tb.sum()) * S * K0
 
+    # error against FP64: one fixed-count frame of the batch from the settled state
+    # against the float64 and the FP32 C restatement of a sample of bodies
+    batch.restore(state["snap"])
+    batch.solve()
+    fp64 = c3_fp64_error(batch.positions(), state, batch, bodies, specs, kw, args.c3_fp64_bodies)
+
     # projection kernel of the batched form (fixed count: every patch works),
     # CUDA events around each launch of one frame
     batch.restore(state["snap"])
@@ -645,6 +692,7 @@ def c3_headline(args, world=1, barrier=lambda: None):
                                "note": "136 B per tet + 128 B per vertex for every iteration a body ran"},
         "kernel_profile": {k: {"ms_per_launch": v["ms"] / max(1, v["launches"]), "launches": v["launches"]}
                            for k, v in prof.items() if v["launches"]},
+        "fp64_error": fp64,
         "e2e": {"value": float(np.sum(e2e_units)) / (np.sum(e2e_ms) * 1e-3), "unit": UNIT,
                 "h2d_bytes_per_step": 2 * int(state["x"].nbytes), "d2h_bytes_per_step": int(state["x"].nbytes),
                 "ms_per_step": float(np.mean(e2e_ms)),
@@ -658,6 +706,41 @@ def c3_headline(args, world=1, barrier=lambda: None):
                                       "ms_per_substep": {"tpt%d" % r["tets_per_thread"]: r["ms"]
                                                          for r in batch.autotune_result["table"]}}
     return line
+
+
+def c3_fp64_error(x_gpu, state, batch, bodies, specs, kw, n_sample):
+    """Max vertex deviation over the bounding-box diagonal of `n_sample` bodies
+    (spread over the sizes) after one fixed-count frame from the settled state:
+    the GPU batch against the C restatement in FP64, and the same restatement in
+    FP32 against FP64 (what an FP32 run of the reference algorithm departs)."""
+    from xpbd_gpu.mesh import TetMesh
+    sizes = np.array([b.rest_pose.n_tets for b in bodies])
+    pick = [int(k) for k in np.argsort(sizes)[np.linspace(0, len(bodies) - 1, n_sample).astype(int)]]
+    threads = os.cpu_count() or 1
+    S = kw["substeps_num"]
+    out = []
+    for k in pick:
+        b = bodies[k]
+        sl = batch.body_vert_slices[k]
+        pts = b.rest_pose.points @ b.rotation.T + np.asarray(b.offset, dtype=np.float64)
+        mesh = TetMesh(pts, b.rest_pose.tets)
+        kwb = dict(kw, young_modulus=b.young_modulus, poisson_ratio=b.poisson_ratio, density=b.density)
+        devs = {}
+        for name, dt_ in (("fp64", np.float64), ("fp32", np.float32)):
+            o = cpu_oracle(mesh, specs, kwb, S, threads, dtype=dt_)
+            o.x[:] = state["x"][sl]
+            o.v[:] = state["v"][sl]
+            o.rho_hat.value = float(state["rho"][k])
+            o.solve()
+            devs[name] = o.x.astype(np.float64)
+        diag = float(np.linalg.norm(pts.max(0) - pts.min(0)))
+        out.append(dict(body=k, tets=int(sizes[k]),
+                        max_dev_over_bbox_diag=float(np.abs(x_gpu[sl] - devs["fp64"]).max()) / diag,
+                        fp32_reference_max_dev_over_bbox_diag=float(np.abs(devs["fp32"] - devs["fp64"]).max()) / diag))
+    return {"reference": "C restatement in FP64 (and FP32), %d threads" % threads, "frames": 1,
+            "start": "the settled state of the timed window", "iterations": kw["constraints_iter"],
+            "bodies": out, "max_over_bodies": max(b["max_dev_over_bbox_diag"] for b in out),
+            "fp32_reference_max_over_bodies": max(b["fp32_reference_max_dev_over_bbox_diag"] for b in out)}
 
 
 def measured_peak():
@@ -1130,8 +1213,9 @@ def c2_line(args, workload_name, world=1, barrier=lambda: None, cpu_substeps=Non
 
 def run_gb300(args):
     """The GB300 arm.  Default (c3): the metric's 256-body batch at equal
-    residual, with the 64^3 single body (c2) and the differentiable cube's
-    adjoint cost (c4) as extra keys of the same line."""
+    residual, with the 64^3 single body (c2), the differentiable cube's
+    adjoint cost (c4) and the batched differentiable form against the plain
+    per-body form (c5, a few Adam steps) as extra keys of the same line."""
     import torch
     rank, local_rank, world = dist_info()
     torch.cuda.set_device(local_rank)
@@ -1153,6 +1237,7 @@ def run_gb300(args):
         if not args.no_extra:
             line["c2"] = c2_line(args, "c2", cpu_substeps=5)
             line["c4"] = c4_block(args)
+            line["c5"] = c5_block(args, args.c5_bench_steps, plain_accuracy_bodies=0, fp64_bodies=3)
     else:
         line = c2_line(args, args.workload, world, barrier)
         if line is None:
@@ -1217,11 +1302,13 @@ def main():
     ap.add_argument("--c3-floor", type=float, default=1e-5, help="r_hat below which a substep has converged")
     ap.add_argument("--c3-settle", type=int, default=90, help="frames stepped before the timed window")
     ap.add_argument("--c3-plain-frames", type=int, default=4, help="timed frames of the plain form")
-    ap.add_argument("--no-extra", action="store_true", help="c3 line without the c2 / c4 keys")
+    ap.add_argument("--c3-fp64-bodies", type=int, default=8, help="bodies checked against FP64")
+    ap.add_argument("--no-extra", action="store_true", help="c3 line without the c2 / c4 / c5 keys")
     ap.add_argument("--c5-frames", type=int, default=30)
     ap.add_argument("--c5-adam-steps", type=int, default=200)
     ap.add_argument("--c5-lr", type=float, default=0.05)
-    ap.add_argument("--c5-plain-bodies", type=int, default=4)
+    ap.add_argument("--c5-plain-bodies", type=int, default=4, help="bodies of the plain-form accuracy run")
+    ap.add_argument("--c5-bench-steps", type=int, default=4, help="Adam steps of the c5 key of the default line")
     ap.add_argument("--c4-frames", type=int, default=60)
     ap.add_argument("--c4-reps", type=int, default=2)
     ap.add_argument("--c4-check-frames", type=int, default=1)
