@@ -203,7 +203,8 @@ def c4_block(args):
     xf = xpbd_simulate(sim2, xt, vt, let, nut, hf)
     (xf.double() * torch.tensor(c, device=dev)).sum().backward()
     okw = {k: v for k, v in kw.items() if k != "block_neohookean_enable"}
-    o = DiffOracle(mesh.points, mesh.tets, [OracleSdf(k, **p) for k, p in specs], *lame_inverse(le0, 0.45), **okw)
+    o = DiffOracle(mesh.points, mesh.tets, [OracleSdf(k, **p) for k, p in specs], *lame_inverse(le0, 0.45),
+                   omega_grad=sim2.omega_grad, **okw)
     o.rho_hat = rho0
     _, xb, vb, gm, gl, _ = o.gradient(x_s.cpu().numpy().astype(np.float64), v_s.cpu().numpy().astype(np.float64),
                                       hf, c)
@@ -222,6 +223,8 @@ def c4_block(args):
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": desc, "step": "forward of %d frames with per-substep checkpoints" % frames},
             "adjoint": {"backward_ms": bwd_ms, "backward_over_forward": bwd_ms / fwd_ms,
+                        "omega": "through omega (omega -> rho_hat -> r_hat adjoint)" if sim.omega_grad
+                        else "stop-gradient",
                         "note": "backward = per-substep tape recompute + reverse kernels"},
             "gradient_check": {"start_frame": args.c4_check_start, "horizon_frames": hf, "directions": 32,
                                "reference": "float64 adjoint (oracle/xpbd_adjoint.py, itself checked against "
@@ -1250,15 +1253,32 @@ def run_profile(args):
     import torch
     from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
     if args.workload == "c3":  # the batched form alone
+        # `profile_settle` frames at the fixed 30 iterations (frame graphs), then
+        # `profile_frames` frames in stop mode (with --profile-stop) or at the fixed
+        # count, as direct launches
         from xpbd_gpu.batched import XPBDBatchedSolver
         bodies, specs, kw, desc = workload_c3()
+        cap = args.c3_cap if args.profile_stop else kw["constraints_iter"]
         batch = XPBDBatchedSolver(bodies, product_sdfs(specs), tets_per_thread=min(args.tets_per_thread, 2),
-                                  use_graph=False, pair_tets=bool(args.pair_tets), **kw)
+                                  use_graph=True, pair_tets=bool(args.pair_tets), **dict(kw, constraints_iter=cap))
+        batch.set_stop(0.0, 0.0, kw["constraints_iter"])
+        for _ in range(args.profile_settle):
+            batch.solve()
+        batch.use_graph = False
+        if args.profile_stop:
+            batch.set_stop(args.c3_target, args.c3_floor, cap)
+        else:
+            batch.set_stop(0.0, 0.0, kw["constraints_iter"])
+        torch.cuda.synchronize()
+        # the profiled frames sit in the NVTX range "frames" (ncu --nvtx --nvtx-include frames/)
+        torch.cuda.nvtx.range_push("frames")
         for _ in range(args.profile_frames):
             batch.solve()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         batch.check_status()
-        print("profile mode: %d frame(s) of %s (batched)" % (args.profile_frames, desc))
+        print("profile mode: %d settle frame(s) + %d %s frame(s) of %s (batched)" % (
+            args.profile_settle, args.profile_frames, "stop-mode" if args.profile_stop else "fixed-count", desc))
         return
     if args.workload == "c5":  # batched forward + adjoint of `profile_frames` frames
         from xpbd_gpu.batched import Body
@@ -1266,7 +1286,7 @@ def run_profile(args):
         meshes, log_E, nus, specs, kw, desc = workload_c5()
         bodies = [Body(m, tet_young_modulus=np.exp(log_E[k]), tet_poisson_ratio=nus[k], density=1000.0,
                        poisson_ratio=float(nus[k])) for k, m in enumerate(meshes)]
-        sim = BatchedDiffSim(bodies, product_sdfs(specs), **kw)
+        sim = BatchedDiffSim(bodies, product_sdfs(specs), use_graphs=False, **kw)
         dev = torch.device("cuda")
         x0 = torch.tensor(np.concatenate([m.points for m in meshes]), dtype=torch.float32, device=dev)
         le = torch.tensor(np.concatenate(log_E), dtype=torch.float64, device=dev, requires_grad=True)
@@ -1330,6 +1350,8 @@ def main():
     ap.add_argument("--fp64-warm-frames", type=int, default=1)
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     ap.add_argument("--profile-frames", type=int, default=1)
+    ap.add_argument("--profile-settle", type=int, default=0, help="c3 profile mode: frames stepped first (graphs)")
+    ap.add_argument("--profile-stop", type=int, default=0, choices=[0, 1], help="c3 profile mode: stop-mode frames")
     args = ap.parse_args()
     if args.mode == "profile":
         run_profile(args)

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define XPBD_ABI_VERSION 2
+#define XPBD_ABI_VERSION 3
 
 enum xpbd_status {
   XPBD_OK = 0,
@@ -270,14 +270,22 @@ int xpbd_check_status(void* handle, void* stream);
  * Differentiation of one substep (block mode, ATOMIC or GATHER variant,
  * per-tet materials).  No counterpart in the reference, which has no
  * gradients; the adjoint follows the forward of neohookean_solver.py:453-587.
- * omega is a stop-gradient; contact sets and the pivot branch are piecewise
- * constant.
+ * Contact sets and the pivot branch are piecewise constant.  The Chebyshev
+ * omega is a stop-gradient unless the tape carries `posts` and `rho_in` and
+ * the adjoint an `omega_state`: then the adjoint also runs back through
+ * omega_k -> rho_hat_k -> r_hat_k -> the post-Jacobi positions, multipliers
+ * and compliances (:298-329, :495-546), the derivative of the forward as it
+ * runs; the clamp of the rho ratio and the warm-up are piecewise constant.
  * ------------------------------------------------------------------------ */
 typedef struct xpbd_tape {
-  float* xs;   /* [(K+1)][V][4] predicted positions entering every iteration */
-  float* lams; /* [K][T][2] multipliers entering every iteration */
-  float* xpre; /* [V][4] predicted positions before the SDF list */
-  float* v1;   /* [V][4] velocities after gravity */
+  float* xs;      /* [(K+1)][V][4] predicted positions entering every iteration */
+  float* lams;    /* [K][T][2] multipliers entering every iteration; with posts
+                     [K+1][T][2], the last being those after the substep */
+  float* xpre;    /* [V][4] predicted positions before the SDF list */
+  float* v1;      /* [V][4] velocities after gravity */
+  float* posts;   /* [K][V][4] post-Jacobi positions of every iteration, or NULL
+                     (omega then is a stop-gradient) */
+  double* rho_in; /* [bodies] rho_hat entering the substep (with posts) */
 } xpbd_tape;
 
 typedef struct xpbd_adjoint {
@@ -291,6 +299,11 @@ typedef struct xpbd_adjoint {
   float* dxbar;         /* [V][4] scratch */
   float* lambar;        /* [T][2] scratch */
   const float* cnt;     /* [V] constraints per vertex (vertex valence) */
+  double* omega_state;  /* [bodies][8 + 6 K] the omega chain's state and the
+                           substep's chain coefficients, or NULL (omega is a
+                           stop-gradient); zero it before the first substep
+                           adjoint of a backward pass (it carries the adjoint of
+                           rho_hat, which persists across substeps, backwards) */
 } xpbd_adjoint;
 
 /* One substep (as xpbd_substep) that records `tape`; history rows [0, K)

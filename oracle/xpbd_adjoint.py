@@ -7,9 +7,15 @@ adjoint kernels (``xpbd_substep_adjoint``) and is itself checked against
 central finite differences in ``tests/test_adjoint_oracle.py``.
 
 Differentiation conventions (the GPU adjoint follows the same):
-* The Chebyshev factor omega is a stop-gradient: it is a control heuristic
-  driven by the residual ratio (neohookean_solver.py:495-546).  Finite
-  differences that check these gradients replay the recorded omega schedule.
+* The Chebyshev factor omega: by default a stop-gradient, a control heuristic
+  driven by the residual ratio (neohookean_solver.py:495-546); finite
+  differences that check such gradients replay the recorded omega schedule.
+  With ``omega_grad=True`` the adjoint also runs backwards through omega:
+  omega_k depends on rho_hat_k (and omega_{k-1}), rho_hat_k on the clamped
+  ratio r_hat_k / r_hat_{k-1} (and rho_hat_{k-1}, which persists across
+  substeps), and r_hat_k on the post-Jacobi positions, the multipliers after
+  the iteration and the compliances (compute_xpbd_residual, :298-329).  The
+  clamp of the ratio and the warm-up are piecewise constant.
 * The active-contact sets (inside a SDF) and the 2x2 pivot branch are
   piecewise constant; the derivative is the derivative of A^-1 b.
 * Materials enter as per-tet inverse Lame parameters inv_mu = 1/mu,
@@ -166,7 +172,8 @@ class DiffOracle:
 
     def __init__(self, points, tets, sdfs, inv_mu, inv_la, frame_dt, dt, substeps_num, constraints_iter,
                  cheb_enable=True, cheb_warmup=5, cheb_gamma=0.6666, total_mass=1.0, damping=5.0,
-                 gravity=(0.0, -9.8, 0.0)):
+                 gravity=(0.0, -9.8, 0.0), omega_grad=False):
+        self.omega_grad = bool(omega_grad)
         self.tets = np.asarray(tets, dtype=np.int64)
         self.x0 = np.asarray(points, dtype=np.float64).copy()
         P = self.x0[self.tets]
@@ -233,6 +240,9 @@ class DiffOracle:
         lam = np.zeros((len(self.tets), 2))
         xs, lams, oms = [xt.copy()], [], []
         prev, omega = None, 1.0
+        # the omega chain: r_hat_k, rho_hat_k, whether rho_hat was updated and the
+        # ratio clamped at iteration k, and the post-Jacobi positions
+        chain = dict(rho_in=self.rho_hat, r=[], rho=[], upd=[], clamped=[], post=[], lam_next=[])
         for it in range(self.K):
             lams.append(lam.copy())
             dp, dlam, _ = project_forward(xt[self.tets], self.Dm, w, lam, aD, aH)
@@ -243,10 +253,21 @@ class DiffOracle:
             if self.cheb:
                 if omegas is None:
                     r = self._residual(post, lam, aD, aH)
-                    if prev is not None and prev > EPSILON:
-                        ri = max(1e-5, min(0.99999, r / (prev + EPSILON)))
+                    upd = prev is not None and prev > EPSILON
+                    clamped = False
+                    if upd:
+                        ratio = r / (prev + EPSILON)
+                        ri = max(1e-5, min(0.99999, ratio))
+                        clamped = ri != ratio
                         self.rho_hat = 0.8 * self.rho_hat + 0.2 * ri
                     prev = r
+                    if tape is not None:
+                        chain["r"].append(r)
+                        chain["rho"].append(self.rho_hat)
+                        chain["upd"].append(upd)
+                        chain["clamped"].append(clamped)
+                        chain["post"].append(post.copy())
+                        chain["lam_next"].append(lam.copy())
                     r2 = self.rho_hat ** 2
                     omega = 1.0 if it < self.warmup else (2.0 / (2.0 - r2) if it == self.warmup
                                                           else 4.0 / (4.0 - r2 * omega))
@@ -266,7 +287,7 @@ class DiffOracle:
         xo[live] = xt[live]
         if tape is not None:
             tape.update(x=x.copy(), v=v.copy(), v1=v1, sdf_q=sdf_q, sdf_act=sdf_act, xs=xs, lams=lams, oms=oms,
-                        aD=aD, aH=aH, sdt=sdt)
+                        aD=aD, aH=aH, sdt=sdt, chain=chain)
         return xo, vo, oms
 
     def run(self, x, v, frames, omegas=None, record=False):
@@ -295,12 +316,20 @@ class DiffOracle:
         g_mu = np.zeros(len(self.tets))
         g_la = np.zeros(len(self.tets))
         yprev_bar_next = np.zeros_like(xbar)
+        chain = tape.get("chain")
+        through_omega = self.omega_grad and self.cheb and chain is not None and len(chain["r"]) == self.K
+        om_carry = r_carry = 0.0  # adjoints of omega_{k} and r_hat_{k} from iteration k + 1
         for it in reversed(range(self.K)):
             xt = tape["xs"][it]
             lam = tape["lams"][it]
+            lam_next_bar = tape.setdefault("_lam_bar", np.zeros_like(lam))
             if self.cheb:
                 om = tape["oms"][it]
                 post_bar = om * self.gamma * xt_bar
+                if through_omega:
+                    post_bar = post_bar + self._omega_chain(tape, it, xt_bar, om_carry, r_carry, lam_next_bar,
+                                                            g_mu, g_la, sdt)
+                    om_carry, r_carry = self._carry
                 cur_bar = om * (1.0 - self.gamma) * xt_bar + post_bar + yprev_bar_next
                 yprev_bar = (1.0 - om) * xt_bar
             else:
@@ -312,7 +341,6 @@ class DiffOracle:
             P = xt[self.tets]
             _, _, cache = project_forward(P, self.Dm, w, lam, tape["aD"], tape["aH"])
             # lambda_{k+1} = lambda_k + dlam: the adjoint of lambda_{k+1} flows to both
-            lam_next_bar = tape.setdefault("_lam_bar", np.zeros_like(lam))
             P_bar, lam_bar, aD_bar, aH_bar = project_adjoint(P, self.Dm, w, lam, tape["aD"], tape["aH"], dp_bar,
                                                              lam_next_bar, cache)
             tape["_lam_bar"] = lam_next_bar + lam_bar
@@ -333,6 +361,65 @@ class DiffOracle:
         v1_bar = v1_bar + qbar * sdt
         return x_bar, v1_bar, g_mu, g_la
 
+    def _omega_chain(self, tape, k, xt_bar, om_carry, r_carry, lam_next_bar, g_mu, g_la, sdt):
+        """Iteration k of the reverse pass through omega (omega_grad): from the
+        adjoint of x~_{k+1} to that of omega_k, rho_hat_k and r_hat_k, and from
+        r_hat_k (the residual at the post-Jacobi positions with lambda_{k+1},
+        neohookean_solver.py:298-329) to the post-Jacobi positions (returned),
+        the multipliers after the iteration (added to lam_next_bar) and the
+        compliances (added to g_mu, g_la).  self._rho_bar carries the adjoint of
+        rho_hat backwards; self._carry receives the adjoints of omega_{k-1} and
+        r_hat_{k-1} that iteration k contributes."""
+        ch = tape["chain"]
+        xs, oms = tape["xs"], tape["oms"]
+        W = self.warmup
+        om = oms[k]
+        y = xs[k - 1] if k > 0 else xs[0]
+        wb = float((xt_bar * (xs[k + 1] - y)).sum()) / om + om_carry  # x~_{k+1} - y = om (xn - y)
+        rho = ch["rho"][k]
+        om_prev = oms[k - 1] if k > 0 else 1.0
+        next_om_carry = 0.0
+        if k == W:
+            self._rho_bar += wb * 4.0 * rho / (2.0 - rho * rho) ** 2
+        elif k > W:
+            den = 4.0 - rho * rho * om_prev
+            self._rho_bar += wb * 8.0 * rho * om_prev / (den * den)
+            next_om_carry = wb * 4.0 * rho * rho / (den * den)
+        r_bar = r_carry
+        next_r_carry = 0.0
+        if ch["upd"][k]:
+            ri_bar = 0.2 * self._rho_bar
+            self._rho_bar *= 0.8
+            if not ch["clamped"][k]:
+                d = ch["r"][k - 1] + EPSILON
+                r_bar += ri_bar / d
+                next_r_carry = -ri_bar * ch["r"][k] / (d * d)
+        self._carry = (next_om_carry, next_r_carry)
+        if r_bar == 0.0:
+            return np.zeros_like(xt_bar)
+        # r_hat = (1/T) sum_t sqrt(rD^2 + rH^2), rD = C_D + aD lambda_D, rH = C_H + aH lambda_H
+        post, lamn = ch["post"][k], ch["lam_next"][k]
+        aD, aH = tape["aD"], tape["aH"]
+        P = post[self.tets]
+        E = np.stack([P[:, 1] - P[:, 0], P[:, 2] - P[:, 0], P[:, 3] - P[:, 0]], axis=-1)
+        F = E @ self.Dm
+        rD = (F * F).sum((1, 2)) - 3.0 + aD * lamn[:, 0]
+        rH = _det3(F) - 1.0 + aH * lamn[:, 1]
+        sq = np.sqrt(rD * rD + rH * rH)
+        sb = r_bar / len(F)
+        nz = sq > 0.0
+        rDb = np.where(nz, sb * rD / np.where(nz, sq, 1.0), 0.0)
+        rHb = np.where(nz, sb * rH / np.where(nz, sq, 1.0), 0.0)
+        Fb = rDb[:, None, None] * 2.0 * F + rHb[:, None, None] * _cof(F)
+        Pb = _corner(Fb, self.Dm)
+        out = np.zeros_like(xt_bar)
+        np.add.at(out, self.tets.reshape(-1), Pb.reshape(-1, 3))
+        lam_next_bar[:, 0] += rDb * aD
+        lam_next_bar[:, 1] += rHb * aH
+        g_mu += rDb * lamn[:, 0] / (self.V0 * sdt * sdt)
+        g_la += rHb * lamn[:, 1] / (self.V0 * sdt * sdt)
+        return out
+
     def gradient(self, x, v, frames, xbar_final, vbar_final=None):
         """Adjoint of `frames` frames from (x, v): returns (omegas, x_bar, v_bar,
         g_inv_mu, g_inv_la) for the loss whose gradient w.r.t. the final
@@ -342,6 +429,7 @@ class DiffOracle:
         vb = np.zeros_like(xb) if vbar_final is None else np.asarray(vbar_final, dtype=np.float64).copy()
         gm = np.zeros(len(self.tets))
         gl = np.zeros(len(self.tets))
+        self._rho_bar = 0.0  # the loss does not read rho_hat; it flows back through omega
         for tape in reversed(tapes):
             xb, vb, a, b = self.substep_adjoint(tape, xb, vb)
             gm += a

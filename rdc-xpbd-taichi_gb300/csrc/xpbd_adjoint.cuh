@@ -12,9 +12,20 @@
 //                2x2 compliance solve -> dx (:358-451), with the material
 //                adjoints accumulated per tet in FP64
 //   ka_begin    SDF list in reverse order + predict (xpbd_base.py:139-178)
-// Conventions: omega is a stop-gradient (a control heuristic of the
-// residual ratio); the contact sets and the pivot branch are piecewise
-// constant; the derivative of the 2x2 solve is that of A^-1 b.
+// Conventions: the contact sets and the pivot branch are piecewise constant;
+// the derivative of the 2x2 solve is that of A^-1 b.  Omega is a
+// stop-gradient unless the tape holds the post-Jacobi positions (Tape::posts)
+// and the adjoint an omega state (Adj::om): then
+//     ka_end           also replays the substep's rho_hat curve into a table of
+//                      per-iteration chain coefficients (FP64, one thread per
+//                      body; neohookean_solver.py:495-504, :537-546)
+//     ka_cheb          also sums omega_k's adjoint over the vertices
+// and, between ka_cheb and the tet adjoint of each iteration,
+//     ka_residual_adj  steps the omega_k -> rho_hat_k -> r_hat_k chain (every
+//                      CTA for its body; one CTA per body stores the state)
+//                      and takes r_hat_k's adjoint to the post-Jacobi
+//                      positions, the multipliers after the iteration and the
+//                      compliances (:298-329).
 //
 // The kernels are templates over the solver's device view D (the single-body
 // and the batched layouts).  Each layout provides, next to its own type so
@@ -27,17 +38,35 @@
 //         (a layout with its own tet kernel calls tet_adjoint directly)
 //   float adj_omega(const D&, int i, int k)          omega of vertex i's body
 //                                                    at iteration k
-// and the members x, v, sdfs, n_sdf.
+// and the members x, v, sdfs, n_sdf.  The omega chain also needs
+//   int    adj_nbodies(const D&)                    bodies (Chebyshev states)
+//   int    adj_vbody(const D&, int i)               body of vertex i
+//   double adj_hist(const D&, int b, int k, int c)  history row k of body b
+//   double adj_body_tets(const D&, int b)           real tets of body b
 #pragma once
 
 namespace xpbd {
 
 struct Tape {
   float4* xs;    // [(K+1)][V] predicted positions entering iteration k (w = inv_m)
-  float2* lams;  // [K][T] multipliers entering iteration k
+  float2* lams;  // [K][T] multipliers entering iteration k ([K+1] with posts: and after the last)
   float4* xpre;  // [V] predicted positions before the SDF list
   float4* v1;    // [V] velocities after gravity
+  float4* posts;  // [K][V] post-Jacobi positions of iteration k; nullptr: omega is a stop-gradient
+  double* rho_in; // [bodies] rho_hat entering the substep (with posts)
 };
+
+// Omega chain state per body (Adj::om), om_stride(K) = 8 + 6 K doubles.  Pairs
+// indexed by the iteration's parity (iteration k reads [k & 1] and writes
+// [(k & 1) ^ 1]): the adjoint of omega_k summed over the vertices (ka_cheb),
+// the adjoints of omega_k and r_hat_k passed down from iteration k + 1, and
+// the adjoint of rho_hat (it persists across substeps: zero the state before
+// a backward pass).  Then per iteration k a row of coefficients (kTab + 6 k):
+//   1 / omega_k, d omega_k / d rho_hat_k, d omega_k / d omega_{k-1},
+//   the rho_hat update weight beta (0 where rho_hat was not updated),
+//   d ratio_k / d r_hat_k and d ratio_k / d r_hat_{k-1} (0 where clamped).
+enum { kOmSum = 0, kOmCarry = 2, kRCarry = 4, kRhoBar = 6, kTab = 8, kTabRow = 6 };
+__host__ __device__ __forceinline__ int om_stride(int K) { return kTab + kTabRow * K; }
 
 struct Adj {
   float4* gx;        // [V] in: dL/dx at the end of the substep, out: at its start
@@ -49,6 +78,8 @@ struct Adj {
   float4* dxbar;     // [V] adjoint of the Jacobi accumulator
   float2* lambar;    // [T] adjoint of the multipliers
   const float* cnt;  // [V] constraints per vertex (valence in block mode)
+  double* om;        // [bodies][om_stride(K)] omega chain state; nullptr: omega is a stop-gradient
+  int om_n;          // om_stride(K)
 };
 
 __device__ __forceinline__ float3 f3(const float4 a) { return make_float3(a.x, a.y, a.z); }
@@ -77,9 +108,63 @@ __global__ void __launch_bounds__(256) k_tape_begin(D d, Tape tp, float dt, floa
 
 // Reverse of advance: live vertices x' = x~_K, v' = (x~_K - x) e / dt; pinned
 // vertices keep x and v.
+// With the omega chain, block 0 also starts the chain state of the substep's
+// last iteration and tabulates its coefficients (ChainPrm).
+struct ChainPrm {
+  int K, warmup;
+  double rho_min, rho_max, beta;
+};
+
 template <class D>
-__global__ void __launch_bounds__(256) ka_end(D d, Adj a, float e_over_dt) {
+__device__ void chain_table(const D& d, const Tape& tp, const Adj& a, const ChainPrm& c, int b) {
+  double* o = a.om + (size_t)a.om_n * b;
+  const int q = (c.K - 1) & 1;
+  // the adjoint of rho_hat entering the later substep (written by its iteration
+  // 0 into slot 1) is that of rho_hat leaving this one
+  o[kRhoBar + q] = o[kRhoBar + 1];
+  o[kOmSum] = o[kOmSum + 1] = o[kOmCarry] = o[kOmCarry + 1] = o[kRCarry] = o[kRCarry + 1] = 0.0;
+  double rho = tp.rho_in[b], prev = 0.0;
+  for (int j = 0; j < c.K; ++j) {
+    const double r = adj_hist(d, b, j, 0);
+    const double om = adj_hist(d, b, j, 1);
+    const bool upd = j > 0 && prev > 1e-12;
+    double c1 = 0.0, c2 = 0.0;
+    if (upd) {
+      const double dd = prev + 1e-12;
+      const double ratio = r / dd;
+      const double ri = fmax(c.rho_min, fmin(c.rho_max, ratio));
+      if (ri == ratio) {
+        c1 = 1.0 / dd;
+        c2 = -ratio / dd;
+      }
+      rho = (1.0 - c.beta) * rho + c.beta * ri;
+    }
+    double A = 0.0, B = 0.0;
+    if (j == c.warmup) {
+      const double den = 2.0 - rho * rho;
+      A = 4.0 * rho / (den * den);
+    } else if (j > c.warmup) {
+      const double om_prev = adj_hist(d, b, j - 1, 1);
+      const double den = 4.0 - rho * rho * om_prev;
+      A = 8.0 * rho * om_prev / (den * den);
+      B = 4.0 * rho * rho / (den * den);
+    }
+    double* t = o + kTab + kTabRow * j;
+    t[0] = 1.0 / om;
+    t[1] = A;
+    t[2] = B;
+    t[3] = upd ? c.beta : 0.0;
+    t[4] = c1;
+    t[5] = c2;
+    prev = r;
+  }
+}
+
+template <class D>
+__global__ void __launch_bounds__(256) ka_end(D d, Tape tp, Adj a, ChainPrm cp, float e_over_dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a.om && blockIdx.x == 0)
+    for (int b = threadIdx.x; b < adj_nbodies(d); b += blockDim.x) chain_table(d, tp, a, cp, b);
   if (i >= adj_verts(d)) return;
   const float4 gx = a.gx[i], gv = a.gv[i];
   if (d.x[i].w > 0.f) {
@@ -98,8 +183,32 @@ __global__ void __launch_bounds__(256) ka_end(D d, Adj a, float e_over_dt) {
 // with y_prev(0) = x~_0.  Reads abuf[src] (adjoint of x~_{k+1}), writes
 // abuf[src^1] (direct part of the adjoint of x~_k), ybar and dxbar.
 template <class D, bool kCheb>
-__global__ void __launch_bounds__(256) ka_cheb(D d, Adj a, int k, float gamma, int src) {
+__global__ void __launch_bounds__(256) ka_cheb(D d, Tape tp, Adj a, int k, float gamma, int src) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (kCheb && a.om) {
+    // omega_k's adjoint: sum over the vertices of x~bar_{k+1} . (xn - y_prev),
+    // with xn - y_prev = (x~_{k+1} - y_prev) / omega_k (divided in chain_step).  A
+    // CTA covers 256 vertices of one body.
+    // FP32 within a warp, FP64 across warps and CTAs
+    float part = 0.f;
+    if (i < adj_verts(d)) {
+      const size_t V = (size_t)adj_verts(d);
+      const float4 xb = adj_buf(a, src)[i];
+      const float4 x1 = tp.xs[(size_t)(k + 1) * V + i], y = tp.xs[(size_t)(k > 0 ? k - 1 : 0) * V + i];
+      part = xb.x * (x1.x - y.x) + xb.y * (x1.y - y.y) + xb.z * (x1.z - y.z);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
+    __shared__ float s_part[8];
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sum = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += (double)s_part[w];
+      const int i0 = blockIdx.x * blockDim.x;
+      if (i0 < adj_verts(d)) atomicAdd(a.om + (size_t)a.om_n * adj_vbody(d, i0) + kOmSum + (k & 1), sum);
+    }
+  }
   if (i >= adj_verts(d)) return;
   const float4 xb = adj_buf(a, src)[i];
   float3 post, cur, yn;
@@ -264,6 +373,93 @@ __global__ void __launch_bounds__(128) ka_project(D d, Tape tp, Adj a, int k, fl
 #pragma unroll
   for (int c = 0; c < 4; ++c) red_add_v4(G + vid[c], gout[c].x, gout[c].y, gout[c].z, 0.f);
   // materials: aD = (1/mu) sD, aH = (1/lambda) sH
+  a.g_mu[t] += (double)(aDb * sD);
+  a.g_la[t] += (double)(aHb * sH);
+}
+
+// One step of the omega chain backwards, iteration k of body b: from omega_k's
+// adjoint to rho_hat_k's and r_hat_k's (returned).  Every CTA that needs r_hat_k's
+// adjoint calls it with the same inputs; the one with `store` keeps the state
+// for iteration k - 1.
+__device__ __forceinline__ double chain_step(const Adj& a, int b, int k, bool store) {
+  double* o = a.om + (size_t)a.om_n * b;
+  const double* t = o + kTab + kTabRow * k;
+  const int q = k & 1;
+  const double wb = o[kOmSum + q] * t[0] + o[kOmCarry + q];
+  double rho_bar = o[kRhoBar + q] + t[1] * wb;
+  const double ri_bar = t[3] * rho_bar;
+  rho_bar -= ri_bar;
+  const double rb = o[kRCarry + q] + t[4] * ri_bar;
+  if (store) {
+    o[kOmCarry + (q ^ 1)] = t[2] * wb;
+    o[kRCarry + (q ^ 1)] = t[5] * ri_bar;
+    o[kRhoBar + (q ^ 1)] = rho_bar;
+    o[kOmSum + (q ^ 1)] = 0.0;  // ka_cheb of iteration k - 1 sums into it
+  }
+  return rb;
+}
+
+// The residual's part of one tet: r_hat = (1/n) sum_t sqrt(rD^2 + rH^2),
+// rD = C_D + aD lambda_D, rH = C_H + aH lambda_H at the post-Jacobi positions
+// (tt.p) with the multipliers after the iteration (L1).  From r_hat's adjoint
+// rb_n = rb / n: the corner position adjoints (g) and those of L1 and of aD, aH.
+template <bool kPrecise>
+__device__ __forceinline__ void residual_adjoint(const Tet& tt, const float2 L1, const float aD, const float aH,
+                                                 const float rb_n, float3 (&g)[4], float2& lb, float& aDb,
+                                                 float& aHb) {
+  float F[9];
+  deformation_gradient(tt, F);
+  float C_D, C_H;
+  invariants<kPrecise>(F, C_D, C_H);
+  const float rD = C_D + aD * L1.x, rH = C_H + aH * L1.y;
+  const float sq = sqrtf(rD * rD + rH * rH);
+  const float rDb = sq > 0.f ? rb_n * rD / sq : 0.f, rHb = sq > 0.f ? rb_n * rH / sq : 0.f;
+  float H[9], Fb[9];
+  cofactor(F, H);
+#pragma unroll
+  for (int q = 0; q < 9; ++q) Fb[q] = 2.f * rDb * F[q] + rHb * H[q];
+  corner_gradients(Fb, tt.dm, g);
+  lb = make_float2(rDb * aD, rHb * aH);
+  aDb = rDb * L1.x;
+  aHb = rHb * L1.y;
+}
+
+// r_hat_k's adjoint into the tets of iteration k (single-body layout, one
+// thread per tet): scatters the position adjoints into the Jacobi
+// accumulator's (dxbar, post = x~ + dx / cnt) and into abuf[dst] (x~_k's),
+// adds to the multipliers' adjoint (still that of lambda_{k+1}) and to the
+// material adjoints.
+template <class D, bool kPrecise>
+__global__ void __launch_bounds__(128) ka_residual_adj(D d, Tape tp, Adj a, int k, float cD, float cH, int dst) {
+  __shared__ float s_rb;
+  if (threadIdx.x == 0) s_rb = (float)(chain_step(a, 0, k, blockIdx.x == 0) / adj_body_tets(d, 0));
+  __syncthreads();
+  const float rb_n = s_rb;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= adj_tets(d) || rb_n == 0.f) return;
+  int vid[4];
+  Tet tt;
+  float inv_v0, m_mu, m_la;
+  if (!adj_load_tet(d, t, vid, tt, inv_v0, m_mu, m_la)) return;
+  const float4* X = tp.posts + (size_t)k * adj_verts(d);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) tt.p[c] = __ldg(X + vid[c]);
+  const float2 L1 = tp.lams[(size_t)(k + 1) * adj_tets(d) + t];
+  const float sD = cD * inv_v0, sH = cH * inv_v0;
+  float3 g[4];
+  float2 lb;
+  float aDb, aHb;
+  residual_adjoint<kPrecise>(tt, L1, sD * m_mu, sH * m_la, rb_n, g, lb, aDb, aHb);
+  float4* G = adj_buf(a, dst);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float cn = a.cnt[vid[c]];
+    const float ic = cn > 0.f ? 1.f / cn : 0.f;
+    red_add_v4(G + vid[c], g[c].x, g[c].y, g[c].z, 0.f);
+    red_add_v4(a.dxbar + vid[c], g[c].x * ic, g[c].y * ic, g[c].z * ic, 0.f);
+  }
+  const float2 l0 = a.lambar[t];
+  a.lambar[t] = make_float2(l0.x + lb.x, l0.y + lb.y);
   a.g_mu[t] += (double)(aDb * sD);
   a.g_la[t] += (double)(aHb * sH);
 }

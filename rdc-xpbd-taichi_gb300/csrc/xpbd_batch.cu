@@ -505,6 +505,7 @@ struct BUpd {
   int stop;
   int use_cond;
   cudaGraphConditionalHandle cond;
+  float4* post_out;  // taping through omega: the post-Jacobi positions (nullptr: none)
 };
 
 template <bool kCheb, bool kFirstIt>
@@ -550,6 +551,7 @@ __global__ void __launch_bounds__(256) kb_update(BDev d, int cur, float gamma, B
     if (i < 0) continue;
     d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 xp = post_position(pc[k], D[k]);
+    if (u.post_out) u.post_out[i] = make_float4(xp.x, xp.y, xp.z, pc[k].w);
     if (kCheb) {
       const float nx = gamma * (xp.x - pc[k].x) + pc[k].x;
       const float ny = gamma * (xp.y - pc[k].y) + pc[k].y;
@@ -629,6 +631,12 @@ __device__ __forceinline__ float adj_omega(const BDev& d, int i, int k) {
   const int b = __ldg(d.vblock_body + (i >> 8));
   return (float)d.hist[4 * ((size_t)b * d.max_records + k) + 1];
 }
+__device__ __forceinline__ int adj_nbodies(const BDev& d) { return d.n_bodies; }
+__device__ __forceinline__ int adj_vbody(const BDev& d, int i) { return __ldg(d.vblock_body + (i >> 8)); }
+__device__ __forceinline__ double adj_hist(const BDev& d, int b, int k, int c) {
+  return d.hist[4 * ((size_t)b * d.max_records + k) + c];
+}
+__device__ __forceinline__ double adj_body_tets(const BDev& d, int b) { return (double)__ldg(d.body_tets + b); }
 }  // namespace batch
 }  // namespace xpbd
 
@@ -713,6 +721,84 @@ __global__ void __launch_bounds__(kP, 3) kba_project(BDev d, Tape tp, Adj a, int
   a.g_la[t] += (double)(aHb * s0);
 }
 
+// r_hat_k's adjoint into the tets of iteration k, one CTA per patch (the
+// batched layout of ka_residual_adj): the patch's post-Jacobi positions are
+// staged in shared memory; each thread takes one tet and scatters its corner
+// adjoints into abuf[dst] and dxbar with red.global.add.v4.
+template <bool kPrecise>
+__global__ void __launch_bounds__(kP) kba_residual_adj(BDev d, Tape tp, Adj a, int k, float c, int dst) {
+  __shared__ float4 sp[256];
+  __shared__ int sg[256];
+  __shared__ float s_rb;
+  const int p = blockIdx.x;
+  const int body = __ldg(d.patch_body + p);
+  // every patch steps its body's chain; the body's first patch stores it
+  if (threadIdx.x == 0)
+    s_rb = (float)(chain_step(a, body, k, p == __ldg(d.body_first + body)) / adj_body_tets(d, body));
+  __syncthreads();
+  const float rb_n = s_rb;
+  if (rb_n == 0.f) return;
+  const int vb = __ldg(d.voff + p);
+  const int nv = __ldg(d.voff + p + 1) - vb;
+  const int nt = __ldg(d.patch_ntets + p);
+  const bool live = (int)threadIdx.x < nt;
+  const int t = p * kP + threadIdx.x;
+  uint32_t lid = 0u;
+  float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;
+  float C = 0.f, m_mu = 0.f, m_la = 0.f;
+  float2 L1 = make_float2(0.f, 0.f);
+  if (live) {
+    lid = __ldg(d.lid + t);
+    A = __ldg(d.dm_a + t);
+    B = __ldg(d.dm_b + t);
+    C = __ldg(d.dm_c + t);
+    if (d.tinv_mu) {
+      m_mu = __ldg(d.tinv_mu + t);
+      m_la = __ldg(d.tinv_la + t);
+    } else {
+      m_mu = __ldg(d.inv_mu + body);
+      m_la = __ldg(d.inv_la + body);
+    }
+    L1 = tp.lams[(size_t)(k + 1) * d.T + t];
+  }
+  const float4* X = tp.posts + (size_t)k * d.V;
+  for (int j = threadIdx.x; j < nv; j += kP) {
+    const int g = __ldg(d.pverts + vb + j);
+    sg[j] = g;
+    sp[j] = __ldg(X + g);
+  }
+  __syncthreads();
+  if (!live) return;
+  Tet tt;
+  tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+  tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+  tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = C;
+  int l[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    l[q] = (int)((lid >> (8 * q)) & 0xffu);
+    tt.p[q] = sp[l[q]];
+  }
+  const float s0 = c * 6.f * det9(tt.dm);  // d aD / d(1/mu) = d aH / d(1/lambda)
+  float3 g[4];
+  float2 lb;
+  float aDb, aHb;
+  residual_adjoint<kPrecise>(tt, L1, s0 * m_mu, s0 * m_la, rb_n, g, lb, aDb, aHb);
+  float4* G = adj_buf(a, dst);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int v = sg[l[q]];
+    const float cn = a.cnt[v];
+    const float ic = cn > 0.f ? 1.f / cn : 0.f;
+    red_add_v4(G + v, g[q].x, g[q].y, g[q].z, 0.f);
+    red_add_v4(a.dxbar + v, g[q].x * ic, g[q].y * ic, g[q].z * ic, 0.f);
+  }
+  const float2 l0 = a.lambar[t];
+  a.lambar[t] = make_float2(l0.x + lb.x, l0.y + lb.y);
+  a.g_mu[t] += (double)(aDb * s0);
+  a.g_la[t] += (double)(aHb * s0);
+}
+
 }  // namespace batch
 }  // namespace xpbd
 
@@ -751,6 +837,7 @@ struct Batch {
   cudaStream_t aux = nullptr;       // stop mode: kb_list beside the update
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaStream_t aux_body = nullptr;  // the same inside the body of a loop node
+  float4* tape_post = nullptr;      // taping through omega: where the update writes post-Jacobi positions
   cudaEvent_t ev_fork_body = nullptr, ev_join_body = nullptr;
   cudaGraphExec_t exec = nullptr;
   double key_frame_dt = -1, key_dt = -1;
@@ -900,6 +987,7 @@ int iteration_b(Batch* s, bool first, int par, float dt, int rec_base, cudaStrea
   u.stop = stop;
   u.use_cond = cond != nullptr;
   if (cond) u.cond = *cond;
+  u.post_out = s->tape_post;
   if (cheb) {
     if (first) kb_update<true, true><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
     else kb_update<true, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
@@ -1424,8 +1512,11 @@ int xpbd_batch_substep_tape(void* h, float dt, const xpbd_tape* tape, void* stre
   cudaStream_t st = BS(stream);
   const int K = s->prm.constraints_iter, V = s->d.V, T = s->d.T;
   Tape tp{reinterpret_cast<float4*>(tape->xs), reinterpret_cast<float2*>(tape->lams),
-          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1)};
+          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1),
+          reinterpret_cast<float4*>(tape->posts), tape->rho_in};
+  if (tp.posts && !tp.rho_in) return bfail(XPBD_ERR_INVALID_ARGUMENT, "a tape with posts needs rho_in");
   const float* g = s->prm.gravity;
+  if (tp.posts) kb_rho_copy<<<nblk(s->d.n_bodies), 256, 0, st>>>(s->d, tp.rho_in, nullptr);
   k_tape_begin<BDev><<<nblk(V), 256, 0, st>>>(s->d, tp, dt, g[0], g[1], g[2]);
   s->cur = 0;
   kb_begin<<<nblk(V), 256, 0, st>>>(s->d, dt, g[0], g[1], g[2], K);
@@ -1434,9 +1525,13 @@ int xpbd_batch_substep_tape(void* h, float dt, const xpbd_tape* tape, void* stre
     if (it == 0) B_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
     else
       B_CUDA(cudaMemcpyAsync(tp.lams + (size_t)it * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
+    s->tape_post = tp.posts ? tp.posts + (size_t)it * V : nullptr;
     const int r = iteration_b(s, it == 0, it & 1, dt, 0, st, nullptr, Fork{s->aux, s->ev_fork, s->ev_join});
+    s->tape_post = nullptr;
     if (r) return r;
   }
+  if (tp.posts)  // the multipliers after the last iteration (the residual's lambda_K)
+    B_CUDA(cudaMemcpyAsync(tp.lams + (size_t)K * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
   B_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
   kb_end<<<nblk(V), 256, 0, st>>>(s->d, s->cur, dt, s->prm.damping, 0, 0, -1);
   B_CUDA(cudaGetLastError());
@@ -1453,8 +1548,13 @@ int xpbd_batch_substep_adjoint(void* h, float dt, const xpbd_tape* tape, const x
   cudaStream_t st = BS(stream);
   const int K = s->prm.constraints_iter, V = s->d.V, T = s->d.T;
   Tape tp{reinterpret_cast<float4*>(tape->xs), reinterpret_cast<float2*>(tape->lams),
-          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1)};
+          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1),
+          reinterpret_cast<float4*>(tape->posts), tape->rho_in};
+  // through omega: the tape holds the post-Jacobi positions and the adjoint a chain state
+  const bool through_omega = tp.posts && tp.rho_in && adj->omega_state && s->prm.cheb_enable;
   Adj a;
+  a.om = through_omega ? adj->omega_state : nullptr;
+  a.om_n = om_stride(K);
   a.gx = reinterpret_cast<float4*>(adj->gx);
   a.gv = reinterpret_cast<float4*>(adj->gv);
   a.g_mu = adj->g_inv_mu;
@@ -1467,12 +1567,17 @@ int xpbd_batch_substep_adjoint(void* h, float dt, const xpbd_tape* tape, const x
   a.cnt = adj->cnt;
   B_CUDA(cudaMemsetAsync(a.lambar, 0, sizeof(float2) * T, st));
   const float e_over_dt = expf(-dt * s->prm.damping) / dt;
-  ka_end<BDev><<<nblk(V), 256, 0, st>>>(s->d, a, e_over_dt);
+  const ChainPrm cp{K, s->prm.cheb_warmup, s->prm.rho_min, s->prm.rho_max, s->prm.rho_beta};
+  ka_end<BDev><<<nblk(V), 256, 0, st>>>(s->d, tp, a, cp, e_over_dt);
   const float c = (float)(1.0 / ((double)dt * (double)dt));
   int src = 0;
   for (int k = K - 1; k >= 0; --k) {
-    if (s->prm.cheb_enable) ka_cheb<BDev, true><<<nblk(V), 256, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
-    else ka_cheb<BDev, false><<<nblk(V), 256, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
+    if (s->prm.cheb_enable) ka_cheb<BDev, true><<<nblk(V), 256, 0, st>>>(s->d, tp, a, k, s->prm.cheb_gamma, src);
+    else ka_cheb<BDev, false><<<nblk(V), 256, 0, st>>>(s->d, tp, a, k, s->prm.cheb_gamma, src);
+    if (through_omega) {
+      if (s->prm.precise_hydro) kba_residual_adj<true><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
+      else kba_residual_adj<false><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
+    }
     if (s->prm.precise_hydro) kba_project<true><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
     else kba_project<false><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
     src ^= 1;

@@ -208,6 +208,7 @@ struct UpdArgs {
   int cur_next;  // buffer holding the positions after this iteration
   int use_cond;  // set the frame graph's loop condition (cond)
   cudaGraphConditionalHandle cond;
+  float4* post_out;  // taping through omega: the post-Jacobi positions (nullptr: none)
   double inv_n;  // 1 / tet count (0 for an empty mesh)
   double rho_min, rho_max, rho_beta;
   double target, floor;  // stop at r_hat <= target * r_hat_0 or r_hat <= floor
@@ -327,6 +328,7 @@ __global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma, 
       xp.y += D[k].y / D[k].w;
       xp.z += D[k].z / D[k].w;
     }
+    if (u.post_out) u.post_out[i] = make_float4(xp.x, xp.y, xp.z, pc[k].w);
     if (kCheb) {
       const float nx = gamma * (xp.x - pc[k].x) + pc[k].x;
       const float ny = gamma * (xp.y - pc[k].y) + pc[k].y;
@@ -1163,6 +1165,10 @@ namespace xpbd {
 __device__ __forceinline__ int adj_verts(const Dev& d) { return d.V; }
 __device__ __forceinline__ int adj_tets(const Dev& d) { return d.T; }
 __device__ __forceinline__ float adj_omega(const Dev& d, int, int k) { return (float)d.hist[4 * k + 1]; }
+__device__ __forceinline__ int adj_nbodies(const Dev&) { return 1; }
+__device__ __forceinline__ int adj_vbody(const Dev&, int) { return 0; }
+__device__ __forceinline__ double adj_hist(const Dev& d, int, int k, int c) { return d.hist[4 * (size_t)k + c]; }
+__device__ __forceinline__ double adj_body_tets(const Dev& d, int) { return (double)d.T; }
 __device__ __forceinline__ bool adj_load_tet(const Dev& d, int t, int (&vid)[4], Tet& tt, float& inv_v0, float& m_mu,
                                              float& m_la) {
   int4 id;
@@ -1233,6 +1239,7 @@ struct Solver {
   int cur = 0;  // buffer holding the current predicted positions
   cudaStream_t cap = nullptr;
   cudaStream_t cap_body = nullptr;  // captures the body of a stop-mode loop node
+  float4* tape_post = nullptr;      // taping through omega: where the update writes post-Jacobi positions
   cudaGraphExec_t exec = nullptr;
   GraphKey key;
   // profiling with use_graph: the frame graph carries an event record node
@@ -1478,6 +1485,7 @@ void launch_iteration(Solver* s, bool first, int par, float dt, int rec_base, in
   u.cur_next = cheb ? s->cur ^ 1 : s->cur;
   u.use_cond = cond != nullptr;
   if (cond) u.cond = *cond;
+  u.post_out = s->tape_post;
   u.inv_n = s->d.T > 0 ? 1.0 / (double)s->d.T : 0.0;
   u.rho_min = p.rho_min;
   u.rho_max = p.rho_max;
@@ -2149,8 +2157,12 @@ int xpbd_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* strea
   cudaStream_t st = S(stream);
   const int K = s->prm.constraints_iter, V = s->d.V, T = s->d.T;
   Tape tp{reinterpret_cast<float4*>(tape->xs), reinterpret_cast<float2*>(tape->lams),
-          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1)};
+          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1),
+          reinterpret_cast<float4*>(tape->posts), tape->rho_in};
+  if (tp.posts && !tp.rho_in) return fail(XPBD_ERR_INVALID_ARGUMENT, "a tape with posts needs rho_in");
   const float* g = s->prm.gravity;
+  if (tp.posts)
+    XPBD_CUDA(cudaMemcpyAsync(tp.rho_in, &s->d.st->rho_hat, sizeof(double), cudaMemcpyDeviceToDevice, st));
   k_tape_begin<Dev><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, dt, g[0], g[1], g[2]);
   s->cur = 0;
   launch_begin(s, true, true, dt, st);
@@ -2159,8 +2171,12 @@ int xpbd_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* strea
     if (it == 0) XPBD_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
     else
       XPBD_CUDA(cudaMemcpyAsync(tp.lams + (size_t)it * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
+    s->tape_post = tp.posts ? tp.posts + (size_t)it * V : nullptr;
     launch_iteration(s, it == 0, it & 1, dt, 0, -1, st, nullptr);
+    s->tape_post = nullptr;
   }
+  if (tp.posts)  // the multipliers after the last iteration (the residual's lambda_K)
+    XPBD_CUDA(cudaMemcpyAsync(tp.lams + (size_t)K * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
   XPBD_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
   k_end<<<blocks_for(V), kBlock, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
   XPBD_CUDA(cudaGetLastError());
@@ -2177,8 +2193,13 @@ int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xp
   cudaStream_t st = S(stream);
   const int K = s->prm.constraints_iter, V = s->d.V, T = s->d.T;
   Tape tp{reinterpret_cast<float4*>(tape->xs), reinterpret_cast<float2*>(tape->lams),
-          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1)};
+          reinterpret_cast<float4*>(tape->xpre), reinterpret_cast<float4*>(tape->v1),
+          reinterpret_cast<float4*>(tape->posts), tape->rho_in};
+  // through omega: the tape holds the post-Jacobi positions and the adjoint a chain state
+  const bool through_omega = tp.posts && tp.rho_in && adj->omega_state && s->prm.cheb_enable;
   Adj a;
+  a.om = through_omega ? adj->omega_state : nullptr;
+  a.om_n = om_stride(K);
   a.gx = reinterpret_cast<float4*>(adj->gx);
   a.gv = reinterpret_cast<float4*>(adj->gv);
   a.g_mu = adj->g_inv_mu;
@@ -2191,14 +2212,20 @@ int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xp
   a.cnt = adj->cnt;
   XPBD_CUDA(cudaMemsetAsync(a.lambar, 0, sizeof(float2) * T, st));
   const float e_over_dt = expf(-dt * s->prm.damping) / dt;
-  ka_end<Dev><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, e_over_dt);
+  const ChainPrm cp{K, s->prm.cheb_warmup, s->prm.rho_min, s->prm.rho_max, s->prm.rho_beta};
+  ka_end<Dev><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, cp, e_over_dt);
   float cD, cH;
   compliance_factors(s, dt, cD, cH);
   int src = 0;
   for (int k = K - 1; k >= 0; --k) {
-    if (s->prm.cheb_enable) ka_cheb<Dev, true><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
-    else ka_cheb<Dev, false><<<blocks_for(V), kBlock, 0, st>>>(s->d, a, k, s->prm.cheb_gamma, src);
+    if (s->prm.cheb_enable)
+      ka_cheb<Dev, true><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, k, s->prm.cheb_gamma, src);
+    else ka_cheb<Dev, false><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, k, s->prm.cheb_gamma, src);
     const int g = (T + 127) / 128;
+    if (through_omega) {
+      if (s->prm.precise_hydro) ka_residual_adj<Dev, true><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
+      else ka_residual_adj<Dev, false><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
+    }
     if (s->prm.precise_hydro) ka_project<Dev, true><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
     else ka_project<Dev, false><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
     src ^= 1;

@@ -23,7 +23,7 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
 SOURCES = ["xpbd_solver.cu", "xpbd_batch.cu", "xpbd_mesh.cpp"]
 
-ABI_VERSION = 2  # XPBD_ABI_VERSION of include/xpbd_gb300.h
+ABI_VERSION = 3  # XPBD_ABI_VERSION of include/xpbd_gb300.h
 XPBD_OK = 0
 STATUS_NAMES = {
     0: "XPBD_OK", 1: "XPBD_ERR_INVALID_ARGUMENT", 2: "XPBD_ERR_CUDA",
@@ -87,12 +87,12 @@ class XpbdBatch(ctypes.Structure):
 
 
 class XpbdTape(ctypes.Structure):
-    _fields_ = [("xs", _P), ("lams", _P), ("xpre", _P), ("v1", _P)]
+    _fields_ = [("xs", _P), ("lams", _P), ("xpre", _P), ("v1", _P), ("posts", _P), ("rho_in", _P)]
 
 
 class XpbdAdjoint(ctypes.Structure):
     _fields_ = [("gx", _P), ("gv", _P), ("g_inv_mu", _P), ("g_inv_lambda", _P), ("work0", _P), ("work1", _P),
-                ("ybar", _P), ("dxbar", _P), ("lambar", _P), ("cnt", _P)]
+                ("ybar", _P), ("dxbar", _P), ("lambar", _P), ("cnt", _P), ("omega_state", _P)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/xpbd_gb300.h

@@ -16,10 +16,16 @@ once as a CUDA graph and replayed, so an optimisation loop launches two
 graphs per step.  A simulation object holds one simulation in flight: its
 backward must run before its next forward.
 
-Differentiation conventions: the Chebyshev factor omega is a stop-gradient
-(it is a control heuristic of the residual ratio, neohookean_solver.py:
-495-546); active contact sets and the 2x2 pivot branch are piecewise
-constant.
+Differentiation conventions: active contact sets and the 2x2 pivot branch
+are piecewise constant.  By default (``omega_grad=True``) the adjoint also
+runs back through the Chebyshev factor: omega_k depends on the spectral
+estimate rho_hat, which follows the residual ratio r_hat_k / r_hat_{k-1}
+(neohookean_solver.py:495-546), and r_hat on the post-Jacobi positions, the
+multipliers and the compliances (:298-329); the tape then also records the
+post-Jacobi positions of every iteration.  ``omega_grad=False`` treats omega
+as a stop-gradient, the derivative of the run with its omega schedule
+replayed: cheaper, but for a uniform Poisson ratio, which moves the whole
+residual curve, far from the derivative of the forward as it runs.
 """
 import numpy as np
 
@@ -98,7 +104,7 @@ class DiffSim:
 
     n_rho = 1
 
-    def __init__(self, rest_pose, sdf, log_E, nu, scatter="atomic", use_graphs=True, **kw):
+    def __init__(self, rest_pose, sdf, log_E, nu, scatter="atomic", use_graphs=True, omega_grad=True, **kw):
         kw.setdefault("block_neohookean_enable", True)
         if not kw["block_neohookean_enable"]:
             raise ValueError("the adjoint supports the block projection only")
@@ -111,27 +117,52 @@ class DiffSim:
         dev = s._device
         V, T, K = s.n_verts, s.n_tets, s.constraints_iter
         self.V, self.T, self.K = V, T, K
+        self._alloc_adjoint_buffers(V, T, K, 1, dev, omega_grad)
+        cnt = np.bincount(s._tets_solver.reshape(-1), minlength=V).astype(np.float32)
+        self._cnt = torch.from_numpy(cnt).to(dev)
+        self._vperm = torch.as_tensor(s._vperm, dtype=torch.int64, device=dev)
+        self._tperm = torch.as_tensor(s._tperm, dtype=torch.int64, device=dev)
+        self._bind()
+        self.initial_rho_hat = s.rho_hat
+        self.use_graphs = bool(use_graphs)
+
+    def _alloc_adjoint_buffers(self, V, T, K, n_bodies, dev, omega_grad):
+        """Tape and adjoint buffers; with omega_grad the tape also keeps the
+        post-Jacobi positions, the multipliers after the last iteration and the
+        rho_hat entering the substep, and the adjoint a chain state per body."""
+        torch = _torch()
         f4 = lambda n: torch.zeros((n, 4), dtype=torch.float32, device=dev)
+        self.omega_grad = bool(omega_grad)
         self._xs = torch.zeros(((K + 1) * V, 4), dtype=torch.float32, device=dev)
-        self._lams = torch.zeros((max(K, 1) * T, 2), dtype=torch.float32, device=dev)
+        self._lams = torch.zeros(((K + 1 if omega_grad else max(K, 1)) * T, 2), dtype=torch.float32, device=dev)
         self._xpre, self._v1 = f4(V), f4(V)
         self._gx, self._gv = f4(V), f4(V)
         self._w0, self._w1, self._yb, self._dxb = f4(V), f4(V), f4(V), f4(V)
         self._lamb = torch.zeros((T, 2), dtype=torch.float32, device=dev)
         self._gmu = torch.zeros(T, dtype=torch.float64, device=dev)
         self._gla = torch.zeros(T, dtype=torch.float64, device=dev)
-        cnt = np.bincount(s._tets_solver.reshape(-1), minlength=V).astype(np.float32)
-        self._cnt = torch.from_numpy(cnt).to(dev)
-        self._vperm = torch.as_tensor(s._vperm, dtype=torch.int64, device=dev)
-        self._tperm = torch.as_tensor(s._tperm, dtype=torch.int64, device=dev)
+        self._posts = f4(K * V) if omega_grad else None
+        self._rho_in = torch.zeros(n_bodies, dtype=torch.float64, device=dev) if omega_grad else None
+        self._om = (torch.zeros((n_bodies, 8 + 6 * K), dtype=torch.float64, device=dev) if omega_grad
+                    else None)
+
+    def _bind(self):
+        ptr = lambda t: t.data_ptr() if t is not None else None
         self.tape = _native.XpbdTape(self._xs.data_ptr(), self._lams.data_ptr(), self._xpre.data_ptr(),
-                                     self._v1.data_ptr())
+                                     self._v1.data_ptr(), ptr(self._posts), ptr(self._rho_in))
         self.adj = _native.XpbdAdjoint(self._gx.data_ptr(), self._gv.data_ptr(), self._gmu.data_ptr(),
                                        self._gla.data_ptr(), self._w0.data_ptr(), self._w1.data_ptr(),
                                        self._yb.data_ptr(), self._dxb.data_ptr(), self._lamb.data_ptr(),
-                                       self._cnt.data_ptr())
-        self.initial_rho_hat = s.rho_hat
-        self.use_graphs = bool(use_graphs)
+                                       self._cnt.data_ptr(), ptr(self._om))
+
+    def reset_adjoint(self):
+        """Zero what a backward pass accumulates (the omega chain included)."""
+        self._gx.zero_()
+        self._gv.zero_()
+        self._gmu.zero_()
+        self._gla.zero_()
+        if self._om is not None:
+            self._om.zero_()
 
     # -- the steps of a plan ---------------------------------------------------
     def _state(self):
@@ -196,11 +227,8 @@ class _Simulate(_torch().autograd.Function):
         torch = _torch()
         sim = ctx.sim
         log_E, nu = ctx.saved_tensors
-        sim._gx.zero_()
-        sim._gv.zero_()
+        sim.reset_adjoint()
         sim._gx[:, :3] = g_out.to(torch.float32)[sim._vperm]
-        sim._gmu.zero_()
-        sim._gla.zero_()
         ctx.plan.backward(sim, ctx.generation)
         gx = torch.empty((sim.V, 3), dtype=torch.float32, device=g_out.device)
         gv = torch.empty_like(gx)
@@ -247,7 +275,7 @@ class BatchedDiffSim:
     its own Chebyshev state, so the gradients of each body equal those of the
     same body simulated alone."""
 
-    def __init__(self, bodies, sdf, use_graphs=True, **kw):
+    def __init__(self, bodies, sdf, use_graphs=True, omega_grad=True, **kw):
         from xpbd_gpu.batched import Body, XPBDBatchedSolver
         kw.setdefault("block_neohookean_enable", True)
         if not kw["block_neohookean_enable"]:
@@ -262,21 +290,9 @@ class BatchedDiffSim:
         V, T, K = s.n_verts_padded, s.n_tets_padded, s.constraints_iter
         self.V, self.T, self.K = V, T, K
         self.n_verts, self.n_tets = s.n_verts, s.n_tets
-        f4 = lambda n: torch.zeros((n, 4), dtype=torch.float32, device=dev)
-        self._xs = torch.zeros(((K + 1) * V, 4), dtype=torch.float32, device=dev)
-        self._lams = torch.zeros((max(K, 1) * T, 2), dtype=torch.float32, device=dev)
-        self._xpre, self._v1 = f4(V), f4(V)
-        self._gx, self._gv = f4(V), f4(V)
-        self._w0, self._w1, self._yb, self._dxb = f4(V), f4(V), f4(V), f4(V)
-        self._lamb = torch.zeros((T, 2), dtype=torch.float32, device=dev)
-        self._gmu = torch.zeros(T, dtype=torch.float64, device=dev)
-        self._gla = torch.zeros(T, dtype=torch.float64, device=dev)
-        self.tape = _native.XpbdTape(self._xs.data_ptr(), self._lams.data_ptr(), self._xpre.data_ptr(),
-                                     self._v1.data_ptr())
-        self.adj = _native.XpbdAdjoint(self._gx.data_ptr(), self._gv.data_ptr(), self._gmu.data_ptr(),
-                                       self._gla.data_ptr(), self._w0.data_ptr(), self._w1.data_ptr(),
-                                       self._yb.data_ptr(), self._dxb.data_ptr(), self._lamb.data_ptr(),
-                                       s._cnt.data_ptr())
+        DiffSim._alloc_adjoint_buffers(self, V, T, K, s.n_bodies, dev, omega_grad)
+        self._cnt = s._cnt
+        DiffSim._bind(self)
         self.initial_rho_hat = torch.empty(s.n_bodies, dtype=torch.float64, device=dev)
         self.rho_copy_to(self.initial_rho_hat)
         self.n_rho = s.n_bodies
@@ -349,11 +365,8 @@ class _SimulateBatch(_torch().autograd.Function):
         sim = ctx.sim
         log_E, nu = ctx.saved_tensors
         s = sim.batch
-        sim._gx.zero_()
-        sim._gv.zero_()
+        DiffSim.reset_adjoint(sim)
         sim._gx[s._vert_slot, :3] = g_out.to(torch.float32)
-        sim._gmu.zero_()
-        sim._gla.zero_()
         ctx.plan.backward(sim, ctx.generation)
         gx = sim._gx[s._vert_slot, :3].clone()
         gv = sim._gv[s._vert_slot, :3].clone()

@@ -85,14 +85,19 @@ def _fd_task(task):
     return kind, k, replay, (vals[0] - vals[1]) / (2 * H)
 
 
-def test_c4_size_adjoint_against_central_differences():
+def _adjoint(s, omega_grad):
     from oracle.xpbd_adjoint import DiffOracle, lame_inverse, lame_inverse_grad
-    s = _scene()
     im, il = lame_inverse(s["log_E"], s["nu"])
-    o = DiffOracle(s["points"], s["tets"], s["sdfs"], im, il, **s["okw"])
+    o = DiffOracle(s["points"], s["tets"], s["sdfs"], im, il, omega_grad=omega_grad, **s["okw"])
     oms, xb, vb, gm, gl, _ = o.gradient(s["x0"], s["v0"], 1, s["c"])
     g_logE, g_nu = lame_inverse_grad(s["log_E"], np.full(len(s["log_E"]), s["nu"]), gm, gl)
-    grads = {"log_E": g_logE, "nu": float(g_nu.sum()), "v0": vb}
+    return oms, {"log_E": g_logE, "nu": float(g_nu.sum()), "v0": vb}
+
+
+def test_c4_size_adjoint_against_central_differences():
+    s = _scene()
+    oms, grads = _adjoint(s, False)
+    _, grads_om = _adjoint(s, True)
     tasks = [("log_E", k, True) for k in range(N_DIR)] + [("v0", k, True) for k in range(N_DIR)]
     tasks += [("nu", 0, True), ("nu", 0, False)]
     tasks += [("log_E", k, False) for k in range(N_DIR_OMEGA)] + [("v0", k, False) for k in range(N_DIR_OMEGA)]
@@ -104,14 +109,15 @@ def test_c4_size_adjoint_against_central_differences():
         for kind in ("log_E", "v0", "nu"):
             rows = [(k, fd) for kd, k, rp, fd in results if kd == kind and rp == replay]
             fd = np.array([r[1] for r in rows])
-            an = np.array([float(np.sum(grads[kind] * _direction(kind, k, np.shape(grads[kind]))))
-                           if kind != "nu" else grads[kind] * float(_direction(kind, k, ())) for k, _ in rows])
             rms = float(np.sqrt(np.mean(fd ** 2)))
-            report[(kind, replay)] = float(np.max(np.abs(fd - an))) / rms
-    print("max |FD - adjoint| / RMS(FD):", {"%s/%s" % (k, "replayed" if r else "recomputed"): "%.2e" % v
-                                            for (k, r), v in report.items()})
+            for label, g in (("stop", grads), ("through_omega", grads_om)):
+                an = np.array([float(np.sum(g[kind] * _direction(kind, k, np.shape(g[kind]))))
+                               if kind != "nu" else g[kind] * float(_direction(kind, k, ())) for k, _ in rows])
+                report[(kind, replay, label)] = float(np.max(np.abs(fd - an))) / rms
+    print("max |FD - adjoint| / RMS(FD):", {"%s/%s/%s" % (k, "replayed" if r else "recomputed", lb): "%.2e" % v
+                                            for (k, r, lb), v in report.items()})
     for kind in ("log_E", "v0", "nu"):
-        assert report[(kind, True)] <= 1e-3, (kind, report[(kind, True)])
-    for kind in ("log_E", "v0"):
-        assert report[(kind, False)] <= 1e-2, (kind, report[(kind, False)])
-    assert np.isfinite(report[("nu", False)])
+        # the stop-gradient adjoint is the derivative of the omega-replayed function
+        assert report[(kind, True, "stop")] <= 1e-3, (kind, report[(kind, True, "stop")])
+        # through omega, the adjoint is the derivative of the forward as it runs
+        assert report[(kind, False, "through_omega")] <= 1e-3, (kind, report[(kind, False, "through_omega")])

@@ -5,7 +5,9 @@ differences in tests/test_adjoint_oracle.py; here the GPU gradients of a
 linear loss on the final positions w.r.t. per-tet log E, nu, the initial
 positions and velocities must match it within 1e-3 relative (L2 norm of the
 difference over the norm of the gradient), on a body with plane, sphere and
-moving-box contact.
+moving-box contact: with the adjoint run back through the Chebyshev omega
+(omega_grad, the derivative of the forward as it runs) and with omega as a
+stop-gradient.
 """
 import numpy as np
 import pytest
@@ -17,8 +19,8 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-@pytest.mark.parametrize("cheb", [True, False])
-def test_gpu_gradients_match_float64_adjoint(cheb):
+@pytest.mark.parametrize("cheb,omega_grad", [(True, True), (True, False), (False, False)])
+def test_gpu_gradients_match_float64_adjoint(cheb, omega_grad):
     import torch
     from oracle.xpbd_adjoint import DiffOracle, lame_inverse, lame_inverse_grad
     from oracle.xpbd_oracle import OracleSdf
@@ -39,12 +41,12 @@ def test_gpu_gradients_match_float64_adjoint(cheb):
                    [OracleSdf("plane", point=[0, 0, 0], dir=[0, 1, 0], fixed=True),
                     OracleSdf("sphere", center=[0.42, -0.18, 0.42], radius=0.2, fixed=True),
                     OracleSdf("cube", center=[0.5, 0.0, 0.5], size=[0.1, 0.03, 0.2], fixed=False)],
-                   *lame_inverse(logE, nu), **kw)
+                   *lame_inverse(logE, nu), omega_grad=omega_grad, **kw)
     _, xb, vb, gm, gl, xe64 = o.gradient(m.points.copy(), v0, frames, c)
     g_logE64, g_nu64 = lame_inverse_grad(logE, nu, gm, gl)
 
     sim = DiffSim(m, [PlaneSdf([0, 0, 0], [0, 1, 0], True), SphereSdf([0.42, -0.18, 0.42], 0.2, True),
-                      CubeSdf([0.5, 0.0, 0.5], [0.1, 0.03, 0.2], False)], logE, nu, **kw)
+                      CubeSdf([0.5, 0.0, 0.5], [0.1, 0.03, 0.2], False)], logE, nu, omega_grad=omega_grad, **kw)
     dev = torch.device("cuda")
     x0_t = torch.tensor(m.points, dtype=torch.float32, device=dev, requires_grad=True)
     v0_t = torch.tensor(v0, dtype=torch.float32, device=dev, requires_grad=True)

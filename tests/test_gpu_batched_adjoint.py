@@ -5,7 +5,8 @@ Three bodies of different sizes and per-tet materials are simulated as one
 batch; the gradients of a linear loss on all final positions w.r.t. every
 tet's log E and nu and every vertex's initial position and velocity must match
 the float64 adjoint of each body simulated alone (oracle/xpbd_adjoint.py,
-itself checked against central finite differences) within 1e-3 relative (L2
+itself checked against central finite differences), through omega and with
+omega as a stop-gradient, within 1e-3 relative (L2
 norm of the difference over the norm of the gradient).  The forward positions
 must match the float64 forward within 1e-4 of each body's bounding-box
 diagonal.
@@ -27,8 +28,8 @@ def _bodies():
             kuhn_grid(4, 2, 3, 0.06, origin=(0.32, 0.01, 0.3), jitter=0.1, seed=6)]
 
 
-@pytest.mark.parametrize("cheb", [True, False])
-def test_batched_gradients_match_float64_adjoint(cheb):
+@pytest.mark.parametrize("cheb,omega_grad", [(True, True), (True, False), (False, False)])
+def test_batched_gradients_match_float64_adjoint(cheb, omega_grad):
     import torch
     from oracle.xpbd_adjoint import DiffOracle, lame_inverse, lame_inverse_grad
     from oracle.xpbd_oracle import OracleSdf
@@ -51,7 +52,7 @@ def test_batched_gradients_match_float64_adjoint(cheb):
         v = rng.normal(size=m.points.shape) * 0.05
         cc = rng.normal(size=m.points.shape)
         o = DiffOracle(m.points, m.tets, [OracleSdf(k, **p) for k, p in specs], *lame_inverse(le, n),
-                       total_mass=1.0, **kw)
+                       total_mass=1.0, omega_grad=omega_grad, **kw)
         _, xb, vb, gm, gl, xe64 = o.gradient(m.points.copy(), v, frames, cc)
         g_le, g_nu = lame_inverse_grad(le, n, gm, gl)
         logE.append(le)
@@ -63,7 +64,7 @@ def test_batched_gradients_match_float64_adjoint(cheb):
             CubeSdf([0.5, 0.0, 0.5], [0.1, 0.03, 0.2], False)]
     bodies = [Body(m, tet_young_modulus=np.exp(le), tet_poisson_ratio=n, total_mass=1.0)
               for m, le, n in zip(meshes, logE, nu)]
-    sim = BatchedDiffSim(bodies, sdfs, **kw)
+    sim = BatchedDiffSim(bodies, sdfs, omega_grad=omega_grad, **kw)
     dev = torch.device("cuda")
     x0_t = torch.tensor(np.concatenate([m.points for m in meshes]), dtype=torch.float32, device=dev,
                         requires_grad=True)
