@@ -141,6 +141,36 @@ def run_c4(args):
     print(json.dumps(c4_block(args)), flush=True)
 
 
+def plain_forward_ms(sim, simulate, x0, v0, log_E, nu, frames, reps):
+    """Mean device time of the forward alone, without tapes (the recompute
+    plan: one CUDA graph of per-substep state checkpoints and plain substeps)."""
+    import torch
+    mode = sim.tape_memory
+    sim.tape_memory = "recompute"
+    out = []
+    with torch.no_grad():
+        for k in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            simulate(sim, x0, v0, log_E.detach(), nu.detach(), frames)
+            b.record()
+            b.synchronize()
+            if k:
+                out.append(a.elapsed_time(b))
+    sim.tape_memory = mode
+    return float(np.mean(out))
+
+
+def tape_note(sim, frames):
+    from xpbd_gpu.differentiable import _plan
+    p = _plan(sim, frames)
+    if p.stored:
+        return ("stored: the forward records every substep's tape (%.1f GB), the backward reverses them"
+                % (sum(t.numel() * t.element_size() for t in vars(p.tapes).values()
+                       if hasattr(t, "numel")) / 1e9))
+    return "recomputed: the backward restores each substep's checkpoint and re-runs it on a tape"
+
+
 def c4_block(args):
     """Differentiable single body: forward (checkpointed) vs adjoint cost, gradient checks."""
     import torch
@@ -181,6 +211,7 @@ def c4_block(args):
             bwd.append(t2 - t1)
     fwd_ms, bwd_ms = 1e3 * float(np.mean(fwd)), 1e3 * float(np.mean(bwd))
     units = T * frames * kw["substeps_num"] * kw["constraints_iter"]
+    plain_fwd_ms = plain_forward_ms(sim, xpbd_simulate, x0, v0, le, nu_t, frames, args.c4_reps)
 
     # gradient check on a short horizon that starts in contact (after c4_check_start
     # frames of the forward), against the FD-checked float64 adjoint
@@ -223,9 +254,10 @@ def c4_block(args):
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": desc, "step": "forward of %d frames with per-substep checkpoints" % frames},
             "adjoint": {"backward_ms": bwd_ms, "backward_over_forward": bwd_ms / fwd_ms,
+                        "plain_forward_ms": plain_fwd_ms, "backward_over_plain_forward": bwd_ms / plain_fwd_ms,
                         "omega": "through omega (omega -> rho_hat -> r_hat adjoint)" if sim.omega_grad
                         else "stop-gradient",
-                        "note": "backward = per-substep tape recompute + reverse kernels"},
+                        "tapes": tape_note(sim, frames)},
             "gradient_check": {"start_frame": args.c4_check_start, "horizon_frames": hf, "directions": 32,
                                "reference": "float64 adjoint (oracle/xpbd_adjoint.py, itself checked against "
                                             "central finite differences), started from the GPU state",
@@ -320,6 +352,7 @@ def c5_block(args, steps, plain_accuracy_bodies=4, plain_timing_steps=2, fp64_bo
         bwd_ms.append(e1.elapsed_time(e2))
         losses.append(float(loss))
     sim.batch.check_status()
+    plain_fwd_ms = plain_forward_ms(sim, xpbd_simulate_batch, x0, v0, theta, nu_t, frames, 3)
     th = theta.detach().cpu().numpy()
     errs = [per_body_rel_err(th[offs[k]:offs[k + 1]], le_true[offs[k]:offs[k + 1]], le0[offs[k]:offs[k + 1]])
             for k in range(nb)]
@@ -380,6 +413,9 @@ def c5_block(args, steps, plain_accuracy_bodies=4, plain_timing_steps=2, fp64_bo
                                "CUDA graph)"},
             "forward_ms": float(np.mean(np.asarray(fwd_ms)[sl])), "backward_ms": float(np.mean(np.asarray(bwd_ms)[sl])),
             "backward_over_forward": float(np.mean(np.asarray(bwd_ms)[sl]) / np.mean(np.asarray(fwd_ms)[sl])),
+            "plain_forward_ms": plain_fwd_ms,
+            "backward_over_plain_forward": float(np.mean(np.asarray(bwd_ms)[sl]) / plain_fwd_ms),
+            "tapes": tape_note(sim, frames),
             "adam": {"steps": steps, "lr": lr, "init": "log E = log 1e5 everywhere",
                      "loss_first_last": [losses[0], losses[-1]],
                      "recovered_rel_err_median": float(np.median(errs)),
@@ -1286,7 +1322,8 @@ def run_profile(args):
         meshes, log_E, nus, specs, kw, desc = workload_c5()
         bodies = [Body(m, tet_young_modulus=np.exp(log_E[k]), tet_poisson_ratio=nus[k], density=1000.0,
                        poisson_ratio=float(nus[k])) for k, m in enumerate(meshes)]
-        sim = BatchedDiffSim(bodies, product_sdfs(specs), use_graphs=False, **kw)
+        sim = BatchedDiffSim(bodies, product_sdfs(specs), use_graphs=False, tape_memory=args.profile_tape_memory,
+                             **kw)
         dev = torch.device("cuda")
         x0 = torch.tensor(np.concatenate([m.points for m in meshes]), dtype=torch.float32, device=dev)
         le = torch.tensor(np.concatenate(log_E), dtype=torch.float64, device=dev, requires_grad=True)
@@ -1352,6 +1389,8 @@ def main():
     ap.add_argument("--profile-frames", type=int, default=1)
     ap.add_argument("--profile-settle", type=int, default=0, help="c3 profile mode: frames stepped first (graphs)")
     ap.add_argument("--profile-stop", type=int, default=0, choices=[0, 1], help="c3 profile mode: stop-mode frames")
+    ap.add_argument("--profile-tape-memory", default="auto", choices=["auto", "store", "recompute"],
+                    help="c5 profile mode: tapes stored by the forward or recomputed by the backward")
     args = ap.parse_args()
     if args.mode == "profile":
         run_profile(args)

@@ -286,6 +286,11 @@ typedef struct xpbd_tape {
   float* posts;   /* [K][V][4] post-Jacobi positions of every iteration, or NULL
                      (omega then is a stop-gradient) */
   double* rho_in; /* [bodies] rho_hat entering the substep (with posts) */
+  double* hist;   /* [bodies][K][4] the substep's history rows (r_hat, omega,
+                     ...), copied by the tape call, or NULL: the adjoint then
+                     reads the solver's own rows 0..K-1, which the next
+                     substep overwrites.  With it, the tapes of many substeps
+                     can be recorded in the forward and reversed later. */
 } xpbd_tape;
 
 typedef struct xpbd_adjoint {
@@ -304,6 +309,8 @@ typedef struct xpbd_adjoint {
                            stop-gradient); zero it before the first substep
                            adjoint of a backward pass (it carries the adjoint of
                            rho_hat, which persists across substeps, backwards) */
+  float* work_res_tet;  /* [T][4] scratch of the batched omega chain (NULL for a
+                           single body) */
 } xpbd_adjoint;
 
 /* One substep (as xpbd_substep) that records `tape`; history rows [0, K)

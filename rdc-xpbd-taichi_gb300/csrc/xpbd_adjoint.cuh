@@ -16,8 +16,8 @@
 // the derivative of the 2x2 solve is that of A^-1 b.  Omega is a
 // stop-gradient unless the tape holds the post-Jacobi positions (Tape::posts)
 // and the adjoint an omega state (Adj::om): then
-//     ka_end           also replays the substep's rho_hat curve into a table of
-//                      per-iteration chain coefficients (FP64, one thread per
+//     ka_chain         replays the substep's rho_hat curve into a table of
+//                      per-iteration chain coefficients (FP64, one warp per
 //                      body; neohookean_solver.py:495-504, :537-546)
 //     ka_cheb          also sums omega_k's adjoint over the vertices
 // and, between ka_cheb and the tet adjoint of each iteration,
@@ -80,12 +80,18 @@ struct Adj {
   const float* cnt;  // [V] constraints per vertex (valence in block mode)
   double* om;        // [bodies][om_stride(K)] omega chain state; nullptr: omega is a stop-gradient
   int om_n;          // om_stride(K)
+  // Batched layout with the omega chain: [T] the residual adjoint's multiplier
+  // and material parts (lambda_{k+1}, 1/mu, 1/lambda) of every tet, read by the
+  // tet adjoint.  nullptr in the single-body layout, whose residual adjoint
+  // adds them in place.
+  float4* rtet;
 };
 
 __device__ __forceinline__ float3 f3(const float4 a) { return make_float3(a.x, a.y, a.z); }
 // abuf[k] for a run-time k without indexing the kernel-parameter array (which
 // would copy the whole Adj parameter block to local memory)
 __device__ __forceinline__ float4* adj_buf(const Adj& a, int k) { return k ? a.abuf[1] : a.abuf[0]; }
+
 __device__ __forceinline__ float3 cross3(const float3 a, const float3 b) {
   return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
@@ -106,65 +112,91 @@ __global__ void __launch_bounds__(256) k_tape_begin(D d, Tape tp, float dt, floa
   tp.xpre[i] = make_float4(xi.x + vi.x * dt, xi.y + vi.y * dt, xi.z + vi.z * dt, xi.w);
 }
 
-// Reverse of advance: live vertices x' = x~_K, v' = (x~_K - x) e / dt; pinned
-// vertices keep x and v.
-// With the omega chain, block 0 also starts the chain state of the substep's
-// last iteration and tabulates its coefficients (ChainPrm).
 struct ChainPrm {
   int K, warmup;
   double rho_min, rho_max, beta;
 };
 
+// Start of the omega chain of a substep (one warp per body): carries the
+// adjoint of rho_hat over from the later substep, clears the other state and
+// tabulates the coefficients of every iteration.  Lane j takes iteration j
+// (32 at a time): the ratio r_hat_j / r_hat_{j-1}, its clamp and the rho_hat
+// update are independent per iteration except for rho_hat_j = a_j rho_hat_{j-1}
+// + b_j, which is an inclusive scan of affine maps across the lanes.
 template <class D>
-__device__ void chain_table(const D& d, const Tape& tp, const Adj& a, const ChainPrm& c, int b) {
+__global__ void __launch_bounds__(256) ka_chain(D d, Tape tp, Adj a, ChainPrm c) {
+  const int b = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (b >= adj_nbodies(d)) return;  // warp-uniform
+  const unsigned full = 0xffffffffu;
   double* o = a.om + (size_t)a.om_n * b;
-  const int q = (c.K - 1) & 1;
-  // the adjoint of rho_hat entering the later substep (written by its iteration
-  // 0 into slot 1) is that of rho_hat leaving this one
-  o[kRhoBar + q] = o[kRhoBar + 1];
-  o[kOmSum] = o[kOmSum + 1] = o[kOmCarry] = o[kOmCarry + 1] = o[kRCarry] = o[kRCarry + 1] = 0.0;
-  double rho = tp.rho_in[b], prev = 0.0;
-  for (int j = 0; j < c.K; ++j) {
-    const double r = adj_hist(d, b, j, 0);
-    const double om = adj_hist(d, b, j, 1);
-    const bool upd = j > 0 && prev > 1e-12;
-    double c1 = 0.0, c2 = 0.0;
+  if (lane == 0) {
+    // the adjoint of rho_hat entering the later substep (written by its
+    // iteration 0 into slot 1) is that of rho_hat leaving this one
+    o[kRhoBar + ((c.K - 1) & 1)] = o[kRhoBar + 1];
+    o[kOmSum] = o[kOmSum + 1] = o[kOmCarry] = o[kOmCarry + 1] = o[kRCarry] = o[kRCarry + 1] = 0.0;
+  }
+  double rho_prev = tp.rho_in[b];
+  for (int j0 = 0; j0 < c.K; j0 += 32) {
+    const int j = j0 + lane;
+    const bool in = j < c.K;
+    double r = 0.0, prev = 0.0, om = 1.0, om_prev = 1.0;
+    if (in) {
+      r = adj_hist(d, b, j, 0);
+      om = adj_hist(d, b, j, 1);
+      if (j > 0) {
+        prev = adj_hist(d, b, j - 1, 0);
+        om_prev = adj_hist(d, b, j - 1, 1);
+      }
+    }
+    const bool upd = in && j > 0 && prev > 1e-12;
+    double ri = 0.0, c1 = 0.0, c2 = 0.0;
     if (upd) {
       const double dd = prev + 1e-12;
       const double ratio = r / dd;
-      const double ri = fmax(c.rho_min, fmin(c.rho_max, ratio));
+      ri = fmax(c.rho_min, fmin(c.rho_max, ratio));
       if (ri == ratio) {
         c1 = 1.0 / dd;
         c2 = -ratio / dd;
       }
-      rho = (1.0 - c.beta) * rho + c.beta * ri;
     }
+    double ma = upd ? 1.0 - c.beta : 1.0, mb = upd ? c.beta * ri : 0.0;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const double pa = __shfl_up_sync(full, ma, off), pb = __shfl_up_sync(full, mb, off);
+      if (lane >= off) {
+        mb = ma * pb + mb;
+        ma = ma * pa;
+      }
+    }
+    const double rho = ma * rho_prev + mb;
+    rho_prev = __shfl_sync(full, rho, 31);
     double A = 0.0, B = 0.0;
     if (j == c.warmup) {
       const double den = 2.0 - rho * rho;
       A = 4.0 * rho / (den * den);
     } else if (j > c.warmup) {
-      const double om_prev = adj_hist(d, b, j - 1, 1);
       const double den = 4.0 - rho * rho * om_prev;
       A = 8.0 * rho * om_prev / (den * den);
       B = 4.0 * rho * rho / (den * den);
     }
-    double* t = o + kTab + kTabRow * j;
-    t[0] = 1.0 / om;
-    t[1] = A;
-    t[2] = B;
-    t[3] = upd ? c.beta : 0.0;
-    t[4] = c1;
-    t[5] = c2;
-    prev = r;
+    if (in) {
+      double* t = o + kTab + kTabRow * j;
+      t[0] = 1.0 / om;
+      t[1] = A;
+      t[2] = B;
+      t[3] = upd ? c.beta : 0.0;
+      t[4] = c1;
+      t[5] = c2;
+    }
   }
 }
 
+// Reverse of advance: live vertices x' = x~_K, v' = (x~_K - x) e / dt; pinned
+// vertices keep x and v.
 template <class D>
-__global__ void __launch_bounds__(256) ka_end(D d, Tape tp, Adj a, ChainPrm cp, float e_over_dt) {
+__global__ void __launch_bounds__(256) ka_end(D d, Adj a, float e_over_dt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a.om && blockIdx.x == 0)
-    for (int b = threadIdx.x; b < adj_nbodies(d); b += blockDim.x) chain_table(d, tp, a, cp, b);
   if (i >= adj_verts(d)) return;
   const float4 gx = a.gx[i], gv = a.gv[i];
   if (d.x[i].w > 0.f) {
@@ -185,6 +217,7 @@ __global__ void __launch_bounds__(256) ka_end(D d, Tape tp, Adj a, ChainPrm cp, 
 template <class D, bool kCheb>
 __global__ void __launch_bounds__(256) ka_cheb(D d, Tape tp, Adj a, int k, float gamma, int src) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const float4 xb = i < adj_verts(d) ? adj_buf(a, src)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   if (kCheb && a.om) {
     // omega_k's adjoint: sum over the vertices of x~bar_{k+1} . (xn - y_prev),
     // with xn - y_prev = (x~_{k+1} - y_prev) / omega_k (divided in chain_step).  A
@@ -193,7 +226,6 @@ __global__ void __launch_bounds__(256) ka_cheb(D d, Tape tp, Adj a, int k, float
     float part = 0.f;
     if (i < adj_verts(d)) {
       const size_t V = (size_t)adj_verts(d);
-      const float4 xb = adj_buf(a, src)[i];
       const float4 x1 = tp.xs[(size_t)(k + 1) * V + i], y = tp.xs[(size_t)(k > 0 ? k - 1 : 0) * V + i];
       part = xb.x * (x1.x - y.x) + xb.y * (x1.y - y.y) + xb.z * (x1.z - y.z);
     }
@@ -210,7 +242,6 @@ __global__ void __launch_bounds__(256) ka_cheb(D d, Tape tp, Adj a, int k, float
     }
   }
   if (i >= adj_verts(d)) return;
-  const float4 xb = adj_buf(a, src)[i];
   float3 post, cur, yn;
   if (kCheb) {
     const float om = adj_omega(d, i, k);

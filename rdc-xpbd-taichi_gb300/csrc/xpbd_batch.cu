@@ -645,11 +645,59 @@ __device__ __forceinline__ double adj_body_tets(const BDev& d, int b) { return (
 namespace xpbd {
 namespace batch {
 
+// Scatters a tet's four corner vectors g into acc (global vertex ids through
+// the patch map sg) with red.global.add.v4.  Thread 2u holds tet 2u of the
+// patch and thread 2u + 1 tet 2u + 1; when the two share a face in the
+// xpbd_pair_tets layout (corners 0, 1, 2 of the odd tet are corners 1, 0, 2
+// of the even one, recognised from the packed patch-local ids) the even
+// thread adds the three shared corners and the odd one flushes only its
+// corner 3: 5 reductions per pair instead of 8.  With acc2, each vector also
+// goes there divided by its vertex's cnt.  Every thread of the warp calls it
+// (padding threads with live = false).
+__device__ __forceinline__ void scatter_corners(bool paired, bool live, uint32_t lid, float3 (&g)[4],
+                                                const int* sg, float4* acc, float4* acc2 = nullptr,
+                                                const float* cnt = nullptr) {
+  bool merge = false;
+  const bool odd = threadIdx.x & 1u;
+  if (paired) {
+    const unsigned full = 0xffffffffu;
+    const uint32_t lid_p = __shfl_xor_sync(full, lid, 1);
+    const bool live_p = __shfl_xor_sync(full, (int)live, 1) != 0;
+    float3 h[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      h[q].x = __shfl_xor_sync(full, g[q].x, 1);
+      h[q].y = __shfl_xor_sync(full, g[q].y, 1);
+      h[q].z = __shfl_xor_sync(full, g[q].z, 1);
+    }
+    const uint32_t le = odd ? lid_p : lid, lo = odd ? lid : lid_p;
+    merge = live && live_p && (lo & 0xffffffu) == (__byte_perm(le, 0u, 0x3201u) & 0xffffffu);
+    if (merge && !odd) {
+      g[0].x += h[1].x; g[0].y += h[1].y; g[0].z += h[1].z;
+      g[1].x += h[0].x; g[1].y += h[0].y; g[1].z += h[0].z;
+      g[2].x += h[2].x; g[2].y += h[2].y; g[2].z += h[2].z;
+    }
+  }
+  if (!live) return;
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (!(merge && odd) || q == 3) {
+      const int v = sg[(lid >> (8 * q)) & 0xffu];
+      red_add_v4(acc + v, g[q].x, g[q].y, g[q].z, 0.f);
+      if (acc2) {
+        const float cn = cnt[v];
+        const float ic = cn > 0.f ? 1.f / cn : 0.f;
+        red_add_v4(acc2 + v, g[q].x * ic, g[q].y * ic, g[q].z * ic, 0.f);
+      }
+    }
+}
+
 // Reverse of the batched block projection of iteration k, one CTA per 256-tet
 // patch: the patch's positions entering the iteration (from the tape) and its
 // vertices' accumulator adjoints are staged in shared memory once, then each
 // thread reverses one tet (tet_adjoint) and scatters its corner adjoints into
-// abuf[dst] with red.global.add.v4.  c = 1 / dt^2; the tet's compliances are
+// abuf[dst] (scatter_corners).  With the omega chain each tet adds the
+// residual's multiplier and material parts (rtet).  c = 1 / dt^2; the tet's compliances are
 // c / V0 times its (or its body's) 1 / mu and 1 / lambda.  Compiled for 3
 // resident CTAs per SM (80 registers; the tet adjoint alone wants 96, which
 // allows only 2 CTAs and leaves the staging latency exposed).
@@ -685,6 +733,11 @@ __global__ void __launch_bounds__(kP, 3) kba_project(BDev d, Tape tp, Adj a, int
     L = tp.lams[(size_t)k * d.T + t];
     lb_next = a.lambar[t];
   }
+  if (a.rtet && live) {  // rtet[t] = (lambda_{k+1} adjoint, material adjoints)
+    const float2 r = reinterpret_cast<const float2*>(a.rtet + t)[0];
+    lb_next.x += r.x;
+    lb_next.y += r.y;
+  }
   const float4* X = tp.xs + (size_t)k * d.V;
   for (int j = threadIdx.x; j < nv; j += kP) {
     const int g = __ldg(d.pverts + vb + j);
@@ -693,38 +746,43 @@ __global__ void __launch_bounds__(kP, 3) kba_project(BDev d, Tape tp, Adj a, int
     sb[j] = a.dxbar[g];
   }
   __syncthreads();
-  if (!live) return;
-  Tet tt;
-  tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
-  tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
-  tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = C;
-  int l[4];
-  float3 dpb[4];
+  float3 gout[4] = {};
+  if (live) {
+    Tet tt;
+    tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+    tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+    tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = C;
+    int l[4];
+    float3 dpb[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    l[q] = (int)((lid >> (8 * q)) & 0xffu);
-    tt.p[q] = sp[l[q]];
-    dpb[q] = f3(sb[l[q]]);
+    for (int q = 0; q < 4; ++q) {
+      l[q] = (int)((lid >> (8 * q)) & 0xffu);
+      tt.p[q] = sp[l[q]];
+      dpb[q] = f3(sb[l[q]]);
+    }
+    const float inv_v0 = 6.f * det9(tt.dm);
+    const float s0 = c * inv_v0;  // d aD / d(1/mu) = d aH / d(1/lambda)
+    const float aD = s0 * m_mu, aH = s0 * m_la;
+    float2 lb;
+    float aDb, aHb;
+    tet_adjoint<kPrecise>(tt, L, aD, aH, lb_next, dpb, gout, lb, aDb, aHb);
+    a.lambar[t] = lb;
+    float2 rm = make_float2(0.f, 0.f);
+    if (a.rtet) rm = reinterpret_cast<const float2*>(a.rtet + t)[1];
+    a.g_mu[t] += (double)(aDb * s0 + rm.x);
+    a.g_la[t] += (double)(aHb * s0 + rm.y);
   }
-  const float inv_v0 = 6.f * det9(tt.dm);
-  const float s0 = c * inv_v0;  // d aD / d(1/mu) = d aH / d(1/lambda)
-  const float aD = s0 * m_mu, aH = s0 * m_la;
-  float3 gout[4];
-  float2 lb;
-  float aDb, aHb;
-  tet_adjoint<kPrecise>(tt, L, aD, aH, lb_next, dpb, gout, lb, aDb, aHb);
-  a.lambar[t] = lb;
-  float4* G = adj_buf(a, dst);
-#pragma unroll
-  for (int q = 0; q < 4; ++q) red_add_v4(G + sg[l[q]], gout[q].x, gout[q].y, gout[q].z, 0.f);
-  a.g_mu[t] += (double)(aDb * s0);
-  a.g_la[t] += (double)(aHb * s0);
+  scatter_corners(d.paired != 0, live, lid, gout, sg, adj_buf(a, dst));
 }
 
 // r_hat_k's adjoint into the tets of iteration k, one CTA per patch (the
-// batched layout of ka_residual_adj): the patch's post-Jacobi positions are
-// staged in shared memory; each thread takes one tet and scatters its corner
-// adjoints into abuf[dst] and dxbar with red.global.add.v4.
+// batched layout of ka_residual_adj): every CTA steps its body's omega chain
+// (the body's first patch stores it), the patch's post-Jacobi positions are
+// staged in shared memory, and each thread takes one tet.  The position part
+// goes to abuf[dst] (x~_k's adjoint: post = x~_k + dx / cnt) and, divided by
+// cnt, to the accumulator's adjoint dxbar (scatter_corners); the multiplier
+// and material parts go to rtet (zero where r_hat_k's adjoint is), read by
+// kba_project of iteration k.
 template <bool kPrecise>
 __global__ void __launch_bounds__(kP) kba_residual_adj(BDev d, Tape tp, Adj a, int k, float c, int dst) {
   __shared__ float4 sp[256];
@@ -732,17 +790,19 @@ __global__ void __launch_bounds__(kP) kba_residual_adj(BDev d, Tape tp, Adj a, i
   __shared__ float s_rb;
   const int p = blockIdx.x;
   const int body = __ldg(d.patch_body + p);
-  // every patch steps its body's chain; the body's first patch stores it
   if (threadIdx.x == 0)
     s_rb = (float)(chain_step(a, body, k, p == __ldg(d.body_first + body)) / adj_body_tets(d, body));
-  __syncthreads();
-  const float rb_n = s_rb;
-  if (rb_n == 0.f) return;
   const int vb = __ldg(d.voff + p);
   const int nv = __ldg(d.voff + p + 1) - vb;
   const int nt = __ldg(d.patch_ntets + p);
   const bool live = (int)threadIdx.x < nt;
   const int t = p * kP + threadIdx.x;
+  __syncthreads();
+  const float rb_n = s_rb;
+  if (rb_n == 0.f) {
+    if (live) a.rtet[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
   uint32_t lid = 0u;
   float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A;
   float C = 0.f, m_mu = 0.f, m_la = 0.f;
@@ -768,35 +828,21 @@ __global__ void __launch_bounds__(kP) kba_residual_adj(BDev d, Tape tp, Adj a, i
     sp[j] = __ldg(X + g);
   }
   __syncthreads();
-  if (!live) return;
-  Tet tt;
-  tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
-  tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
-  tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = C;
-  int l[4];
+  float3 g[4] = {};
+  if (live) {
+    Tet tt;
+    tt.dm[0] = A.x; tt.dm[1] = A.y; tt.dm[2] = A.z;
+    tt.dm[3] = A.w; tt.dm[4] = B.x; tt.dm[5] = B.y;
+    tt.dm[6] = B.z; tt.dm[7] = B.w; tt.dm[8] = C;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    l[q] = (int)((lid >> (8 * q)) & 0xffu);
-    tt.p[q] = sp[l[q]];
+    for (int q = 0; q < 4; ++q) tt.p[q] = sp[(lid >> (8 * q)) & 0xffu];
+    const float s0 = c * 6.f * det9(tt.dm);  // d aD / d(1/mu) = d aH / d(1/lambda)
+    float2 lb;
+    float aDb, aHb;
+    residual_adjoint<kPrecise>(tt, L1, s0 * m_mu, s0 * m_la, rb_n, g, lb, aDb, aHb);
+    a.rtet[t] = make_float4(lb.x, lb.y, aDb * s0, aHb * s0);
   }
-  const float s0 = c * 6.f * det9(tt.dm);  // d aD / d(1/mu) = d aH / d(1/lambda)
-  float3 g[4];
-  float2 lb;
-  float aDb, aHb;
-  residual_adjoint<kPrecise>(tt, L1, s0 * m_mu, s0 * m_la, rb_n, g, lb, aDb, aHb);
-  float4* G = adj_buf(a, dst);
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int v = sg[l[q]];
-    const float cn = a.cnt[v];
-    const float ic = cn > 0.f ? 1.f / cn : 0.f;
-    red_add_v4(G + v, g[q].x, g[q].y, g[q].z, 0.f);
-    red_add_v4(a.dxbar + v, g[q].x * ic, g[q].y * ic, g[q].z * ic, 0.f);
-  }
-  const float2 l0 = a.lambar[t];
-  a.lambar[t] = make_float2(l0.x + lb.x, l0.y + lb.y);
-  a.g_mu[t] += (double)(aDb * s0);
-  a.g_la[t] += (double)(aHb * s0);
+  scatter_corners(d.paired != 0, live, lid, g, sg, adj_buf(a, dst), a.dxbar, a.cnt);
 }
 
 }  // namespace batch
@@ -1533,6 +1579,10 @@ int xpbd_batch_substep_tape(void* h, float dt, const xpbd_tape* tape, void* stre
   if (tp.posts)  // the multipliers after the last iteration (the residual's lambda_K)
     B_CUDA(cudaMemcpyAsync(tp.lams + (size_t)K * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
   B_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
+  if (tape->hist)  // rows 0..K-1 of every body
+    B_CUDA(cudaMemcpy2DAsync(tape->hist, sizeof(double) * 4 * (size_t)K, s->d.hist,
+                             sizeof(double) * 4 * (size_t)s->d.max_records, sizeof(double) * 4 * (size_t)K,
+                             (size_t)s->d.n_bodies, cudaMemcpyDeviceToDevice, st));
   kb_end<<<nblk(V), 256, 0, st>>>(s->d, s->cur, dt, s->prm.damping, 0, 0, -1);
   B_CUDA(cudaGetLastError());
   return XPBD_OK;
@@ -1552,9 +1602,17 @@ int xpbd_batch_substep_adjoint(void* h, float dt, const xpbd_tape* tape, const x
           reinterpret_cast<float4*>(tape->posts), tape->rho_in};
   // through omega: the tape holds the post-Jacobi positions and the adjoint a chain state
   const bool through_omega = tp.posts && tp.rho_in && adj->omega_state && s->prm.cheb_enable;
+  BDev dv = s->d;  // the history rows of the substep: the tape's copy, else the batch's rows 0..K-1
+  if (tape->hist) {
+    dv.hist = tape->hist;
+    dv.max_records = K;
+  }
   Adj a;
   a.om = through_omega ? adj->omega_state : nullptr;
   a.om_n = om_stride(K);
+  a.rtet = through_omega ? reinterpret_cast<float4*>(adj->work_res_tet) : nullptr;
+  if (through_omega && !a.rtet)
+    return bfail(XPBD_ERR_INVALID_ARGUMENT, "the omega chain of a batch needs work_res_tet");
   a.gx = reinterpret_cast<float4*>(adj->gx);
   a.gv = reinterpret_cast<float4*>(adj->gv);
   a.g_mu = adj->g_inv_mu;
@@ -1568,21 +1626,22 @@ int xpbd_batch_substep_adjoint(void* h, float dt, const xpbd_tape* tape, const x
   B_CUDA(cudaMemsetAsync(a.lambar, 0, sizeof(float2) * T, st));
   const float e_over_dt = expf(-dt * s->prm.damping) / dt;
   const ChainPrm cp{K, s->prm.cheb_warmup, s->prm.rho_min, s->prm.rho_max, s->prm.rho_beta};
-  ka_end<BDev><<<nblk(V), 256, 0, st>>>(s->d, tp, a, cp, e_over_dt);
+  if (a.om) ka_chain<BDev><<<(s->d.n_bodies + 7) / 8, 256, 0, st>>>(dv, tp, a, cp);
+  ka_end<BDev><<<nblk(V), 256, 0, st>>>(dv, a, e_over_dt);
   const float c = (float)(1.0 / ((double)dt * (double)dt));
   int src = 0;
   for (int k = K - 1; k >= 0; --k) {
-    if (s->prm.cheb_enable) ka_cheb<BDev, true><<<nblk(V), 256, 0, st>>>(s->d, tp, a, k, s->prm.cheb_gamma, src);
-    else ka_cheb<BDev, false><<<nblk(V), 256, 0, st>>>(s->d, tp, a, k, s->prm.cheb_gamma, src);
+    if (s->prm.cheb_enable) ka_cheb<BDev, true><<<nblk(V), 256, 0, st>>>(dv, tp, a, k, s->prm.cheb_gamma, src);
+    else ka_cheb<BDev, false><<<nblk(V), 256, 0, st>>>(dv, tp, a, k, s->prm.cheb_gamma, src);
     if (through_omega) {
-      if (s->prm.precise_hydro) kba_residual_adj<true><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
-      else kba_residual_adj<false><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
+      if (s->prm.precise_hydro) kba_residual_adj<true><<<s->d.n_patches, kP, 0, st>>>(dv, tp, a, k, c, src ^ 1);
+      else kba_residual_adj<false><<<s->d.n_patches, kP, 0, st>>>(dv, tp, a, k, c, src ^ 1);
     }
-    if (s->prm.precise_hydro) kba_project<true><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
-    else kba_project<false><<<s->d.n_patches, kP, 0, st>>>(s->d, tp, a, k, c, src ^ 1);
+    if (s->prm.precise_hydro) kba_project<true><<<s->d.n_patches, kP, 0, st>>>(dv, tp, a, k, c, src ^ 1);
+    else kba_project<false><<<s->d.n_patches, kP, 0, st>>>(dv, tp, a, k, c, src ^ 1);
     src ^= 1;
   }
-  ka_begin<BDev><<<nblk(V), 256, 0, st>>>(s->d, tp, a, src, dt);
+  ka_begin<BDev><<<nblk(V), 256, 0, st>>>(dv, tp, a, src, dt);
   B_CUDA(cudaGetLastError());
   return XPBD_OK;
 }

@@ -2178,6 +2178,8 @@ int xpbd_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* strea
   if (tp.posts)  // the multipliers after the last iteration (the residual's lambda_K)
     XPBD_CUDA(cudaMemcpyAsync(tp.lams + (size_t)K * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
   XPBD_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
+  if (tape->hist)
+    XPBD_CUDA(cudaMemcpyAsync(tape->hist, s->d.hist, sizeof(double) * 4 * (size_t)K, cudaMemcpyDeviceToDevice, st));
   k_end<<<blocks_for(V), kBlock, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
   XPBD_CUDA(cudaGetLastError());
   return XPBD_OK;
@@ -2197,9 +2199,12 @@ int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xp
           reinterpret_cast<float4*>(tape->posts), tape->rho_in};
   // through omega: the tape holds the post-Jacobi positions and the adjoint a chain state
   const bool through_omega = tp.posts && tp.rho_in && adj->omega_state && s->prm.cheb_enable;
+  Dev dv = s->d;  // the history rows of the substep: the tape's copy, else the solver's rows 0..K-1
+  if (tape->hist) dv.hist = tape->hist;
   Adj a;
   a.om = through_omega ? adj->omega_state : nullptr;
   a.om_n = om_stride(K);
+  a.rtet = nullptr;  // the single-body residual adjoint adds its tet parts in place
   a.gx = reinterpret_cast<float4*>(adj->gx);
   a.gv = reinterpret_cast<float4*>(adj->gv);
   a.g_mu = adj->g_inv_mu;
@@ -2213,24 +2218,25 @@ int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xp
   XPBD_CUDA(cudaMemsetAsync(a.lambar, 0, sizeof(float2) * T, st));
   const float e_over_dt = expf(-dt * s->prm.damping) / dt;
   const ChainPrm cp{K, s->prm.cheb_warmup, s->prm.rho_min, s->prm.rho_max, s->prm.rho_beta};
-  ka_end<Dev><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, cp, e_over_dt);
+  if (a.om) ka_chain<Dev><<<1, 32, 0, st>>>(dv, tp, a, cp);
+  ka_end<Dev><<<blocks_for(V), kBlock, 0, st>>>(dv, a, e_over_dt);
   float cD, cH;
   compliance_factors(s, dt, cD, cH);
   int src = 0;
   for (int k = K - 1; k >= 0; --k) {
     if (s->prm.cheb_enable)
-      ka_cheb<Dev, true><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, k, s->prm.cheb_gamma, src);
-    else ka_cheb<Dev, false><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, k, s->prm.cheb_gamma, src);
+      ka_cheb<Dev, true><<<blocks_for(V), kBlock, 0, st>>>(dv, tp, a, k, s->prm.cheb_gamma, src);
+    else ka_cheb<Dev, false><<<blocks_for(V), kBlock, 0, st>>>(dv, tp, a, k, s->prm.cheb_gamma, src);
     const int g = (T + 127) / 128;
     if (through_omega) {
-      if (s->prm.precise_hydro) ka_residual_adj<Dev, true><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
-      else ka_residual_adj<Dev, false><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
+      if (s->prm.precise_hydro) ka_residual_adj<Dev, true><<<g, 128, 0, st>>>(dv, tp, a, k, cD, cH, src ^ 1);
+      else ka_residual_adj<Dev, false><<<g, 128, 0, st>>>(dv, tp, a, k, cD, cH, src ^ 1);
     }
-    if (s->prm.precise_hydro) ka_project<Dev, true><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
-    else ka_project<Dev, false><<<g, 128, 0, st>>>(s->d, tp, a, k, cD, cH, src ^ 1);
+    if (s->prm.precise_hydro) ka_project<Dev, true><<<g, 128, 0, st>>>(dv, tp, a, k, cD, cH, src ^ 1);
+    else ka_project<Dev, false><<<g, 128, 0, st>>>(dv, tp, a, k, cD, cH, src ^ 1);
     src ^= 1;
   }
-  ka_begin<Dev><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, a, src, dt);
+  ka_begin<Dev><<<blocks_for(V), kBlock, 0, st>>>(dv, tp, a, src, dt);
   XPBD_CUDA(cudaGetLastError());
   return XPBD_OK;
 }

@@ -87,12 +87,13 @@ class XpbdBatch(ctypes.Structure):
 
 
 class XpbdTape(ctypes.Structure):
-    _fields_ = [("xs", _P), ("lams", _P), ("xpre", _P), ("v1", _P), ("posts", _P), ("rho_in", _P)]
+    _fields_ = [("xs", _P), ("lams", _P), ("xpre", _P), ("v1", _P), ("posts", _P), ("rho_in", _P), ("hist", _P)]
 
 
 class XpbdAdjoint(ctypes.Structure):
     _fields_ = [("gx", _P), ("gv", _P), ("g_inv_mu", _P), ("g_inv_lambda", _P), ("work0", _P), ("work1", _P),
-                ("ybar", _P), ("dxbar", _P), ("lambar", _P), ("cnt", _P), ("omega_state", _P)]
+                ("ybar", _P), ("dxbar", _P), ("lambar", _P), ("cnt", _P), ("omega_state", _P),
+                ("work_res_tet", _P)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/xpbd_gb300.h

@@ -5,13 +5,23 @@ initial velocities.
 The reference has no gradients.  The forward is the reference's substep
 (``neohookean_solver.py:453-587``) run on the GPU with per-tet materials;
 ``xpbd_simulate`` wraps it in a ``torch.autograd.Function`` whose backward
-runs hand-written adjoint kernels (``xpbd_substep_adjoint``).  The state is
-checkpointed once per substep (positions, velocities, rho_hat) and every
-substep's Jacobi iterations are recomputed on a tape before its reverse pass.
+runs hand-written adjoint kernels (``xpbd_substep_adjoint``) over a tape of
+each substep: the predicted positions and multipliers entering every Jacobi
+iteration, the states around predict and the SDF list, and the substep's
+history rows (omega, r_hat).
 
-Each simulation length gets a plan (``_Plan``): static checkpoint buffers
-and its two passes -- the forward (per substep: checkpoint, substep) and the
-backward (per substep in reverse: restore, tape, adjoint) -- each captured
+Each simulation length gets a plan (``_Plan``) in one of two forms:
+* tapes stored (``tape_memory="store"``): the forward records every
+  substep's tape as it runs; the backward only reverses them.  A tape is
+  about (K + 1) (32 V + 8 T) bytes per substep (K iterations, V vertices, T
+  tets), e.g. 80 GB for 64 bodies of 1.75 M tets over 150 substeps of 20
+  iterations -- HBM that a GB300 has;
+* recomputed (``tape_memory="recompute"``): the forward checkpoints the
+  state once per substep (positions, velocities, rho_hat); the backward
+  restores each checkpoint and re-runs the substep on one shared tape before
+  reversing it, which costs one more forward.
+``tape_memory="auto"`` (default) stores when the plan's tapes take at most
+half of the free device memory at plan creation.  Each pass is captured
 once as a CUDA graph and replayed, so an optimisation loop launches two
 graphs per step.  A simulation object holds one simulation in flight: its
 backward must run before its next forward.
@@ -35,18 +45,22 @@ from xpbd_gpu.xpbd_base import _torch
 
 
 class _Plan:
-    """Checkpoints and passes of one simulation length of `sim` (a DiffSim or a
-    BatchedDiffSim): captured as two CUDA graphs with `use_graphs`, else run
-    directly."""
+    """Tapes or checkpoints and the two passes of one simulation length of `sim`
+    (a DiffSim or a BatchedDiffSim): captured as two CUDA graphs with
+    `use_graphs`, else run directly."""
 
     def __init__(self, sim, frames, use_graphs):
         torch = _torch()
         self.dts = sim.substep_dts(frames)
         n = len(self.dts)
-        x4, v4 = sim._state()
-        self.ck_x = torch.empty((n,) + tuple(x4.shape), dtype=x4.dtype, device=x4.device)
-        self.ck_v = torch.empty((n,) + tuple(v4.shape), dtype=v4.dtype, device=v4.device)
-        self.ck_rho = torch.empty((n, sim.n_rho), dtype=torch.float64, device=x4.device)
+        self.stored = sim._store_tapes(n)
+        if self.stored:
+            self.tapes = _Tapes(sim, n)
+        else:
+            x4, v4 = sim._state()
+            self.ck_x = torch.empty((n,) + tuple(x4.shape), dtype=x4.dtype, device=x4.device)
+            self.ck_v = torch.empty((n,) + tuple(v4.shape), dtype=v4.dtype, device=v4.device)
+            self.ck_rho = torch.empty((n, sim.n_rho), dtype=torch.float64, device=x4.device)
         self.generation = 0
         self._graphs = None
         if use_graphs:
@@ -58,6 +72,10 @@ class _Plan:
             self._graphs = (gf, gb)
 
     def _forward(self, sim):
+        if self.stored:
+            for k, dt in enumerate(self.dts):
+                sim._tape(dt, self.tapes.structs[k])
+            return
         x4, v4 = sim._state()
         for k, dt in enumerate(self.dts):
             self.ck_x[k].copy_(x4)
@@ -66,6 +84,10 @@ class _Plan:
             sim._substep(dt)
 
     def _backward(self, sim):
+        if self.stored:
+            for k in reversed(range(len(self.dts))):
+                sim._adjoint(self.dts[k], self.tapes.structs[k])
+            return
         x4, v4 = sim._state()
         for k in reversed(range(len(self.dts))):
             x4.copy_(self.ck_x[k])
@@ -92,11 +114,43 @@ class _Plan:
             self._backward(sim)
 
 
+class _Tapes:
+    """The tapes of `n` substeps of `sim`, one slice of each buffer per substep."""
+
+    def __init__(self, sim, n):
+        torch = _torch()
+        V, T, K, nb = sim.V, sim.T, sim.K, sim.n_rho
+        dev = sim._gx.device
+        f32 = dict(dtype=torch.float32, device=dev)
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.xs = torch.empty((n, (K + 1) * V, 4), **f32)
+        self.lams = torch.empty((n, sim._lams.shape[0], 2), **f32)
+        self.xpre = torch.empty((n, V, 4), **f32)
+        self.v1 = torch.empty((n, V, 4), **f32)
+        self.posts = torch.empty((n, K * V, 4), **f32) if sim.omega_grad else None
+        self.rho_in = torch.empty((n, nb), **f64) if sim.omega_grad else None
+        self.hist = torch.empty((n, nb * K * 4), **f64)
+        p = lambda t, k: t[k].data_ptr() if t is not None else None
+        self.structs = [_native.XpbdTape(p(self.xs, k), p(self.lams, k), p(self.xpre, k), p(self.v1, k),
+                                         p(self.posts, k), p(self.rho_in, k), p(self.hist, k)) for k in range(n)]
+
+    @staticmethod
+    def nbytes(sim, n):
+        V, T, K, nb = sim.V, sim.T, sim.K, sim.n_rho
+        per = 16 * ((K + 1) * V + 2 * V) + 8 * sim._lams.shape[0] + 32 * nb * K
+        if sim.omega_grad:
+            per += 16 * K * V + 8 * nb
+        return n * per
+
+
 def _plan(sim, frames):
+    """The plan of `frames` frames under the simulation's current tape_memory
+    (an "auto" plan keeps the choice it made when it was created)."""
     plans = sim.__dict__.setdefault("_plans", {})
-    if frames not in plans:
-        plans[frames] = _Plan(sim, frames, sim.use_graphs)
-    return plans[frames]
+    key = (frames, sim.tape_memory)
+    if key not in plans:
+        plans[key] = _Plan(sim, frames, sim.use_graphs)
+    return plans[key]
 
 
 class DiffSim:
@@ -104,7 +158,8 @@ class DiffSim:
 
     n_rho = 1
 
-    def __init__(self, rest_pose, sdf, log_E, nu, scatter="atomic", use_graphs=True, omega_grad=True, **kw):
+    def __init__(self, rest_pose, sdf, log_E, nu, scatter="atomic", use_graphs=True, omega_grad=True,
+                 tape_memory="auto", **kw):
         kw.setdefault("block_neohookean_enable", True)
         if not kw["block_neohookean_enable"]:
             raise ValueError("the adjoint supports the block projection only")
@@ -125,6 +180,14 @@ class DiffSim:
         self._bind()
         self.initial_rho_hat = s.rho_hat
         self.use_graphs = bool(use_graphs)
+        self.tape_memory = _check_tape_memory(tape_memory)
+
+    def _store_tapes(self, n_substeps):
+        """Whether a plan of `n_substeps` substeps stores its tapes (tape_memory)."""
+        if self.tape_memory != "auto":
+            return self.tape_memory == "store"
+        free, _ = _torch().cuda.mem_get_info(self._gx.device)
+        return _Tapes.nbytes(self, n_substeps) <= free // 2
 
     def _alloc_adjoint_buffers(self, V, T, K, n_bodies, dev, omega_grad):
         """Tape and adjoint buffers; with omega_grad the tape also keeps the
@@ -145,6 +208,8 @@ class DiffSim:
         self._rho_in = torch.zeros(n_bodies, dtype=torch.float64, device=dev) if omega_grad else None
         self._om = (torch.zeros((n_bodies, 8 + 6 * K), dtype=torch.float64, device=dev) if omega_grad
                     else None)
+        # the batch hands the residual adjoint's tet parts to the tet adjoint through this
+        self._rtet = f4(T) if omega_grad else None
 
     def _bind(self):
         ptr = lambda t: t.data_ptr() if t is not None else None
@@ -153,7 +218,7 @@ class DiffSim:
         self.adj = _native.XpbdAdjoint(self._gx.data_ptr(), self._gv.data_ptr(), self._gmu.data_ptr(),
                                        self._gla.data_ptr(), self._w0.data_ptr(), self._w1.data_ptr(),
                                        self._yb.data_ptr(), self._dxb.data_ptr(), self._lamb.data_ptr(),
-                                       self._cnt.data_ptr(), ptr(self._om))
+                                       self._cnt.data_ptr(), ptr(self._om), ptr(self._rtet))
 
     def reset_adjoint(self):
         """Zero what a backward pass accumulates (the omega chain included)."""
@@ -172,13 +237,15 @@ class DiffSim:
         s = self.solver
         _native.check(s._lib.xpbd_substep(s._handle, float(dt), 0, s._stream()))
 
-    def _tape(self, dt):
+    def _tape(self, dt, tape=None):
         s = self.solver
-        _native.check(s._lib.xpbd_substep_tape(s._handle, float(dt), self.tape, s._stream()))
+        tape = self.tape if tape is None else tape
+        _native.check(s._lib.xpbd_substep_tape(s._handle, float(dt), tape, s._stream()))
 
-    def _adjoint(self, dt):
+    def _adjoint(self, dt, tape=None):
         s = self.solver
-        _native.check(s._lib.xpbd_substep_adjoint(s._handle, float(dt), self.tape, self.adj, s._stream()))
+        tape = self.tape if tape is None else tape
+        _native.check(s._lib.xpbd_substep_adjoint(s._handle, float(dt), tape, self.adj, s._stream()))
 
     def rho_copy_to(self, dst):
         """Stream-ordered copy of the device rho_hat into a 1-element float64 tensor."""
@@ -275,7 +342,7 @@ class BatchedDiffSim:
     its own Chebyshev state, so the gradients of each body equal those of the
     same body simulated alone."""
 
-    def __init__(self, bodies, sdf, use_graphs=True, omega_grad=True, **kw):
+    def __init__(self, bodies, sdf, use_graphs=True, omega_grad=True, tape_memory="auto", **kw):
         from xpbd_gpu.batched import Body, XPBDBatchedSolver
         kw.setdefault("block_neohookean_enable", True)
         if not kw["block_neohookean_enable"]:
@@ -297,6 +364,9 @@ class BatchedDiffSim:
         self.rho_copy_to(self.initial_rho_hat)
         self.n_rho = s.n_bodies
         self.use_graphs = bool(use_graphs)
+        self.tape_memory = _check_tape_memory(tape_memory)
+
+    _store_tapes = DiffSim._store_tapes
 
     # -- the steps of a plan ---------------------------------------------------
     def _state(self):
@@ -306,13 +376,15 @@ class BatchedDiffSim:
         s = self.batch
         _native.check(s._lib.xpbd_batch_substep(s._handle, float(dt), 0, s._stream()), batch=True)
 
-    def _tape(self, dt):
+    def _tape(self, dt, tape=None):
         s = self.batch
-        _native.check(s._lib.xpbd_batch_substep_tape(s._handle, float(dt), self.tape, s._stream()), batch=True)
+        tape = self.tape if tape is None else tape
+        _native.check(s._lib.xpbd_batch_substep_tape(s._handle, float(dt), tape, s._stream()), batch=True)
 
-    def _adjoint(self, dt):
+    def _adjoint(self, dt, tape=None):
         s = self.batch
-        _native.check(s._lib.xpbd_batch_substep_adjoint(s._handle, float(dt), self.tape, self.adj, s._stream()),
+        tape = self.tape if tape is None else tape
+        _native.check(s._lib.xpbd_batch_substep_adjoint(s._handle, float(dt), tape, self.adj, s._stream()),
                       batch=True)
 
     def rho_copy_to(self, dst):
@@ -340,6 +412,12 @@ class BatchedDiffSim:
     def positions(self):
         s = self.batch
         return s._x4[s._vert_slot, :3].clone()
+
+
+def _check_tape_memory(mode):
+    if mode not in ("auto", "store", "recompute"):
+        raise ValueError("tape_memory must be 'auto', 'store' or 'recompute', not %r" % (mode,))
+    return mode
 
 
 def _n_tets(rest_pose):

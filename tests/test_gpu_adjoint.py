@@ -7,7 +7,8 @@ positions and velocities must match it within 1e-3 relative (L2 norm of the
 difference over the norm of the gradient), on a body with plane, sphere and
 moving-box contact: with the adjoint run back through the Chebyshev omega
 (omega_grad, the derivative of the forward as it runs) and with omega as a
-stop-gradient.
+stop-gradient, with the tapes stored by the forward and recomputed by the
+backward.
 """
 import numpy as np
 import pytest
@@ -19,8 +20,9 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-@pytest.mark.parametrize("cheb,omega_grad", [(True, True), (True, False), (False, False)])
-def test_gpu_gradients_match_float64_adjoint(cheb, omega_grad):
+@pytest.mark.parametrize("cheb,omega_grad,tape_memory", [(True, True, "store"), (True, True, "recompute"),
+                                                        (True, False, "store"), (False, False, "recompute")])
+def test_gpu_gradients_match_float64_adjoint(cheb, omega_grad, tape_memory):
     import torch
     from oracle.xpbd_adjoint import DiffOracle, lame_inverse, lame_inverse_grad
     from oracle.xpbd_oracle import OracleSdf
@@ -46,7 +48,8 @@ def test_gpu_gradients_match_float64_adjoint(cheb, omega_grad):
     g_logE64, g_nu64 = lame_inverse_grad(logE, nu, gm, gl)
 
     sim = DiffSim(m, [PlaneSdf([0, 0, 0], [0, 1, 0], True), SphereSdf([0.42, -0.18, 0.42], 0.2, True),
-                      CubeSdf([0.5, 0.0, 0.5], [0.1, 0.03, 0.2], False)], logE, nu, omega_grad=omega_grad, **kw)
+                      CubeSdf([0.5, 0.0, 0.5], [0.1, 0.03, 0.2], False)], logE, nu, omega_grad=omega_grad,
+                  tape_memory=tape_memory, **kw)
     dev = torch.device("cuda")
     x0_t = torch.tensor(m.points, dtype=torch.float32, device=dev, requires_grad=True)
     v0_t = torch.tensor(v0, dtype=torch.float32, device=dev, requires_grad=True)

@@ -6,7 +6,8 @@ batch; the gradients of a linear loss on all final positions w.r.t. every
 tet's log E and nu and every vertex's initial position and velocity must match
 the float64 adjoint of each body simulated alone (oracle/xpbd_adjoint.py,
 itself checked against central finite differences), through omega and with
-omega as a stop-gradient, within 1e-3 relative (L2
+omega as a stop-gradient, with stored and recomputed tapes, within 1e-3
+relative (L2
 norm of the difference over the norm of the gradient).  The forward positions
 must match the float64 forward within 1e-4 of each body's bounding-box
 diagonal.
@@ -28,8 +29,9 @@ def _bodies():
             kuhn_grid(4, 2, 3, 0.06, origin=(0.32, 0.01, 0.3), jitter=0.1, seed=6)]
 
 
-@pytest.mark.parametrize("cheb,omega_grad", [(True, True), (True, False), (False, False)])
-def test_batched_gradients_match_float64_adjoint(cheb, omega_grad):
+@pytest.mark.parametrize("cheb,omega_grad,tape_memory", [(True, True, "store"), (True, True, "recompute"),
+                                                        (True, False, "store"), (False, False, "recompute")])
+def test_batched_gradients_match_float64_adjoint(cheb, omega_grad, tape_memory):
     import torch
     from oracle.xpbd_adjoint import DiffOracle, lame_inverse, lame_inverse_grad
     from oracle.xpbd_oracle import OracleSdf
@@ -64,7 +66,7 @@ def test_batched_gradients_match_float64_adjoint(cheb, omega_grad):
             CubeSdf([0.5, 0.0, 0.5], [0.1, 0.03, 0.2], False)]
     bodies = [Body(m, tet_young_modulus=np.exp(le), tet_poisson_ratio=n, total_mass=1.0)
               for m, le, n in zip(meshes, logE, nu)]
-    sim = BatchedDiffSim(bodies, sdfs, omega_grad=omega_grad, **kw)
+    sim = BatchedDiffSim(bodies, sdfs, omega_grad=omega_grad, tape_memory=tape_memory, **kw)
     dev = torch.device("cuda")
     x0_t = torch.tensor(np.concatenate([m.points for m in meshes]), dtype=torch.float32, device=dev,
                         requires_grad=True)
