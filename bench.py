@@ -141,6 +141,92 @@ def run_c4(args):
     print(json.dumps(c4_block(args)), flush=True)
 
 
+# the reference's four-way comparison: (label, block Neo-Hookean, dynamic Chebyshev)
+MATRIX = [("NH", False, False), ("NH-DC", False, True), ("BNH", True, False), ("BNH-DC", True, True)]
+
+
+def matrix_scene(args):
+    """Scene, material and stepping of the reference's convergence comparison
+    (scripts/compare_convergence_armadillo.bat:14-17 with the driver
+    run_neohookean_usd.py:82-106): the mesh at scale 0.01 and offset (0, 1, 0),
+    E 5e8, nu 0.4999, relaxation 1.2, dt 0.01 at 60 fps (two chunks per frame),
+    1 substep of 200 iterations, Chebyshev warm-up 5 and gamma 0.666, the plane
+    y = -2 and the fixed sphere at (0, -1, 0) of radius 0.3, monitoring on."""
+    kw = dict(scale=args.matrix_scale, offset=(0.0, 1.0, 0.0), hydrostatic_relaxation=1.2,
+              deviatoric_relaxation=1.2, frame_dt=1.0 / 60, dt=0.01, substeps_num=1, constraints_iter=200,
+              young_modulus=5e8, poisson_ratio=0.4999, cheb_warmup=5, cheb_gamma=0.666, monitor_convergence=True)
+    sdfs = [("plane", dict(point=[0.0, -2.0, 0.0], dir=[0.0, 1.0, 0.0], fixed=True)),
+            ("sphere", dict(center=[0.0, -1.0, 0.0], radius=0.3, fixed=True))]
+    return kw, sdfs
+
+
+def run_matrix(args):
+    """NH / NH-DC / BNH / BNH-DC on one mesh for `matrix_frame` + 1 frames: the
+    convergence records of frame `matrix_frame` (r_hat, hydrostatic and
+    deviatoric error per iteration, both chunks), the solver time per frame
+    (monitoring on, as the driver runs it), and that frame against the C
+    restatement in FP64 and FP32 started from the GPU state before it."""
+    import torch
+    from oracle.xpbd_oracle import OracleSdf
+    from oracle.xpbd_oracle_c import COracle
+    from xpbd_gpu.mesh import read_tetgen
+    from xpbd_gpu.neohookean_solver import XPBDNeoHookeanSolver
+    torch.cuda.set_device(0)
+    mesh = read_tetgen(args.mesh)
+    kw0, specs = matrix_scene(args)
+    F = args.matrix_frame
+    out = {"workload": "convergence matrix", "mesh": os.path.basename(args.mesh), "verts": mesh.n_verts,
+           "tets": mesh.n_tets, "frames": F + 1, "recorded_frame": F,
+           "scene": "scale %g, offset (0, 1, 0), E 5e8, nu 0.4999, relax 1.2, dt 0.01 at 60 fps, 1 substep x 200 it, "
+                    "plane y=-2 + sphere (0,-1,0) r 0.3" % args.matrix_scale, "configs": {}}
+    for label, block, cheb in MATRIX:
+        kw = dict(kw0, block_neohookean_enable=block, cheb_enable=cheb)
+        s = XPBDNeoHookeanSolver(rest_pose=mesh, sdf=product_sdfs(specs), **kw)
+        recs = []
+
+        def record(frame, substep, data, s=s, recs=recs):
+            if frame == F:  # r_hat from the history rows (computed with the Chebyshev step only)
+                rh = s.read_history(s.constraints_iter)[:, 0].tolist() if s.cheb_enable else None
+                recs.append((rh, [dict(r) for r in data]))
+        s.convergence_callback = record
+        times = []
+        for f in range(F + 1):
+            if f == F:
+                x_prev = s.mesh.verts.x.to_numpy().astype(np.float64)
+                v_prev = s.mesh.verts.v.to_numpy().astype(np.float64)
+                rho_prev = float(s.rho_hat)
+            t0 = time.perf_counter()
+            s.solve()
+            times.append(time.perf_counter() - t0)
+        s.check_status()
+        x_gpu = s.mesh.verts.x.to_numpy().astype(np.float64)
+        diag = float(np.linalg.norm(x_gpu.max(0) - x_gpu.min(0)))
+        cfg = {"ms_per_frame": 1e3 * float(np.mean(times[1:])),
+               "chunks": [{"r_hat": rh, "hydro_error": [r["hydro_error"] for r in c],
+                           "dev_error": [r["dev_error"] for r in c]} for rh, c in recs]}
+        # the recorded frame from the same state in the C restatement
+        ok = dict(kw, block_neohookean_enable=block, cheb_enable=cheb)
+        hist_len = 2 * 200
+        for name, dt_ in (("fp64", np.float64), ("fp32", np.float32)):
+            o = COracle(mesh.points, mesh.tets, [OracleSdf(k, **p) for k, p in specs], dtype=dt_, **ok)
+            o.x[:] = x_prev
+            o.v[:] = v_prev
+            o.rho_hat.value = rho_prev
+            hist = np.zeros(hist_len)
+            o.solve(1, r_hat_hist=hist)
+            cfg[name + "_max_dev_over_bbox_diag"] = float(np.abs(x_gpu - o.x).max()) / diag
+            if name == "fp64":
+                x64 = o.x.astype(np.float64).copy()
+                cfg["fp64_r_hat"] = hist.tolist()
+            else:
+                cfg["fp32_vs_fp64_max_dev_over_bbox_diag"] = float(np.abs(o.x - x64).max()) / diag
+        out["configs"][label] = cfg
+        print("%s: %.2f ms/frame, vs FP64 %.2e (FP32 reference vs FP64 %.2e)" % (
+            label, cfg["ms_per_frame"], cfg["fp64_max_dev_over_bbox_diag"],
+            cfg["fp32_vs_fp64_max_dev_over_bbox_diag"]), file=sys.stderr, flush=True)
+    print(json.dumps(out), flush=True)
+
+
 def plain_forward_ms(sim, simulate, x0, v0, log_E, nu, frames, reps):
     """Mean device time of the forward alone, without tapes (the recompute
     plan: one CUDA graph of per-substep state checkpoints and plain substeps)."""
@@ -1353,7 +1439,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c3", choices=["c2", "c1", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c3", choices=["c2", "c1", "c3", "c4", "c5", "matrix"])
+    ap.add_argument("--mesh", default=None, help="matrix workload: a TetGen .node path (e.g. the reference's "
+                                                 "assets/tetmesh/armadillo.node)")
+    ap.add_argument("--matrix-frame", type=int, default=300, help="matrix workload: the recorded frame")
+    ap.add_argument("--matrix-scale", type=float, default=0.01, help="matrix workload: the mesh scale")
     ap.add_argument("--c3-cap", type=int, default=200, help="iteration cap of the equal-residual runs")
     ap.add_argument("--c3-target", type=float, default=1e-3, help="r_hat_k / r_hat_0 target")
     ap.add_argument("--c3-floor", type=float, default=1e-5, help="r_hat below which a substep has converged")
@@ -1398,6 +1488,10 @@ def main():
         run_c4(args)
     elif args.workload == "c5" and args.impl != "reference":
         run_c5(args)
+    elif args.workload == "matrix":
+        if not args.mesh:
+            ap.error("--workload matrix needs --mesh")
+        run_matrix(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -299,7 +299,8 @@ __device__ __forceinline__ void tet_adjoint(const Tet& tt, const float2 L, const
     A12 += w[c] * dot3(gD[c], gH[c]);
   }
   const float b1 = -(C_D + aD * L.x), b2 = -(C_H + aH * L.y);
-  const float det = A11 * A22 - A12 * A12;
+  // products rounded before the difference, as in the forward's elimination
+  const float det = __fmul_rn(A11, A22) - __fmul_rn(A12, A12);
   const float idet = 1.f / det;
   const float dD = (A22 * b1 - A12 * b2) * idet;
   const float dH = (A11 * b2 - A12 * b1) * idet;

@@ -72,8 +72,23 @@ def single_tet():
     return pts, tets
 
 
+def read_tetgen(node_path):
+    """TetGen .node / .ele pair (the reference's assets/tetmesh format) ->
+    (points, tets); the first index of each file is the base (0 or 1)."""
+    def rows(path):
+        lines = [ln.split("#")[0].split() for ln in open(path)]
+        lines = [ln for ln in lines if ln]
+        n = int(lines[0][0])
+        return lines[1:n + 1]
+    nodes = rows(node_path)
+    base = int(nodes[0][0])
+    pts = np.array([[float(v) for v in ln[1:4]] for ln in nodes], dtype=np.float64)
+    tets = np.array([[int(v) - base for v in ln[1:5]] for ln in rows(node_path[:-5] + ".ele")], dtype=np.int64)
+    return pts, tets
+
+
 # name -> dict(mesh, sdfs, solver kwargs, frames)
-def cases():
+def cases(ref=None):
     c = {}
     k2 = kuhn_grid(2, 2, 2, 0.1, (0.35, 0.02, 0.35), 0.1, 1)
     k3 = kuhn_grid(3, 3, 3, 0.08, (0.3, 0.015, 0.3), 0.1, 2)
@@ -103,6 +118,19 @@ def cases():
                ("sphere", dict(center=[0.45, 0.3, 0.45], radius=0.14, fixed=True))]
     c["kuhn2_pinned_nonfixed"] = dict(mesh=kuhn_grid(2, 2, 2, 0.1, (0.35, 0.2, 0.35), 0.1, 3),
                                       sdfs=sdf_pin, kw=dict(base), frames=6)
+    if ref is not None:
+        # the reference's own cow (assets/tetmesh/cow.node: 4,784 vertices, 17,360
+        # tets) with the driver's material (run_neohookean_usd.py:27-30: E 5e8,
+        # nu 0.4999), its hooves 3 mm into the plane; one frame, since this stiff
+        # contact scene amplifies round-off from frame to frame (FP32 departs
+        # 3e-5 of the diagonal from FP64 after one frame, 1.5e-4 after two)
+        cow = read_tetgen(os.path.join(ref, "assets", "tetmesh", "cow.node"))
+        floor = float(cow[0][:, 1].min()) + 0.003
+        c["cow_block_cheb"] = dict(
+            mesh=cow, sdfs=[("plane", dict(point=[0.0, floor, 0.0], dir=[0.0, 1.0, 0.0], fixed=True))],
+            kw=dict(base, young_modulus=5e8, poisson_ratio=0.4999, substeps_num=1, constraints_iter=20,
+                    cheb_warmup=5, cheb_gamma=0.666),
+            frames=1)
     return c
 
 
@@ -166,6 +194,12 @@ def run_case(ref, name, spec, precision):
         solver_kw=repr(spec["kw"]),
         precision=precision,
     )
+    if len(out["tets"]) > 5000:
+        # a reference asset: the setup arrays follow from the mesh (and are checked
+        # on the small cases), so the fixture keeps the mesh, the states and the curves
+        for k in ("V0", "inv_Dm", "indices", "mass"):
+            del out[k]
+        out["tets"] = out["tets"].astype(np.int32)
     for m in [m for m in list(sys.modules) if m == "xpbd_gpu" or m.startswith("xpbd_gpu.")]:
         del sys.modules[m]
     return out
@@ -181,7 +215,7 @@ def main():
     args = ap.parse_args()
     if not args.ref:
         ap.error("give --ref or set XPBD_REFERENCE_DIR")
-    for name, spec in cases().items():
+    for name, spec in cases(os.path.abspath(args.ref)).items():
         if args.only and name not in args.only:
             continue
         t0 = time.time()

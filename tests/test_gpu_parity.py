@@ -5,7 +5,8 @@ tests/golden/make_golden.py).  The GPU computes in FP32 with float atomics
 (order nondeterministic) or with the deterministic gather, so positions are
 compared within the stated tolerance: max vertex deviation <= 1e-4 of the
 bounding-box diagonal after every frame; per-iteration residuals r_hat within
-2e-3 relative plus an absolute 2e-4 of the curve's maximum, the FP32
+2e-3 relative (1e-2 on the stiff reference cow, where FP32 itself departs
+4e-3) plus an absolute 2e-4 of the curve's maximum, the FP32
 round-off floor of a body in free fall (there FP64 gives r_hat ~ 1e-16 and
 FP32 ~ 1e-7, and rho_hat is driven by that noise, so it is compared only for
 bodies that are in contact from the first frame).
@@ -19,6 +20,10 @@ pytestmark = pytest.mark.gpu
 
 POS_TOL = 1e-4   # of the bounding-box diagonal, after each frame
 RES_RTOL = 2e-3
+# The reference's cow at E 5e8: rD = C_D + aD lambda_D nearly cancels, and the
+# reference algorithm's r_hat in FP32 (the C restatement) departs up to 4.1e-3
+# from FP64 there, 2.5e-3 at the first iteration
+RES_RTOL_CASE = {"cow_block_cheb": 1e-2}
 
 
 def make_solver(d, **over):
@@ -58,7 +63,7 @@ def test_frames_match_reference(name, scatter):
     if r_hat:
         r = np.concatenate(r_hat)
         g = d["r_hat"]
-        np.testing.assert_allclose(r, g, rtol=RES_RTOL, atol=2e-4 * np.abs(g).max())
+        np.testing.assert_allclose(r, g, rtol=RES_RTOL_CASE.get(name, RES_RTOL), atol=2e-4 * np.abs(g).max())
         if not name.startswith("tet1"):
             assert abs(s.rho_hat - float(d["rho_hat_frame"][-1])) < 2e-3
 

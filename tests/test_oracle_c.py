@@ -6,7 +6,7 @@ import golden_cases as gc
 
 
 @pytest.mark.parametrize("name", ["kuhn2_block_cheb", "kuhn2_split_cheb", "kuhn2_block_nocheb",
-                                  "kuhn3_block_cheb_nu049", "kuhn2_pinned_nonfixed"])
+                                  "kuhn3_block_cheb_nu049", "kuhn2_pinned_nonfixed", "cow_block_cheb"])
 @pytest.mark.parametrize("threads", [1, 3])
 def test_c_oracle_matches_reference_goldens(name, threads):
     from oracle.xpbd_oracle_c import COracle
@@ -34,7 +34,7 @@ def test_c_oracle_thread_count_does_not_change_results():
 
 
 @pytest.mark.parametrize("name", ["kuhn2_block_cheb", "kuhn2_split_cheb", "kuhn3_block_cheb_nu049",
-                                  "kuhn2_pinned_nonfixed"])
+                                  "kuhn2_pinned_nonfixed", "cow_block_cheb"])
 def test_c_oracle_fp64_matches_reference_goldens_tightly(name):
     """The FP64 build (the float64 reference run of large meshes) reproduces the
     float64 runs of the reference's own code far below the FP32 tolerance; its

@@ -19,11 +19,13 @@ def test_oracle_f64_matches_reference(name):
     s = OracleSolver(d["points"], d["tets"], gc.oracle_sdfs(d), dtype=np.float64, **gc.solver_kwargs(d))
     np.testing.assert_allclose(s.x, d["x_init"], rtol=0, atol=1e-15)
     np.testing.assert_allclose(s.inv_m, d["inv_m"], rtol=1e-12)
-    np.testing.assert_allclose(s.V0, d["V0"], rtol=1e-12)
-    np.testing.assert_allclose(s.inv_Dm, d["inv_Dm"], rtol=1e-10, atol=1e-10)
-    np.testing.assert_array_equal(s.indices, d["indices"])
-    # tet1 free-falls first: r_hat is round-off noise there, so omega differs at 1e-8
-    tol = 1e-8 if name.startswith("tet1") else 1e-11
+    if "V0" in d.files:  # the fixtures of reference assets keep only the mesh, states and curves
+        np.testing.assert_allclose(s.V0, d["V0"], rtol=1e-12)
+        np.testing.assert_allclose(s.inv_Dm, d["inv_Dm"], rtol=1e-10, atol=1e-10)
+        np.testing.assert_array_equal(s.indices, d["indices"])
+    # tet1 free-falls first: r_hat is round-off noise there, so omega differs at 1e-8;
+    # the cow (E 5e8, 17,360 tets) amplifies the FP64 round-off of the sums to ~3e-11
+    tol = 1e-8 if name.startswith("tet1") else (1e-10 if name.startswith("cow") else 1e-11)
     for f in range(int(d["frames"])):
         s.solve()
         np.testing.assert_allclose(s.x, d["x"][f], rtol=0, atol=tol)
