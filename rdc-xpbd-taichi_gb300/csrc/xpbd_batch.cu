@@ -261,23 +261,49 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_projec
   uint32_t lid[kTPT];
   float2 L[kTPT];
   float mD[kTPT], mH[kTPT];
+  if (kTPT == 2) {  // one load per record array (the patch's slots are padded to kP)
+    ldg_pair(d.dm_a + t0, A[0], A[1]);
+    ldg_pair(d.dm_b + t0, B[0], B[1]);
+    const float2 c = __ldg(reinterpret_cast<const float2*>(d.dm_c + t0));
+    const uint2 li = __ldg(reinterpret_cast<const uint2*>(d.lid + t0));
+    C[0] = c.x;
+    C[1] = c.y;
+    lid[0] = li.x;
+    lid[1] = li.y;
+    L[0] = L[1] = make_float2(0.f, 0.f);
+    if (!kFirst) {
+      const float4 l2 = *reinterpret_cast<const float4*>(d.lam + t0);
+      L[0] = make_float2(l2.x, l2.y);
+      L[1] = make_float2(l2.z, l2.w);
+    }
+    mD[0] = mD[1] = mH[0] = mH[1] = 0.f;
+    if (kTetMat) {
+      const float2 u = __ldg(reinterpret_cast<const float2*>(d.tinv_mu + t0));
+      const float2 v = __ldg(reinterpret_cast<const float2*>(d.tinv_la + t0));
+      mD[0] = u.x;
+      mD[1] = u.y;
+      mH[0] = v.x;
+      mH[1] = v.y;
+    }
+  } else {
 #pragma unroll
-  for (int k = 0; k < kTPT; ++k) {
-    A[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    B[k] = A[k];
-    C[k] = 0.f;
-    lid[k] = 0u;
-    L[k] = make_float2(0.f, 0.f);
-    mD[k] = mH[k] = 0.f;
-    if (l0 + k < nt) {
-      A[k] = __ldg(d.dm_a + t0 + k);
-      B[k] = __ldg(d.dm_b + t0 + k);
-      C[k] = __ldg(d.dm_c + t0 + k);
-      lid[k] = __ldg(d.lid + t0 + k);
-      if (!kFirst) L[k] = d.lam[t0 + k];
-      if (kTetMat) {
-        mD[k] = __ldg(d.tinv_mu + t0 + k);
-        mH[k] = __ldg(d.tinv_la + t0 + k);
+    for (int k = 0; k < kTPT; ++k) {
+      A[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      B[k] = A[k];
+      C[k] = 0.f;
+      lid[k] = 0u;
+      L[k] = make_float2(0.f, 0.f);
+      mD[k] = mH[k] = 0.f;
+      if (l0 + k < nt) {
+        A[k] = __ldg(d.dm_a + t0 + k);
+        B[k] = __ldg(d.dm_b + t0 + k);
+        C[k] = __ldg(d.dm_c + t0 + k);
+        lid[k] = __ldg(d.lid + t0 + k);
+        if (!kFirst) L[k] = d.lam[t0 + k];
+        if (kTetMat) {
+          mD[k] = __ldg(d.tinv_mu + t0 + k);
+          mH[k] = __ldg(d.tinv_la + t0 + k);
+        }
       }
     }
   }
@@ -433,17 +459,42 @@ __global__ void __launch_bounds__(kP / kTPT) kb_residual(BDev d, BSweep a, int c
     uint32_t lid[kTPT];
     float2 L[kTPT];
     float mD[kTPT], mH[kTPT];
+    if (kTPT == 2) {  // one load per record array (the patch's slots are padded to kP)
+      ldg_pair(d.dm_a + t0, A[0], A[1]);
+      ldg_pair(d.dm_b + t0, B[0], B[1]);
+      const float2 c = __ldg(reinterpret_cast<const float2*>(d.dm_c + t0));
+      const uint2 li = __ldg(reinterpret_cast<const uint2*>(d.lid + t0));
+      C[0] = c.x;
+      C[1] = c.y;
+      lid[0] = li.x;
+      lid[1] = li.y;
+      L[0] = L[1] = make_float2(0.f, 0.f);
+      if (kRes) {
+        const float4 l2 = *reinterpret_cast<const float4*>(d.lam + t0);
+        L[0] = make_float2(l2.x, l2.y);
+        L[1] = make_float2(l2.z, l2.w);
+      }
+      if (kTetMat && kRes) {
+        const float2 u = __ldg(reinterpret_cast<const float2*>(d.tinv_mu + t0));
+        const float2 v = __ldg(reinterpret_cast<const float2*>(d.tinv_la + t0));
+        mD[0] = u.x;
+        mD[1] = u.y;
+        mH[0] = v.x;
+        mH[1] = v.y;
+      }
+    } else {
 #pragma unroll
-    for (int k = 0; k < kTPT; ++k) {
-      if (l0 + k < nt) {
-        A[k] = __ldg(d.dm_a + t0 + k);
-        B[k] = __ldg(d.dm_b + t0 + k);
-        C[k] = __ldg(d.dm_c + t0 + k);
-        lid[k] = __ldg(d.lid + t0 + k);
-        L[k] = kRes ? d.lam[t0 + k] : make_float2(0.f, 0.f);
-        if (kTetMat && kRes) {
-          mD[k] = __ldg(d.tinv_mu + t0 + k);
-          mH[k] = __ldg(d.tinv_la + t0 + k);
+      for (int k = 0; k < kTPT; ++k) {
+        if (l0 + k < nt) {
+          A[k] = __ldg(d.dm_a + t0 + k);
+          B[k] = __ldg(d.dm_b + t0 + k);
+          C[k] = __ldg(d.dm_c + t0 + k);
+          lid[k] = __ldg(d.lid + t0 + k);
+          L[k] = kRes ? d.lam[t0 + k] : make_float2(0.f, 0.f);
+          if (kTetMat && kRes) {
+            mD[k] = __ldg(d.tinv_mu + t0 + k);
+            mH[k] = __ldg(d.tinv_la + t0 + k);
+          }
         }
       }
     }

@@ -309,6 +309,35 @@ __device__ __forceinline__ int ldg_hint(const int* p, uint64_t pol) {
   return r;
 }
 
+// The records of two consecutive tets (t even: float4 pairs 32-byte aligned,
+// scalar pairs 8-byte aligned) in one load per array.  With two tets per
+// thread, loading t and t + 1 separately makes each warp instruction touch
+// every other 16 bytes of a 1 KiB span, so a warp reads each sector through
+// L1 twice; the 256-bit load (sm_100+) reads it once.
+__device__ __forceinline__ void ldg_pair(const float4* p, uint64_t pol, float4& a, float4& b) {
+  asm("ld.global.nc.L2::cache_hint.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8], %9;"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p), "l"(pol));
+}
+
+__device__ __forceinline__ void ldg_pair(const float4* p, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+
+__device__ __forceinline__ float2 ldg_pair(const float* p, uint64_t pol) {
+  float2 r;
+  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(r.x), "=f"(r.y) : "l"(p), "l"(pol));
+  return r;
+}
+
+__device__ __forceinline__ uint2 ldg_pair(const uint32_t* p, uint64_t pol) {
+  uint2 r;
+  asm("ld.global.nc.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;" : "=r"(r.x), "=r"(r.y) : "l"(p), "l"(pol));
+  return r;
+}
+
 // ---------------------------------------------------------------------------
 // Bulk asynchronous copies (TMA, cp.async.bulk) tracked by an mbarrier.
 // ---------------------------------------------------------------------------

@@ -553,6 +553,108 @@ __global__ void __launch_bounds__(256) k_project_tile(Dev d, int cur, float cD, 
   }
 }
 
+// Gather vertex g of the patch's list position j into stage s.
+__device__ __forceinline__ void gather_vertex(TileSmem<false>& sm, int s, const float4* P, int g, int j) {
+  sm.sg[s][j] = g;
+  cp_async16(&sm.sp[s][j], P + g);
+}
+
+// Pipelined tile projection with two consecutive tets per thread (128 threads
+// per 256-tet patch): the walk, stages and copies of k_project_tile, and per
+// thread the chain of k_project_patchN (the corner sums a face pair shares
+// merged before the reduction).  Each thread gathers vertices j and j + 128
+// of the next tile.
+template <bool kBlockMode, bool kFirst, bool kPrecise>
+__global__ void __launch_bounds__(128, 6) k_project_tile2(Dev d, int cur, float cD, float cH, float relax_h,
+                                                         float relax_d) {
+  if (stopped(d)) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TileSmem<false>& sm = *reinterpret_cast<TileSmem<false>*>(smem_raw);
+  __shared__ int abort_flag;
+  if (threadIdx.x == 0) {
+    mbar_init(reinterpret_cast<uint64_t*>(&sm.bar[0]), 1);
+    mbar_init(reinterpret_cast<uint64_t*>(&sm.bar[1]), 1);
+    fence_mbar_init();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  const int n = d.n_patches, G = gridDim.x, tid = threadIdx.x;
+  const float4* P = d.p[cur];
+  int q = blockIdx.x;
+  if (q >= n) return;
+  // prologue: records + tile of q, vertex ids of q + G
+  if (tid == 0) issue_records<!kFirst>(d, sm.st[0], &sm.bar[0], q, 256);
+  {
+    const int vb = __ldg(d.voff + q), nv = __ldg(d.voff + q + 1) - vb;
+    if (tid < nv) gather_vertex(sm, 0, P, __ldg(d.pverts + vb + tid), tid);
+    if (tid + 128 < nv) gather_vertex(sm, 0, P, __ldg(d.pverts + vb + tid + 128), tid + 128);
+  }
+  cp_async_commit();
+  int gn0 = -1, gn1 = -1;
+  if (q + G < n) {
+    const int vb = __ldg(d.voff + q + G), nv = __ldg(d.voff + q + G + 1) - vb;
+    if (tid < nv) gn0 = __ldg(d.pverts + vb + tid);
+    if (tid + 128 < nv) gn1 = __ldg(d.pverts + vb + tid + 128);
+  }
+  int k = 0;
+  bool issued_next = false;
+  const int l0 = 2 * tid;
+  for (; q < n; q += G, ++k) {
+    const int s = k & 1;
+    const int qn = q + G;
+    issued_next = qn < n;
+    if (issued_next) {
+      if (tid == 0) {
+        fence_proxy_async();
+        issue_records<!kFirst>(d, sm.st[s ^ 1], &sm.bar[s ^ 1], qn, 256);
+      }
+      if (gn0 >= 0) gather_vertex(sm, s ^ 1, P, gn0, tid);
+      if (gn1 >= 0) gather_vertex(sm, s ^ 1, P, gn1, tid + 128);
+    }
+    cp_async_commit();
+    gn0 = gn1 = -1;
+    if (qn + G < n) {
+      const int vb = __ldg(d.voff + qn + G), nv = __ldg(d.voff + qn + G + 1) - vb;
+      if (tid < nv) gn0 = __ldg(d.pverts + vb + tid);
+      if (tid + 128 < nv) gn1 = __ldg(d.pverts + vb + tid + 128);
+    }
+    cp_async_wait<1>();
+    if (tid == 0 && !mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[s]), (k >> 1) & 1, kMaxPolls)) {
+      abort_flag = 1;
+      d.st->timeout = 1;
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    const int t0 = q * 256;
+    const int nt = d.T - t0 < 256 ? d.T - t0 : 256;
+    const int nk = nt - l0 < 2 ? nt - l0 : 2;
+    if (nk > 0) {
+      const PatchStage& st = sm.st[s];
+      float4 A[2], B[2];
+      float C[2];
+      uint32_t lid[2];
+      float2 L[2];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int i = j < nk ? l0 + j : l0;
+        A[j] = st.dma[i];
+        B[j] = st.dmb[i];
+        C[j] = st.dmc[i];
+        lid[j] = st.lid[i];
+        L[j] = kFirst ? make_float2(0.f, 0.f) : st.lam[i];
+      }
+      project_chain<kBlockMode, kPrecise, 2>(A, B, C, lid, L, d.lam + t0 + l0, nk, sm.sp[s], sm.sg[s], d.dx, cD, cH,
+                                             relax_h, relax_d, d.paired != 0);
+    }
+    __syncthreads();  // stage s is refilled two iterations later
+  }
+  cp_async_wait<0>();
+  if (abort_flag && tid == 0) {
+    mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[k & 1]), (k >> 1) & 1, kMaxPolls);
+    if (issued_next) mbar_wait(reinterpret_cast<uint64_t*>(&sm.bar[(k & 1) ^ 1]), ((k + 1) >> 1) & 1, kMaxPolls);
+  }
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -855,19 +957,38 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) k_project
   uint32_t lid[kTPT];
   float2 L[kTPT];
   const uint64_t pol = l2_policy(d.l2_keep != 0);
+  if (kTPT == 2 && l0 + 1 < nt) {  // a full pair: one load per record array
+    const int t = t0 + l0;
+    ldg_pair(d.dm_a + t, pol, A[0], A[1]);
+    ldg_pair(d.dm_b + t, pol, B[0], B[1]);
+    const float2 c = ldg_pair(d.dm_c + t, pol);
+    const uint2 li = ldg_pair(d.lid + t, pol);
+    C[0] = c.x;
+    C[1] = c.y;
+    lid[0] = li.x;
+    lid[1] = li.y;
+    if (!kFirst) {
+      const float4 l2 = *reinterpret_cast<const float4*>(d.lam + t);
+      L[0] = make_float2(l2.x, l2.y);
+      L[1] = make_float2(l2.z, l2.w);
+    } else {
+      L[0] = L[1] = make_float2(0.f, 0.f);
+    }
+  } else {
 #pragma unroll
-  for (int k = 0; k < kTPT; ++k) {
-    A[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    B[k] = A[k];
-    C[k] = 0.f;
-    lid[k] = 0u;
-    L[k] = make_float2(0.f, 0.f);
-    if (l0 + k < nt) {
-      A[k] = ldg_hint(d.dm_a + t0 + l0 + k, pol);
-      B[k] = ldg_hint(d.dm_b + t0 + l0 + k, pol);
-      C[k] = ldg_hint(d.dm_c + t0 + l0 + k, pol);
-      lid[k] = ldg_hint(d.lid + t0 + l0 + k, pol);
-      if (!kFirst) L[k] = d.lam[t0 + l0 + k];
+    for (int k = 0; k < kTPT; ++k) {
+      A[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      B[k] = A[k];
+      C[k] = 0.f;
+      lid[k] = 0u;
+      L[k] = make_float2(0.f, 0.f);
+      if (l0 + k < nt) {
+        A[k] = ldg_hint(d.dm_a + t0 + l0 + k, pol);
+        B[k] = ldg_hint(d.dm_b + t0 + l0 + k, pol);
+        C[k] = ldg_hint(d.dm_c + t0 + l0 + k, pol);
+        lid[k] = ldg_hint(d.lid + t0 + l0 + k, pol);
+        if (!kFirst) L[k] = d.lam[t0 + l0 + k];
+      }
     }
   }
   const float4* P = d.p[cur];
@@ -947,14 +1068,31 @@ __global__ void __launch_bounds__(kP / kTPT) k_residual_patchN(Dev d, SweepArgs 
     float C[kTPT];
     uint32_t lid[kTPT];
     float2 L[kTPT];
+    if (kTPT == 2 && t0 + 1 < d.T) {  // a full pair: one load per record array
+      ldg_pair(d.dm_a + t0, pol, A[0], A[1]);
+      ldg_pair(d.dm_b + t0, pol, B[0], B[1]);
+      const float2 c = ldg_pair(d.dm_c + t0, pol);
+      const uint2 li = ldg_pair(d.lid + t0, pol);
+      C[0] = c.x;
+      C[1] = c.y;
+      lid[0] = li.x;
+      lid[1] = li.y;
+      L[0] = L[1] = make_float2(0.f, 0.f);
+      if (kRes) {
+        const float4 l2 = *reinterpret_cast<const float4*>(d.lam + t0);
+        L[0] = make_float2(l2.x, l2.y);
+        L[1] = make_float2(l2.z, l2.w);
+      }
+    } else {
 #pragma unroll
-    for (int k = 0; k < kTPT; ++k) {
-      if (t0 + k < d.T) {
-        A[k] = ldg_hint(d.dm_a + t0 + k, pol);
-        B[k] = ldg_hint(d.dm_b + t0 + k, pol);
-        C[k] = ldg_hint(d.dm_c + t0 + k, pol);
-        lid[k] = ldg_hint(d.lid + t0 + k, pol);
-        L[k] = kRes ? d.lam[t0 + k] : make_float2(0.f, 0.f);
+      for (int k = 0; k < kTPT; ++k) {
+        if (t0 + k < d.T) {
+          A[k] = ldg_hint(d.dm_a + t0 + k, pol);
+          B[k] = ldg_hint(d.dm_b + t0 + k, pol);
+          C[k] = ldg_hint(d.dm_c + t0 + k, pol);
+          lid[k] = ldg_hint(d.lid + t0 + k, pol);
+          L[k] = kRes ? d.lam[t0 + k] : make_float2(0.f, 0.f);
+        }
       }
     }
     __syncthreads();  // the previous patch's readers are done with sp
@@ -1232,6 +1370,7 @@ struct Solver {
   int sm_count = 0;
   int res_grid = 0;        // grid of the grid-stride residual kernels
   int patch_grid = 0;      // grid of the persistent tile kernels
+  int patch2_grid = 0;     // grid of the persistent two-tets-per-thread tile projection
   int patch1_grid = 0;     // grid of the one-CTA-per-patch residual
   int patchN_grid = 0;     // grid of the two-tets-per-thread residual
   int tile_res_grid = 0;   // grid of the pipelined tile residual
@@ -1337,7 +1476,11 @@ void launch_project_t(Solver* s, float cD, float cH, cudaStream_t st) {
 template <bool kBlockMode, bool kFirst, bool kPrecise, int kP>
 void launch_project_patch_p(Solver* s, float cD, float cH, cudaStream_t st) {
   const xpbd_params& p = s->prm;
-  if (p.patch_pipeline == 1 && kP == 256) {
+  if (p.patch_pipeline == 1 && kP == 256 && p.tets_per_thread == 2) {
+    const int g = s->d.n_patches < s->patch2_grid ? s->d.n_patches : s->patch2_grid;
+    k_project_tile2<kBlockMode, kFirst, kPrecise><<<g, 128, sizeof(TileSmem<false>), st>>>(
+        s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
+  } else if (p.patch_pipeline == 1 && kP == 256) {
     const int g = s->d.n_patches < s->patch_grid ? s->d.n_patches : s->patch_grid;
     k_project_tile<kBlockMode, kFirst, kPrecise><<<g, 256, sizeof(TileSmem<false>), st>>>(
         s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
@@ -1810,6 +1953,12 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
         bps < 1)
       bps = 2;
     s->patch_grid = s->sm_count * bps;
+    bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_project_tile2<true, false, true>, 128,
+                                                      sizeof(TileSmem<false>)) != cudaSuccess ||
+        bps < 1)
+      bps = 2;
+    s->patch2_grid = s->sm_count * bps;
     bps = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_residual_tile<true, false, true>, 256,
                                                       sizeof(TileSmem<true>)) != cudaSuccess ||

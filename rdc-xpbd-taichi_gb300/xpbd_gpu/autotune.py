@@ -31,7 +31,7 @@ from xpbd_gpu import _native
 
 # (scatter, patch_tets, tets_per_thread, patch_pipeline); grouped by device layout
 SINGLE_CANDIDATES = (
-    ("patch", 256, 2, 0), ("patch", 256, 1, 0), ("patch", 256, 4, 0), ("patch", 256, 1, 1),
+    ("patch", 256, 2, 0), ("patch", 256, 1, 0), ("patch", 256, 4, 0), ("patch", 256, 2, 1), ("patch", 256, 1, 1),
     ("patch", 128, 2, 0), ("patch", 128, 1, 0),
     ("patch", 64, 2, 0), ("patch", 64, 1, 0),
     ("atomic", 0, 1, 0), ("gather", 0, 1, 0),

@@ -34,12 +34,14 @@ def make_solver(d, **over):
 
 
 @pytest.mark.parametrize("name", gc.golden_names())
-@pytest.mark.parametrize("scatter", ["atomic", "gather", "patch", "patch-tma", "patch-reduce", "patch-1tpt",
-                                     "patch-4tpt"])
+@pytest.mark.parametrize("scatter", ["atomic", "gather", "patch", "patch-tma", "patch-tma-1tpt", "patch-reduce",
+                                     "patch-1tpt", "patch-4tpt"])
 def test_frames_match_reference(name, scatter):
     d = gc.load(name)
     if scatter == "patch-tma":
         s = make_solver(d, scatter="patch", patch_pipeline=1, monitor_convergence=False)
+    elif scatter == "patch-tma-1tpt":
+        s = make_solver(d, scatter="patch", patch_pipeline=1, tets_per_thread=1, monitor_convergence=False)
     elif scatter == "patch-reduce":
         s = make_solver(d, scatter="patch", patch_reduce=1, monitor_convergence=False)
     elif scatter == "patch-1tpt":
