@@ -100,6 +100,7 @@ struct BDev {
   // stop mode: parity of the launched iteration (its index & 1), whose index
   // the kernels read from ctl->it[stop_par]; -1 = fixed iteration count
   int stop_par;
+  float2* lam_tape;  // taping: the projection also stores the multipliers entering it here (nullptr: none)
 };
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
@@ -318,11 +319,13 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) kb_projec
   if (n <= 0) return;
   if (kTetMat) {
     project_chain<kBlockMode, kPrecise, kTPT, true>(A, B, C, lid, L, d.lam + t0, n, sp, sg, d.dx, inv_dt2, inv_dt2,
-                                                    relax_h, relax_d, d.paired != 0, mD, mH);
+                                                    relax_h, relax_d, d.paired != 0, mD, mH,
+                                                    d.lam_tape ? d.lam_tape + t0 : nullptr);
   } else {
     const float cD = __ldg(d.inv_mu + b) * inv_dt2, cH = __ldg(d.inv_la + b) * inv_dt2;
     project_chain<kBlockMode, kPrecise, kTPT>(A, B, C, lid, L, d.lam + t0, n, sp, sg, d.dx, cD, cH, relax_h,
-                                              relax_d, d.paired != 0);
+                                              relax_d, d.paired != 0, nullptr, nullptr,
+                                              d.lam_tape ? d.lam_tape + t0 : nullptr);
   }
 }
 
@@ -557,6 +560,7 @@ struct BUpd {
   int use_cond;
   cudaGraphConditionalHandle cond;
   float4* post_out;  // taping through omega: the post-Jacobi positions (nullptr: none)
+  float4* xs_out;    // taping: the positions entering the next iteration (nullptr: none)
 };
 
 template <bool kCheb, bool kFirstIt>
@@ -603,15 +607,19 @@ __global__ void __launch_bounds__(256) kb_update(BDev d, int cur, float gamma, B
     d.dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     const float3 xp = post_position(pc[k], D[k]);
     if (u.post_out) u.post_out[i] = make_float4(xp.x, xp.y, xp.z, pc[k].w);
+    float4 xo;
     if (kCheb) {
       const float nx = gamma * (xp.x - pc[k].x) + pc[k].x;
       const float ny = gamma * (xp.y - pc[k].y) + pc[k].y;
       const float nz = gamma * (xp.z - pc[k].z) + pc[k].z;
-      d.p[cur ^ 1][i] = make_float4(yp[k].x + om[k] * (nx - yp[k].x), yp[k].y + om[k] * (ny - yp[k].y),
-                                    yp[k].z + om[k] * (nz - yp[k].z), pc[k].w);
+      xo = make_float4(yp[k].x + om[k] * (nx - yp[k].x), yp[k].y + om[k] * (ny - yp[k].y),
+                       yp[k].z + om[k] * (nz - yp[k].z), pc[k].w);
+      d.p[cur ^ 1][i] = xo;
     } else {
-      d.p[cur][i] = make_float4(xp.x, xp.y, xp.z, pc[k].w);
+      xo = make_float4(xp.x, xp.y, xp.z, pc[k].w);
+      d.p[cur][i] = xo;
     }
+    if (u.xs_out) u.xs_out[i] = xo;
   }
 }
 
@@ -935,6 +943,7 @@ struct Batch {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaStream_t aux_body = nullptr;  // the same inside the body of a loop node
   float4* tape_post = nullptr;      // taping through omega: where the update writes post-Jacobi positions
+  float4* tape_xs = nullptr;        // taping: where the update writes the next iteration's positions
   cudaEvent_t ev_fork_body = nullptr, ev_join_body = nullptr;
   cudaGraphExec_t exec = nullptr;
   double key_frame_dt = -1, key_dt = -1;
@@ -1085,6 +1094,7 @@ int iteration_b(Batch* s, bool first, int par, float dt, int rec_base, cudaStrea
   u.use_cond = cond != nullptr;
   if (cond) u.cond = *cond;
   u.post_out = s->tape_post;
+  u.xs_out = s->tape_xs;
   if (cheb) {
     if (first) kb_update<true, true><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
     else kb_update<true, false><<<g, 256, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
@@ -1617,19 +1627,23 @@ int xpbd_batch_substep_tape(void* h, float dt, const xpbd_tape* tape, void* stre
   k_tape_begin<BDev><<<nblk(V), 256, 0, st>>>(s->d, tp, dt, g[0], g[1], g[2]);
   s->cur = 0;
   kb_begin<<<nblk(V), 256, 0, st>>>(s->d, dt, g[0], g[1], g[2], K);
+  // iteration 0 enters with the predicted positions and zero multipliers; after
+  // it the projection records the multipliers entering each iteration and the
+  // update the positions entering the next (xs[K]: those after the last)
+  B_CUDA(cudaMemcpyAsync(tp.xs, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
+  B_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
   for (int it = 0; it < K; ++it) {
-    B_CUDA(cudaMemcpyAsync(tp.xs + (size_t)it * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
-    if (it == 0) B_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
-    else
-      B_CUDA(cudaMemcpyAsync(tp.lams + (size_t)it * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
+    s->d.lam_tape = it > 0 ? tp.lams + (size_t)it * T : nullptr;
     s->tape_post = tp.posts ? tp.posts + (size_t)it * V : nullptr;
+    s->tape_xs = tp.xs + (size_t)(it + 1) * V;
     const int r = iteration_b(s, it == 0, it & 1, dt, 0, st, nullptr, Fork{s->aux, s->ev_fork, s->ev_join});
+    s->d.lam_tape = nullptr;
     s->tape_post = nullptr;
+    s->tape_xs = nullptr;
     if (r) return r;
   }
   if (tp.posts)  // the multipliers after the last iteration (the residual's lambda_K)
     B_CUDA(cudaMemcpyAsync(tp.lams + (size_t)K * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
-  B_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
   if (tape->hist)  // rows 0..K-1 of every body
     B_CUDA(cudaMemcpy2DAsync(tape->hist, sizeof(double) * 4 * (size_t)K, s->d.hist,
                              sizeof(double) * 4 * (size_t)s->d.max_records, sizeof(double) * 4 * (size_t)K,

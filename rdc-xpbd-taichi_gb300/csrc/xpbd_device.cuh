@@ -432,13 +432,15 @@ __device__ __forceinline__ void add4(float4& a, const float4 b) {
 // packed patch-local ids) merges its three shared corners without comparisons.  cD, cH: time-scaled inverse Lame parameters;
 // the tet's compliances are 6 det(inv_Dm) cD and 6 det(inv_Dm) cH (1 / V0).
 // kTetMat: per-tet materials, the compliances are further multiplied by the
-// tet's 1 / mu and 1 / lambda (mD[k], mH[k]).
+// tet's 1 / mu and 1 / lambda (mD[k], mH[k]).  lam_in (taping): the
+// multipliers entering the iteration are also stored there.
 template <bool kBlockMode, bool kPrecise, int kTPT, bool kTetMat = false>
 __device__ __forceinline__ void project_chain(const float4 (&A)[kTPT], const float4 (&B)[kTPT], const float (&C)[kTPT],
                                               const uint32_t (&lid)[kTPT], float2 (&L)[kTPT], float2* lam_out,
                                               int n, const float4* sp, const int* sg, float4* dx, float cD,
                                               float cH, float relax_h, float relax_d, bool paired,
-                                              const float* mD = nullptr, const float* mH = nullptr) {
+                                              const float* mD = nullptr, const float* mH = nullptr,
+                                              float2* lam_in = nullptr) {
   float4 acc[4];
   int hid[4] = {-1, -1, -1, -1};
 #pragma unroll
@@ -457,6 +459,7 @@ __device__ __forceinline__ void project_chain(const float4 (&A)[kTPT], const flo
     const float six_det = 6.f * det9(tt.dm);
     float3 dp[4];
     float cnt;
+    if (lam_in) lam_in[k] = L[k];
     if (kTetMat)
       project_tet<kBlockMode, kPrecise>(tt, six_det * (cD * mD[k]), six_det * (cH * mH[k]), relax_h, relax_d, L[k],
                                         dp, cnt);
