@@ -100,6 +100,7 @@ struct Dev {
   // slot entering the launched iteration; nullptr = always run
   const int* act;
   int dyn_end;  // stop mode: advance and the vertex-field accessors read p[st->pos_cur]
+  float2* lam_tape;  // taping (ATOMIC / GATHER projection): the multipliers entering the iteration (nullptr: none)
 };
 
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
@@ -209,6 +210,7 @@ struct UpdArgs {
   int use_cond;  // set the frame graph's loop condition (cond)
   cudaGraphConditionalHandle cond;
   float4* post_out;  // taping through omega: the post-Jacobi positions (nullptr: none)
+  float4* xs_out;    // taping: the positions entering the next iteration (nullptr: none)
   double inv_n;  // 1 / tet count (0 for an empty mesh)
   double rho_min, rho_max, rho_beta;
   double target, floor;  // stop at r_hat <= target * r_hat_0 or r_hat <= floor
@@ -329,15 +331,19 @@ __global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma, 
       xp.z += D[k].z / D[k].w;
     }
     if (u.post_out) u.post_out[i] = make_float4(xp.x, xp.y, xp.z, pc[k].w);
+    float4 xo;
     if (kCheb) {
       const float nx = gamma * (xp.x - pc[k].x) + pc[k].x;
       const float ny = gamma * (xp.y - pc[k].y) + pc[k].y;
       const float nz = gamma * (xp.z - pc[k].z) + pc[k].z;
-      d.p[cur ^ 1][i] = make_float4(yp[k].x + om * (nx - yp[k].x), yp[k].y + om * (ny - yp[k].y),
-                                    yp[k].z + om * (nz - yp[k].z), pc[k].w);
+      xo = make_float4(yp[k].x + om * (nx - yp[k].x), yp[k].y + om * (ny - yp[k].y),
+                       yp[k].z + om * (nz - yp[k].z), pc[k].w);
+      d.p[cur ^ 1][i] = xo;
     } else {
-      d.p[cur][i] = make_float4(xp.x, xp.y, xp.z, pc[k].w);
+      xo = make_float4(xp.x, xp.y, xp.z, pc[k].w);
+      d.p[cur][i] = xo;
     }
+    if (u.xs_out) u.xs_out[i] = xo;
   }
 }
 
@@ -385,6 +391,7 @@ __global__ void __launch_bounds__(kBlock) k_project(Dev d, int cur, float cD, fl
   tt.p[2] = ldg4(P + id.z);
   tt.p[3] = ldg4(P + id.w);
   float2 L = kFirst ? make_float2(0.f, 0.f) : d.lam[t];
+  if (d.lam_tape) d.lam_tape[t] = L;
   const int vid[4] = {id.x, id.y, id.z, id.w};
   float3 dp[4];
   float cnt;
@@ -1379,6 +1386,7 @@ struct Solver {
   cudaStream_t cap = nullptr;
   cudaStream_t cap_body = nullptr;  // captures the body of a stop-mode loop node
   float4* tape_post = nullptr;      // taping through omega: where the update writes post-Jacobi positions
+  float4* tape_xs = nullptr;        // taping: where the update writes the next iteration's positions
   cudaGraphExec_t exec = nullptr;
   GraphKey key;
   // profiling with use_graph: the frame graph carries an event record node
@@ -1629,6 +1637,7 @@ void launch_iteration(Solver* s, bool first, int par, float dt, int rec_base, in
   u.use_cond = cond != nullptr;
   if (cond) u.cond = *cond;
   u.post_out = s->tape_post;
+  u.xs_out = s->tape_xs;
   u.inv_n = s->d.T > 0 ? 1.0 / (double)s->d.T : 0.0;
   u.rho_min = p.rho_min;
   u.rho_max = p.rho_max;
@@ -2315,18 +2324,22 @@ int xpbd_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* strea
   k_tape_begin<Dev><<<blocks_for(V), kBlock, 0, st>>>(s->d, tp, dt, g[0], g[1], g[2]);
   s->cur = 0;
   launch_begin(s, true, true, dt, st);
+  // iteration 0 enters with the predicted positions and zero multipliers; after
+  // it the projection records the multipliers entering each iteration and the
+  // update the positions entering the next (xs[K]: those after the last)
+  XPBD_CUDA(cudaMemcpyAsync(tp.xs, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
+  XPBD_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
   for (int it = 0; it < K; ++it) {
-    XPBD_CUDA(cudaMemcpyAsync(tp.xs + (size_t)it * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
-    if (it == 0) XPBD_CUDA(cudaMemsetAsync(tp.lams, 0, sizeof(float2) * T, st));
-    else
-      XPBD_CUDA(cudaMemcpyAsync(tp.lams + (size_t)it * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
+    s->d.lam_tape = it > 0 ? tp.lams + (size_t)it * T : nullptr;
     s->tape_post = tp.posts ? tp.posts + (size_t)it * V : nullptr;
+    s->tape_xs = tp.xs + (size_t)(it + 1) * V;
     launch_iteration(s, it == 0, it & 1, dt, 0, -1, st, nullptr);
+    s->d.lam_tape = nullptr;
     s->tape_post = nullptr;
+    s->tape_xs = nullptr;
   }
   if (tp.posts)  // the multipliers after the last iteration (the residual's lambda_K)
     XPBD_CUDA(cudaMemcpyAsync(tp.lams + (size_t)K * T, s->d.lam, sizeof(float2) * T, cudaMemcpyDeviceToDevice, st));
-  XPBD_CUDA(cudaMemcpyAsync(tp.xs + (size_t)K * V, s->d.p[s->cur], sizeof(float4) * V, cudaMemcpyDeviceToDevice, st));
   if (tape->hist)
     XPBD_CUDA(cudaMemcpyAsync(tape->hist, s->d.hist, sizeof(double) * 4 * (size_t)K, cudaMemcpyDeviceToDevice, st));
   k_end<<<blocks_for(V), kBlock, 0, st>>>(s->d, s->cur, dt, s->prm.damping);
