@@ -124,7 +124,7 @@ class _Tapes:
         f32 = dict(dtype=torch.float32, device=dev)
         f64 = dict(dtype=torch.float64, device=dev)
         self.xs = torch.empty((n, (K + 1) * V, 4), **f32)
-        self.lams = torch.empty((n, sim._lams.shape[0], 2), **f32)
+        self.lams = torch.empty((n, _lam_rows(sim), 2), **f32)
         self.xpre = torch.empty((n, V, 4), **f32)
         self.v1 = torch.empty((n, V, 4), **f32)
         self.posts = torch.empty((n, K * V, 4), **f32) if sim.omega_grad else None
@@ -137,10 +137,16 @@ class _Tapes:
     @staticmethod
     def nbytes(sim, n):
         V, T, K, nb = sim.V, sim.T, sim.K, sim.n_rho
-        per = 16 * ((K + 1) * V + 2 * V) + 8 * sim._lams.shape[0] + 32 * nb * K
+        per = 16 * ((K + 1) * V + 2 * V) + 8 * _lam_rows(sim) + 32 * nb * K
         if sim.omega_grad:
             per += 16 * K * V + 8 * nb
         return n * per
+
+
+def _lam_rows(sim):
+    """Multiplier rows of one tape: those entering every iteration, and with
+    omega_grad those after the last."""
+    return (sim.K + 1 if sim.omega_grad else max(sim.K, 1)) * sim.T
 
 
 def _plan(sim, frames):
@@ -197,7 +203,7 @@ class DiffSim:
         f4 = lambda n: torch.zeros((n, 4), dtype=torch.float32, device=dev)
         self.omega_grad = bool(omega_grad)
         self._xs = torch.zeros(((K + 1) * V, 4), dtype=torch.float32, device=dev)
-        self._lams = torch.zeros(((K + 1 if omega_grad else max(K, 1)) * T, 2), dtype=torch.float32, device=dev)
+        self._lams = torch.zeros((_lam_rows(self), 2), dtype=torch.float32, device=dev)
         self._xpre, self._v1 = f4(V), f4(V)
         self._gx, self._gv = f4(V), f4(V)
         self._w0, self._w1, self._yb, self._dxb = f4(V), f4(V), f4(V), f4(V)

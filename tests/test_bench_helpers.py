@@ -37,3 +37,25 @@ def test_c3_workload_shape():
     assert E.min() >= 1e4 and E.max() <= 1e7
     assert nu.min() >= 0.30 and nu.max() <= 0.495
     assert sum(1 for k, _ in specs if k == "sphere") == 32
+
+
+def test_matrix_scene_is_the_reference_comparison():
+    """bench.py --workload matrix uses the scene of the reference's convergence
+    comparison (scripts/compare_convergence_armadillo.bat:14-17 with the
+    driver's scene, run_neohookean_usd.py:82-106)."""
+    import bench
+
+    class A:
+        matrix_scale = 0.01
+    kw, sdfs = bench.matrix_scene(A)
+    assert kw["scale"] == 0.01 and kw["offset"] == (0.0, 1.0, 0.0)
+    assert kw["young_modulus"] == 5e8 and kw["poisson_ratio"] == 0.4999
+    assert kw["dt"] == 0.01 and abs(kw["frame_dt"] - 1.0 / 60) < 1e-15
+    assert kw["substeps_num"] == 1 and kw["constraints_iter"] == 200
+    assert kw["cheb_warmup"] == 5 and kw["cheb_gamma"] == 0.666
+    assert kw["hydrostatic_relaxation"] == 1.2 and kw["deviatoric_relaxation"] == 1.2
+    assert kw["monitor_convergence"]
+    assert [k for k, _ in sdfs] == ["plane", "sphere"]
+    assert sdfs[0][1]["point"] == [0.0, -2.0, 0.0] and sdfs[1][1]["radius"] == 0.3
+    assert [(lab, b, c) for lab, b, c in bench.MATRIX] == [("NH", False, False), ("NH-DC", False, True),
+                                                           ("BNH", True, False), ("BNH-DC", True, True)]
