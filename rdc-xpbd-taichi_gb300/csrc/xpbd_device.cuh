@@ -264,6 +264,17 @@ __device__ __forceinline__ void sdf_project_all(const xpbd_sdf* __restrict__ sdf
   }
 }
 
+// Programmatic dependent launch (sm_90+).  A kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may start while its
+// predecessor in the stream drains.  pdl_wait() returns once the predecessor
+// has completed and its writes are visible (without the attribute it returns
+// at once); pdl_trigger() lets the successor launch.  Every kernel of such a
+// chain waits before it triggers, so when a kernel starts, every kernel
+// before its immediate predecessor has completed: what those wrote may be
+// read before pdl_wait().
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Vector reduction into global memory: red.global.add.v4.f32 (sm_90+).
 __device__ __forceinline__ void red_add_v4(float4* addr, float a, float b, float c, float d) {
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c), "f"(d)

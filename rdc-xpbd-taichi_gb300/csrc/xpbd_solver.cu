@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <mutex>
 #include <new>
 #include <string>
@@ -211,6 +212,7 @@ struct UpdArgs {
   cudaGraphConditionalHandle cond;
   float4* post_out;  // taping through omega: the post-Jacobi positions (nullptr: none)
   float4* xs_out;    // taping: the positions entering the next iteration (nullptr: none)
+  int pre;           // a residual sweep ran between the projection and this update
   double inv_n;  // 1 / tet count (0 for an empty mesh)
   double rho_min, rho_max, rho_beta;
   double target, floor;  // stop at r_hat <= target * r_hat_0 or r_hat <= floor
@@ -299,6 +301,9 @@ __global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma, 
   // every load is issued before the first store: as far as the compiler
   // knows the buffers may alias, so a load after a store would wait for it
   float4 pc[kUpdateVerts], D[kUpdateVerts], yp[kUpdateVerts];
+  // after a residual sweep the positions and Jacobi sums were written two or
+  // more kernels back; straight after the projection the sums are not yet
+  if (!u.pre) pdl_wait();
 #pragma unroll
   for (int k = 0; k < kUpdateVerts; ++k) {
     const int i = base + k * kBlock;
@@ -308,6 +313,8 @@ __global__ void __launch_bounds__(kBlock) k_update(Dev d, int cur, float gamma, 
       yp[k] = (kCheb && !kFirstIt) ? d.p[cur ^ 1][i] : pc[k];
     }
   }
+  if (u.pre) pdl_wait();  // the residual's sums (sweep_step), and the stores below
+  pdl_trigger();
   __shared__ float s_om;
   __shared__ int s_run;
   if (threadIdx.x == 0) {
@@ -998,6 +1005,10 @@ __global__ void __launch_bounds__(kP / kTPT, project_min_blocks(kTPT)) k_project
       }
     }
   }
+  // the records and multipliers above were written two kernels back; the
+  // positions come from the update that precedes this launch
+  pdl_wait();
+  pdl_trigger();
   const float4* P = d.p[cur];
   for (int j = threadIdx.x; j < nv; j += kThreads) {
     const int g = ldg_hint(d.pverts + vb + j, pol);
@@ -1058,6 +1069,8 @@ __global__ void __launch_bounds__(kP) k_residual_patch1(Dev d, SweepArgs a) {
 // the vertex tile lets both sets of loads be in flight together.
 template <bool kRes, bool kMon, bool kPrecise, int kP, int kTPT>
 __global__ void __launch_bounds__(kP / kTPT) k_residual_patchN(Dev d, SweepArgs a) {
+  pdl_wait();  // the Jacobi sums and multipliers of the projection before it
+  pdl_trigger();
   if (stopped(d)) return;
   constexpr int kThreads = kP / kTPT;
   __shared__ float4 sp[256];
@@ -1366,6 +1379,11 @@ struct GraphKey {
 struct Solver {
   // profiling (xpbd_set_profiling): event pairs per kernel class
   bool profiling = false;
+  // programmatic dependent launch of the iteration's kernels (off with
+  // XPBD_NO_PDL=1 in the environment at creation); pdl_now: the launch being
+  // issued may overlap its predecessor
+  bool pdl = true;
+  bool pdl_now = false;
   int l2_auto = 0;  // automatic L2 policy of the tile sweeps (xpbd_set_l2_hint)
   std::vector<cudaEvent_t> pool;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[XPBD_K_COUNT];
@@ -1440,6 +1458,24 @@ struct Prof {
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
+// Launch `k` on `st`; with `overlap` it may start while its predecessor in the
+// stream drains (programmatic dependent launch: the kernel calls pdl_wait()
+// before it reads what the predecessor writes).
+template <typename... KArgs, typename... Args>
+void launch_k(void (*k)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, bool overlap, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = overlap ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 int check_params(const xpbd_params* p) {
   if (!p) return fail(XPBD_ERR_INVALID_ARGUMENT, "params is NULL");
   if (p->constraints_iter < 0) return fail(XPBD_ERR_INVALID_ARGUMENT, "constraints_iter < 0");
@@ -1493,8 +1529,8 @@ void launch_project_patch_p(Solver* s, float cD, float cH, cudaStream_t st) {
     k_project_tile<kBlockMode, kFirst, kPrecise><<<g, 256, sizeof(TileSmem<false>), st>>>(
         s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
   } else if (p.tets_per_thread == 2 && !p.patch_reduce) {
-    k_project_patchN<kBlockMode, kFirst, kPrecise, kP, 2><<<s->d.n_patches, kP / 2, 0, st>>>(
-        s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
+    launch_k(k_project_patchN<kBlockMode, kFirst, kPrecise, kP, 2>, s->d.n_patches, kP / 2, 0, st, s->pdl_now,
+             s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
   } else if (p.tets_per_thread == 4 && !p.patch_reduce) {
     k_project_patchN<kBlockMode, kFirst, kPrecise, kP, 4><<<s->d.n_patches, kP / 4, 0, st>>>(
         s->d, s->cur, cD, cH, p.hydrostatic_relaxation, p.deviatoric_relaxation);
@@ -1557,7 +1593,7 @@ void launch_residual_patch_p(Solver* s, const SweepArgs& a, cudaStream_t st) {
     k_residual_tile<kRes, kMon, kPrecise><<<g, 256, sizeof(TileSmem<true>), st>>>(s->d, a);
   } else if (s->prm.tets_per_thread == 2 && !s->prm.patch_reduce) {
     const int g = n < s->patchN_grid ? n : s->patchN_grid;
-    k_residual_patchN<kRes, kMon, kPrecise, kP, 2><<<g, kP / 2, 0, st>>>(s->d, a);
+    launch_k(k_residual_patchN<kRes, kMon, kPrecise, kP, 2>, g, kP / 2, 0, st, s->pdl_now, s->d, a);
   } else {
     const int g = n < s->patch1_grid ? n : s->patch1_grid;
     k_residual_patch1<kRes, kMon, kPrecise, kP><<<g, kP, 0, st>>>(s->d, a);
@@ -1615,6 +1651,10 @@ void launch_iteration(Solver* s, bool first, int par, float dt, int rec_base, in
   const xpbd_params& p = s->prm;
   const bool stop = stop_mode(p);
   s->d.act = stop ? &s->d.st->slot[par].active : nullptr;
+  // the fixed-count tile path (two tets per thread) launches its kernels so
+  // that each may start while its predecessor drains
+  s->pdl_now = s->pdl && !stop && !s->profiling && p.scatter == XPBD_SCATTER_PATCH && p.tets_per_thread == 2 &&
+               !p.patch_pipeline && !p.patch_reduce;
   launch_project(s, first, dt, st);
   if (p.scatter == XPBD_SCATTER_GATHER) {
     Prof prof(s, XPBD_K_GATHER, st);
@@ -1638,6 +1678,7 @@ void launch_iteration(Solver* s, bool first, int par, float dt, int rec_base, in
   if (cond) u.cond = *cond;
   u.post_out = s->tape_post;
   u.xs_out = s->tape_xs;
+  u.pre = cheb || mon || stop;
   u.inv_n = s->d.T > 0 ? 1.0 / (double)s->d.T : 0.0;
   u.rho_min = p.rho_min;
   u.rho_max = p.rho_max;
@@ -1645,19 +1686,21 @@ void launch_iteration(Solver* s, bool first, int par, float dt, int rec_base, in
   u.target = p.target_rel_residual;
   u.floor = p.residual_floor;
   Prof prof(s, XPBD_K_UPDATE, st);
+  const bool o = s->pdl_now;
   if (cheb) {
     if (first) {
-      if (reset) k_update<true, true, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
-      else k_update<true, true, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
+      if (reset) launch_k(k_update<true, true, true>, g, kBlock, 0, st, o, s->d, s->cur, p.cheb_gamma, u);
+      else launch_k(k_update<true, true, false>, g, kBlock, 0, st, o, s->d, s->cur, p.cheb_gamma, u);
     } else {
-      if (reset) k_update<true, false, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
-      else k_update<true, false, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
+      if (reset) launch_k(k_update<true, false, true>, g, kBlock, 0, st, o, s->d, s->cur, p.cheb_gamma, u);
+      else launch_k(k_update<true, false, false>, g, kBlock, 0, st, o, s->d, s->cur, p.cheb_gamma, u);
     }
     s->cur ^= 1;
   } else {
-    if (reset) k_update<false, false, true><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
-    else k_update<false, false, false><<<g, kBlock, 0, st>>>(s->d, s->cur, p.cheb_gamma, u);
+    if (reset) launch_k(k_update<false, false, true>, g, kBlock, 0, st, o, s->d, s->cur, p.cheb_gamma, u);
+    else launch_k(k_update<false, false, false>, g, kBlock, 0, st, o, s->d, s->cur, p.cheb_gamma, u);
   }
+  s->pdl_now = false;
   s->d.act = nullptr;
 }
 
@@ -1948,6 +1991,8 @@ int xpbd_create(const xpbd_params* params, const xpbd_body* body, const xpbd_sdf
     const double records = 40.0 * d.T + 4.0 * d.n_pverts;
     const double state = 48.0 * d.V + 8.0 * d.T;
     s->l2_auto = records + state <= 0.8 * l2;
+    const char* no_pdl = std::getenv("XPBD_NO_PDL");
+    s->pdl = !(no_pdl && no_pdl[0] == '1');
     d.l2_keep = s->l2_auto;
   }
   {
