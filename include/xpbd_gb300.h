@@ -317,7 +317,9 @@ typedef struct xpbd_adjoint {
  * receive its omegas for xpbd_substep_adjoint. */
 int xpbd_substep_tape(void* handle, float dt, const xpbd_tape* tape, void* stream);
 
-/* Reverse of the substep last run by xpbd_substep_tape with the same tape. */
+/* Reverse of the substep recorded on `tape` by xpbd_substep_tape: the last
+ * one run, or, when the tape holds its history rows (`hist`), any recorded
+ * substep, with the solver's materials and SDFs as they were then. */
 int xpbd_substep_adjoint(void* handle, float dt, const xpbd_tape* tape, const xpbd_adjoint* adj, void* stream);
 
 /* Residual sweep that allocates nothing.  No counterpart in the reference.
