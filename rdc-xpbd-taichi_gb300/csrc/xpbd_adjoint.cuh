@@ -216,6 +216,8 @@ __global__ void __launch_bounds__(256) ka_end(D d, Adj a, float e_over_dt) {
 // abuf[src^1] (direct part of the adjoint of x~_k), ybar and dxbar.
 template <class D, bool kCheb>
 __global__ void __launch_bounds__(256) ka_cheb(D d, Tape tp, Adj a, int k, float gamma, int src) {
+  pdl_wait();  // x~_{k+1}'s adjoint from the tet adjoint before it
+  pdl_trigger();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const float4 xb = i < adj_verts(d) ? adj_buf(a, src)[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   if (kCheb && a.om) {

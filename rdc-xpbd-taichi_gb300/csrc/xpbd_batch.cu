@@ -10,6 +10,7 @@
 // ticket lets the last patch CTA of a body apply that body's rho_hat / omega
 // recurrence (neohookean_solver.py:495-504, :537-546), so bodies never wait
 // for each other and no grid-wide barrier is needed.
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -790,8 +791,10 @@ __global__ void __launch_bounds__(kP, 3) kba_project(BDev d, Tape tp, Adj a, int
       m_la = __ldg(d.inv_la + body);
     }
     L = tp.lams[(size_t)k * d.T + t];
-    lb_next = a.lambar[t];
+    lb_next = a.lambar[t];  // written three kernels back
   }
+  pdl_wait();  // the accumulator adjoints and rtet of the kernels before it
+  pdl_trigger();
   if (a.rtet && live) {  // rtet[t] = (lambda_{k+1} adjoint, material adjoints)
     const float2 r = reinterpret_cast<const float2*>(a.rtet + t)[0];
     lb_next.x += r.x;
@@ -844,6 +847,8 @@ __global__ void __launch_bounds__(kP, 3) kba_project(BDev d, Tape tp, Adj a, int
 // kba_project of iteration k.
 template <bool kPrecise>
 __global__ void __launch_bounds__(kP) kba_residual_adj(BDev d, Tape tp, Adj a, int k, float c, int dst) {
+  pdl_wait();  // omega_k's adjoint summed by ka_cheb before it
+  pdl_trigger();
   __shared__ float4 sp[256];
   __shared__ int sg[256];
   __shared__ float s_rb;
@@ -949,6 +954,7 @@ struct Batch {
   double key_frame_dt = -1, key_dt = -1;
   int key_sub = -1;
   bool profiling = false;
+  bool pdl = true;  // programmatic dependent launch of the reverse iterations (off with XPBD_NO_PDL=1)
   std::vector<cudaEvent_t> pool;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending[XPBD_K_COUNT];
   double prof_ms[XPBD_K_COUNT] = {0, 0, 0, 0, 0, 0};
@@ -1226,6 +1232,10 @@ int xpbd_batch_create(const xpbd_params* params, const xpbd_batch* body, const x
   if (!(params->target_rel_residual >= 0.0) || !(params->residual_floor >= 0.0))
     return bfail(XPBD_ERR_INVALID_ARGUMENT, "target_rel_residual and residual_floor must be >= 0");
   Batch* s = new (std::nothrow) Batch();
+  if (s) {
+    const char* no_pdl = std::getenv("XPBD_NO_PDL");
+    s->pdl = !(no_pdl && no_pdl[0] == '1');
+  }
   if (!s) return bfail(XPBD_ERR_INVALID_ARGUMENT, "out of host memory");
   s->prm = *params;
   s->d.stop_par = -1;
@@ -1695,15 +1705,19 @@ int xpbd_batch_substep_adjoint(void* h, float dt, const xpbd_tape* tape, const x
   ka_end<BDev><<<nblk(V), 256, 0, st>>>(dv, a, e_over_dt);
   const float c = (float)(1.0 / ((double)dt * (double)dt));
   int src = 0;
+  // the reverse iterations' kernels may each start while the one before
+  // drains (programmatic dependent launch; they wait before reading its output)
+  const bool o = s->pdl && !s->profiling;
+  const int np = s->d.n_patches;
   for (int k = K - 1; k >= 0; --k) {
-    if (s->prm.cheb_enable) ka_cheb<BDev, true><<<nblk(V), 256, 0, st>>>(dv, tp, a, k, s->prm.cheb_gamma, src);
-    else ka_cheb<BDev, false><<<nblk(V), 256, 0, st>>>(dv, tp, a, k, s->prm.cheb_gamma, src);
+    if (s->prm.cheb_enable) launch_k(ka_cheb<BDev, true>, nblk(V), 256, 0, st, o, dv, tp, a, k, s->prm.cheb_gamma, src);
+    else launch_k(ka_cheb<BDev, false>, nblk(V), 256, 0, st, o, dv, tp, a, k, s->prm.cheb_gamma, src);
     if (through_omega) {
-      if (s->prm.precise_hydro) kba_residual_adj<true><<<s->d.n_patches, kP, 0, st>>>(dv, tp, a, k, c, src ^ 1);
-      else kba_residual_adj<false><<<s->d.n_patches, kP, 0, st>>>(dv, tp, a, k, c, src ^ 1);
+      if (s->prm.precise_hydro) launch_k(kba_residual_adj<true>, np, kP, 0, st, o, dv, tp, a, k, c, src ^ 1);
+      else launch_k(kba_residual_adj<false>, np, kP, 0, st, o, dv, tp, a, k, c, src ^ 1);
     }
-    if (s->prm.precise_hydro) kba_project<true><<<s->d.n_patches, kP, 0, st>>>(dv, tp, a, k, c, src ^ 1);
-    else kba_project<false><<<s->d.n_patches, kP, 0, st>>>(dv, tp, a, k, c, src ^ 1);
+    if (s->prm.precise_hydro) launch_k(kba_project<true>, np, kP, 0, st, o, dv, tp, a, k, c, src ^ 1);
+    else launch_k(kba_project<false>, np, kP, 0, st, o, dv, tp, a, k, c, src ^ 1);
     src ^= 1;
   }
   ka_begin<BDev><<<nblk(V), 256, 0, st>>>(dv, tp, a, src, dt);

@@ -275,6 +275,24 @@ __device__ __forceinline__ void sdf_project_all(const xpbd_sdf* __restrict__ sdf
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// Launch `k` on `st`; with `overlap` it may start while its predecessor in the
+// stream drains (programmatic dependent launch: the kernel calls pdl_wait()
+// before it reads what the predecessor writes).
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*k)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, bool overlap, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = overlap ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Vector reduction into global memory: red.global.add.v4.f32 (sm_90+).
 __device__ __forceinline__ void red_add_v4(float4* addr, float a, float b, float c, float d) {
   asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c), "f"(d)

@@ -1458,23 +1458,6 @@ struct Prof {
 
 inline int blocks_for(int n) { return (n + kBlock - 1) / kBlock; }
 
-// Launch `k` on `st`; with `overlap` it may start while its predecessor in the
-// stream drains (programmatic dependent launch: the kernel calls pdl_wait()
-// before it reads what the predecessor writes).
-template <typename... KArgs, typename... Args>
-void launch_k(void (*k)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, bool overlap, Args... args) {
-  cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3((unsigned)block);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = overlap ? 1 : 0;
-  cudaLaunchKernelEx(&cfg, k, args...);
-}
 
 int check_params(const xpbd_params* p) {
   if (!p) return fail(XPBD_ERR_INVALID_ARGUMENT, "params is NULL");
