@@ -8,7 +8,8 @@ difference over the norm of the gradient), on a body with plane, sphere and
 moving-box contact: with the adjoint run back through the Chebyshev omega
 (omega_grad, the derivative of the forward as it runs) and with omega as a
 stop-gradient, with the tapes stored by the forward and recomputed by the
-backward.
+backward, and with the forward scattering by atomics or by the deterministic
+gather.
 """
 import numpy as np
 import pytest
@@ -20,11 +21,15 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-@pytest.mark.parametrize("cheb,omega_grad,tape_memory,iters", [
-    (True, True, "store", 8), (True, True, "recompute", 8), (True, False, "store", 8), (False, False, "recompute", 8),
+@pytest.mark.parametrize("cheb,omega_grad,tape_memory,iters,scatter", [
+    (True, True, "store", 8, "atomic"), (True, True, "recompute", 8, "atomic"), (True, False, "store", 8, "atomic"),
+    (False, False, "recompute", 8, "atomic"),
+    # the deterministic scatter: the forward (and its tapes) goes through the
+    # per-corner buffer and the CSR gather
+    (True, True, "store", 8, "gather"), (True, True, "recompute", 8, "gather"),
     # more than 32 iterations: the omega chain's table spans two warp scans
-    (True, True, "store", 40), (True, False, "store", 40)])
-def test_gpu_gradients_match_float64_adjoint(cheb, omega_grad, tape_memory, iters):
+    (True, True, "store", 40, "atomic"), (True, False, "store", 40, "atomic")])
+def test_gpu_gradients_match_float64_adjoint(cheb, omega_grad, tape_memory, iters, scatter):
     import torch
     from oracle.xpbd_adjoint import DiffOracle, lame_inverse, lame_inverse_grad
     from oracle.xpbd_oracle import OracleSdf
@@ -51,7 +56,8 @@ def test_gpu_gradients_match_float64_adjoint(cheb, omega_grad, tape_memory, iter
 
     sim = DiffSim(m, [PlaneSdf([0, 0, 0], [0, 1, 0], True), SphereSdf([0.42, -0.18, 0.42], 0.2, True),
                       CubeSdf([0.5, 0.0, 0.5], [0.1, 0.03, 0.2], False)], logE, nu, omega_grad=omega_grad,
-                  tape_memory=tape_memory, **kw)
+                  tape_memory=tape_memory, scatter=scatter, **kw)
+    assert sim.solver.scatter == scatter
     dev = torch.device("cuda")
     x0_t = torch.tensor(m.points, dtype=torch.float32, device=dev, requires_grad=True)
     v0_t = torch.tensor(v0, dtype=torch.float32, device=dev, requires_grad=True)
