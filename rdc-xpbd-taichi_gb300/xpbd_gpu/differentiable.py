@@ -166,9 +166,7 @@ class DiffSim:
 
     def __init__(self, rest_pose, sdf, log_E, nu, scatter="atomic", use_graphs=True, omega_grad=True,
                  tape_memory="auto", **kw):
-        kw.setdefault("block_neohookean_enable", True)
-        if not kw["block_neohookean_enable"]:
-            raise ValueError("the adjoint supports the block projection only")
+        _check_solver_kwargs(kw)
         log_E = np.asarray(log_E, dtype=np.float64)
         self.solver = XPBDNeoHookeanSolver(rest_pose, sdf, tet_young_modulus=np.exp(log_E),
                                            tet_poisson_ratio=np.asarray(nu, dtype=np.float64), scatter=scatter,
@@ -350,9 +348,7 @@ class BatchedDiffSim:
 
     def __init__(self, bodies, sdf, use_graphs=True, omega_grad=True, tape_memory="auto", **kw):
         from xpbd_gpu.batched import Body, XPBDBatchedSolver
-        kw.setdefault("block_neohookean_enable", True)
-        if not kw["block_neohookean_enable"]:
-            raise ValueError("the adjoint supports the block projection only")
+        _check_solver_kwargs(kw)
         bodies = [b if b.tet_young_modulus is not None else
                   Body(**dict(b.__dict__, tet_young_modulus=np.full(_n_tets(b.rest_pose), b.young_modulus)))
                   for b in bodies]
@@ -418,6 +414,16 @@ class BatchedDiffSim:
     def positions(self):
         s = self.batch
         return s._x4[s._vert_slot, :3].clone()
+
+
+def _check_solver_kwargs(kw):
+    """The adjoint reverses the block projection over a fixed number of
+    iterations (the library checks the same at every taped substep)."""
+    kw.setdefault("block_neohookean_enable", True)
+    if not kw["block_neohookean_enable"]:
+        raise ValueError("the adjoint supports the block projection only")
+    if kw.get("target_rel_residual", 0.0) > 0.0 or kw.get("residual_floor", 0.0) > 0.0:
+        raise ValueError("the adjoint needs a fixed iteration count: no target_rel_residual or residual_floor")
 
 
 def _check_tape_memory(mode):

@@ -38,3 +38,16 @@ def test_stored_tape_size(omega_grad):
     # the C5 workload: 64 bodies, 1.75 M tets, 20 iterations, 150 substeps -- about 80 GB
     big = _Tapes.nbytes(_Sim(348087, 1753152, 20, 64, True), 150)
     assert 7.0e10 < big < 9.0e10
+
+
+def test_solver_kwargs_are_checked():
+    """The adjoint reverses the block projection at a fixed iteration count:
+    the split projection and stop mode are refused before any device work."""
+    from xpbd_gpu.differentiable import _check_solver_kwargs
+    kw = {}
+    _check_solver_kwargs(kw)
+    assert kw["block_neohookean_enable"] is True
+    _check_solver_kwargs(dict(target_rel_residual=0.0, residual_floor=0.0))
+    for bad in (dict(block_neohookean_enable=False), dict(target_rel_residual=1e-3), dict(residual_floor=1e-6)):
+        with pytest.raises(ValueError):
+            _check_solver_kwargs(bad)

@@ -131,3 +131,31 @@ def test_omega_chain_table_matches_a_sequential_replay():
         want[j] = (1.0 / om, A, B, beta if upd else 0.0, c1, c2)
         prev = r
     np.testing.assert_allclose(table, want, rtol=1e-10, atol=1e-300)
+
+
+def test_unsupported_configurations_are_rejected():
+    """The adjoint covers the block projection at a fixed iteration count with
+    per-tet materials on the ATOMIC or GATHER layout.  The split projection and
+    stop mode fail in the constructor; stop mode switched on afterwards fails
+    at the next taped substep in the library (XPBD_ERR_INVALID_ARGUMENT); a
+    PATCH request takes the ATOMIC layout, as every solver with per-tet
+    materials does."""
+    from xpbd_gpu._native import STATUS_NAMES, XpbdError
+    from xpbd_gpu.differentiable import DiffSim
+    from xpbd_gpu.mesh import kuhn_grid
+    from xpbd_gpu.sdf import PlaneSdf
+    m = kuhn_grid(2, 2, 2, 0.1, origin=(0.3, 0.05, 0.3))
+    kw = dict(frame_dt=1 / 60, dt=1 / 60, substeps_num=1, constraints_iter=4, total_mass=1.0)
+    args = (m, [PlaneSdf([0, 0, 0], [0, 1, 0], True)], np.full(m.n_tets, np.log(1e5)), np.full(m.n_tets, 0.4))
+    with pytest.raises(ValueError, match="block"):
+        DiffSim(*args, block_neohookean_enable=False, **kw)
+    for stop in (dict(target_rel_residual=1e-3), dict(residual_floor=1e-6)):
+        with pytest.raises(ValueError, match="fixed iteration count"):
+            DiffSim(*args, **stop, **kw)
+    assert DiffSim(*args, scatter="patch", **kw).solver.scatter == "atomic"
+    sim = DiffSim(*args, use_graphs=False, tape_memory="recompute", **kw)
+    sim.solver.target_rel_residual = 1e-3
+    sim.solver._sync()
+    with pytest.raises(XpbdError, match="fixed iteration count") as e:
+        sim._tape(kw["dt"])
+    assert STATUS_NAMES[e.value.status] == "XPBD_ERR_INVALID_ARGUMENT"
