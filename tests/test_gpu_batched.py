@@ -174,3 +174,46 @@ def test_batch_monitoring_records_match_single_bodies():
         np.testing.assert_allclose(hb[k, :, 3], hs[:, 3], rtol=5e-3, atol=1e-6)
         recs = s.convergence_history[-K:]
         np.testing.assert_allclose([r["hydro_error"] for r in recs], hs[:, 2], rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("tpt", [1, 2])
+def test_batch_with_tiny_and_ragged_bodies(tpt):
+    """Bodies of 1, 6, 12 and 258 tets beside a larger one: a patch with a
+    single live tet, odd and even tet counts for the two-tets-per-thread
+    kernels, and a body whose second patch holds 2 tets.  Every body follows
+    its single-body solver within the parity tolerance, in free fall and in
+    contact (the plane, and for the 12-tet body a fixed sphere)."""
+    from xpbd_gpu.batched import Body, XPBDBatchedSolver
+    from xpbd_gpu.mesh import TetMesh, kuhn_grid
+    from xpbd_gpu.sdf import PlaneSdf, SphereSdf
+    tet = TetMesh(np.array([[0.0, 0.0, 0.0], [0.1, 0.0, 0.0], [0.0, 0.1, 0.0], [0.0, 0.0, 0.1]]) + [2.0, 0.05, 2.0],
+                  np.array([[0, 1, 2, 3]]))
+    meshes = [tet, kuhn_grid(1, 1, 1, 0.1, origin=(2.5, 0.06, 2.0)),
+              kuhn_grid(2, 1, 1, 0.1, origin=(3.0, 0.04, 2.0)),
+              kuhn_grid(43, 1, 1, 0.02, origin=(2.0, 0.03, 2.6), jitter=0.1, seed=6),
+              kuhn_grid(3, 2, 4, 0.1, origin=(0.0, 0.05, 0.0), jitter=0.1, seed=1)]
+    assert [m.n_tets for m in meshes] == [1, 6, 12, 258, 144]
+    bodies = [Body(m, young_modulus=E, poisson_ratio=0.4, total_mass=0.5)
+              for m, E in zip(meshes, (1e5, 3e5, 1e5, 2e5, 1e5))]
+    center, radius = np.array([3.1, -0.17, 2.05]), 0.2  # top at y = 0.03, under the 12-tet body
+    sdfs = lambda: [PlaneSdf([0, 0, 0], [0, 1, 0], True), SphereSdf(center.tolist(), radius, True)]
+    kw = dict(frame_dt=1 / 60, dt=1 / 60, substeps_num=3, constraints_iter=12, cheb_enable=True, cheb_warmup=4,
+              cheb_gamma=0.6666, block_neohookean_enable=True)
+    batch = XPBDBatchedSolver(bodies, sdfs(), tets_per_thread=tpt, **kw)
+    singles = [_single(b, sdfs, kw) for b in bodies]
+    for k, s in enumerate(singles):  # nothing starts inside the sphere (no pinned vertex)
+        assert (np.linalg.norm(s.mesh.verts.x.to_numpy() - center, axis=1) > radius).all()
+    contact = [False] * len(bodies)
+    for f in range(14):
+        batch.solve()
+        X = batch.positions()
+        for k, s in enumerate(singles):
+            s.solve()
+            x = s.mesh.verts.x.to_numpy()
+            diag = float(np.linalg.norm(x.max(0) - x.min(0)))
+            err = np.abs(X[batch.body_vert_slices[k]] - x).max()
+            assert err <= POS_TOL * diag, "frame %d body %d: %.3e" % (f, k, err)
+            gap = np.minimum(x[:, 1], np.linalg.norm(x - center, axis=1) - radius)
+            contact[k] |= bool(gap.min() < 2e-3)
+    batch.check_status()
+    assert all(contact), contact
