@@ -35,10 +35,16 @@ def make_solver(d, **over):
 
 @pytest.mark.parametrize("name", gc.golden_names())
 @pytest.mark.parametrize("scatter", ["atomic", "gather", "patch", "patch-tma", "patch-tma-1tpt", "patch-reduce",
-                                     "patch-1tpt", "patch-4tpt"])
+                                     "patch-1tpt", "patch-4tpt", "patch-128", "patch-64", "patch-64-1tpt"])
 def test_frames_match_reference(name, scatter):
     d = gc.load(name)
-    if scatter == "patch-tma":
+    if scatter.startswith(("patch-128", "patch-64")):
+        # the smaller patches the autotuner may pick (kernels compiled per patch size)
+        P = 128 if scatter.startswith("patch-128") else 64
+        s = make_solver(d, scatter="patch", patch_tets=P, tets_per_thread=1 if scatter.endswith("1tpt") else 2,
+                        monitor_convergence=False)
+        assert s.scatter == "patch" and s._patch_tets == P
+    elif scatter == "patch-tma":
         s = make_solver(d, scatter="patch", patch_pipeline=1, monitor_convergence=False)
     elif scatter == "patch-tma-1tpt":
         s = make_solver(d, scatter="patch", patch_pipeline=1, tets_per_thread=1, monitor_convergence=False)
