@@ -214,3 +214,45 @@ def test_pair_tets_leaves_unpairable_tets_last(native_lib):
     np.testing.assert_allclose(_signed_volumes(pts, new), _signed_volumes(pts, tets)[order], rtol=1e-12)
     with pytest.raises(Exception):
         _native.pair_tets(native_lib, np.array([[0, 1, 2, 13]]), 13)
+
+
+def test_batch_create_rejects_bad_arguments(native_lib):
+    """xpbd_batch_create checks its arguments before any device work, in this
+    order: NULL arguments, the SDF list, an empty batch, the padded sizes
+    (n_verts a multiple of 256, n_tets = 256 n_patches), NULL buffers,
+    half-given per-tet materials, max_records and the stop-mode parameters.
+    The pointers here are never dereferenced: each case fails a check first."""
+    prm = _native.XpbdParams()
+    prm.lame_mu = prm.lame_lambda = 1.0
+    b = _native.XpbdBatch()
+    sdf = (_native.XpbdSdf * 1)()
+    h = ctypes.c_void_p()
+
+    def create(n_sdf=1, sdfs=sdf, max_records=1):
+        st = native_lib.xpbd_batch_create(prm, b, sdfs, n_sdf, max_records, ctypes.byref(h))
+        assert h.value is None
+        return st, native_lib.xpbd_batch_last_error().decode()
+
+    assert native_lib.xpbd_batch_create(None, b, sdf, 1, 1, ctypes.byref(h)) == 1
+    assert create(n_sdf=0, sdfs=None)[0] == 4
+    sdf[0].kind = 3
+    assert create() == (1, "unknown SDF kind")
+    sdf[0].kind = 0
+    assert create() == (5, "empty batch")
+    b.n_bodies, b.n_verts, b.n_tets, b.n_patches = 1, 256, 300, 1
+    assert create()[0] == 5
+    b.n_verts, b.n_tets = 257, 256
+    assert create()[0] == 5
+    b.n_verts = 256
+    assert create() == (1, "NULL batch buffer")
+    for name, _ in _native.XpbdBatch._fields_[6:-3]:
+        setattr(b, name, 256)  # non-NULL, never read
+    b.tet_inv_mu = 256
+    assert create()[0] == 1 and "tet_inv_mu" in create()[1]
+    b.tet_inv_mu = None
+    assert create(max_records=-1) == (1, "max_records < 0")
+    prm.target_rel_residual = -1.0
+    assert create()[0] == 1
+    prm.target_rel_residual, prm.residual_floor = 0.0, float("nan")
+    assert create()[0] == 1
+    assert native_lib.xpbd_batch_destroy(None) == 0
