@@ -256,3 +256,19 @@ def test_batch_create_rejects_bad_arguments(native_lib):
     prm.target_rel_residual, prm.residual_floor = 0.0, float("nan")
     assert create()[0] == 1
     assert native_lib.xpbd_batch_destroy(None) == 0
+
+
+def test_tape_and_adjoint_entries_reject_missing_buffers(native_lib):
+    """The forward-with-tape and adjoint entries of both forms refuse a NULL
+    handle or a tape / adjoint without its required buffers
+    (XPBD_ERR_INVALID_ARGUMENT) before touching the device."""
+    tape, adj = _native.XpbdTape(), _native.XpbdAdjoint()
+    dt = ctypes.c_float(0.01)
+    for tape_fn, adj_fn, err in ((native_lib.xpbd_substep_tape, native_lib.xpbd_substep_adjoint,
+                                  native_lib.xpbd_last_error),
+                                 (native_lib.xpbd_batch_substep_tape, native_lib.xpbd_batch_substep_adjoint,
+                                  native_lib.xpbd_batch_last_error)):
+        assert tape_fn(None, dt, tape, None) == 1 and b"NULL" in err()
+        assert tape_fn(None, dt, None, None) == 1
+        assert adj_fn(None, dt, tape, adj, None) == 1 and b"NULL" in err()
+        assert adj_fn(None, dt, tape, None, None) == 1
