@@ -1442,7 +1442,9 @@ def run_profile(args):
     print("profile mode: %d frame(s) of %s" % (args.profile_frames, desc))
 
 
-def main():
+def make_parser():
+    """The command line of bench.py (also used to check the commands quoted in
+    the profile summaries)."""
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -1490,6 +1492,11 @@ def main():
     ap.add_argument("--profile-stop", type=int, default=0, choices=[0, 1], help="c3 profile mode: stop-mode frames")
     ap.add_argument("--profile-tape-memory", default="auto", choices=["auto", "store", "recompute"],
                     help="c5 profile mode: tapes stored by the forward or recomputed by the backward")
+    return ap
+
+
+def main():
+    ap = make_parser()
     args = ap.parse_args()
     if args.mode == "profile":
         run_profile(args)
